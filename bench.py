@@ -1,0 +1,482 @@
+"""Benchmark: EPG voxel·pulse·state updates/s on the MRF dictionary workload.
+
+Workload (one step): the 880-pulse MRF sequence (flip 5->60 deg over 300
+pulses, 60->2 deg over 300, 280 x 2 deg; TR 10 ms; inversion at t = 0) over a
+128 x 64 x 32 grid of T1 (geomspace 100-4000 ms) x T2 (geomspace 5-500 ms) x
+B1 (linspace 0.6-1.4) = 262,144 atoms, nstates 20, FP32, writing the
+complex64 signal AND the forward-mode Jacobian w.r.t. T1, T2 and B1 in one
+fused kernel pass. Atoms with T2 >= T1 are simulated like the rest (the count
+stays 262,144). Inputs are synthetic and seeded; the outputs (7.4 GB per step)
+are larger than L2, and an explicit 512 MB L2 flush runs between timed steps.
+
+Printed: one JSON line (rank 0). ``value`` is updates/s with inputs resident
+on the device; ``e2e`` is the same metric through the public API with the
+tissue copied in from pinned host memory and the signal and Jacobian copied
+back to pinned host memory inside the timed region. ``--impl reference`` times
+the reference's own CPU kernels (or, where they cannot be built, the oracle's
+FP32 port of them) on the host cores instead.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PULSES = 880
+STATES = 20
+GRID = (128, 64, 32)
+ATOMS = GRID[0] * GRID[1] * GRID[2]
+# Algorithmic FP32 FLOPs per voxel, pulse and order (FMA = 2): 18 for the
+# forward (relaxation 3, rotation 15) and 42 per forward-mode tangent.
+FLOPS_PER_UPDATE = 18 + 42 * 3
+WORKLOAD = "mrf_dictionary_fwd_jac"
+
+
+def mrf_schedule() -> np.ndarray:
+    return np.concatenate(
+        [np.linspace(5, 60, 300), np.linspace(60, 2, 300), np.full(280, 2.0)]
+    ).astype(np.float32)
+
+
+def dictionary_grid():
+    t1 = np.geomspace(100, 4000, GRID[0]).astype(np.float32)
+    t2 = np.geomspace(5, 500, GRID[1]).astype(np.float32)
+    b1 = np.linspace(0.6, 1.4, GRID[2]).astype(np.float32)
+    T1, T2, B1 = np.meshgrid(t1, t2, b1, indexing="ij")
+    return T1.ravel().copy(), T2.ravel().copy(), B1.ravel().copy()
+
+
+def config(extra=None):
+    c = {
+        "workload": WORKLOAD,
+        "sequence": "MRF inversion + 880 pulses (5-60-2 deg), TR 10 ms",
+        "atoms": ATOMS,
+        "grid": "T1 geomspace(100,4000,128) x T2 geomspace(5,500,64) x B1 linspace(0.6,1.4,32)",
+        "nstates": STATES,
+        "jacobian": ["T1", "T2", "B1"],
+        "outputs": "complex64 signal (262144,880) + Jacobian (262144,3,880)",
+        "l2": "512 MB flush between timed steps; outputs 7.4 GB per step exceed L2",
+        "parallelism": "replicas",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---- clocks -----------------------------------------------------------------
+
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9], strict=False):
+                if flag.lower() in ("active", "1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- the GPU arm ------------------------------------------------------------
+
+
+def fp32_peak(torch, lib, device) -> float:
+    """FP32 FLOP/s of the FMA probe kernel on this GPU (best of 5)."""
+    import ctypes
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    out = torch.zeros(blocks, device=device)
+    stream = torch.cuda.current_stream().cuda_stream
+    flops = ctypes.c_double()
+    best = 0.0
+    for _ in range(6):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        rc = lib.tsg_probe_fp32(blocks, threads, iters, out.data_ptr(), stream, ctypes.byref(flops))
+        e.record()
+        e.synchronize()
+        if rc != 0:
+            raise RuntimeError("fp32 probe failed")
+        best = max(best, flops.value / (s.elapsed_time(e) * 1e-3))
+    return best
+
+
+def traffic_per_launch() -> float | None:
+    """DRAM bytes per launch of the fused dictionary kernel, from the
+    committed ncu summary (profiles/), if one has been recorded."""
+    path = ROOT / "profiles" / "sweep_t12b_mrf_dictionary.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def run_gpu(args, rank: int, world: int, dist) -> dict | None:
+    import torch
+
+    from torchsim_gb300 import _native, engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    lib = _native.library()
+    flip = mrf_schedule()
+    events = mrf_events(flip, 10.0)
+    program = program_for(events, device)
+    t1, t2, b1 = dictionary_grid()
+    tissue = engine.tissue_maps(device, ATOMS, torch.from_numpy(t1), torch.from_numpy(t2), None,
+                                torch.from_numpy(b1), None)
+    names = ("T1", "T2", "B1")
+    sig = torch.empty((ATOMS, PULSES), dtype=torch.complex64, device=device)
+    jac = torch.empty((ATOMS, 3, PULSES), dtype=torch.complex64, device=device)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    launch = tuple(args.launch) if args.launch else None
+
+    def step():
+        engine.forward_tangents(program, tissue, STATES, names, sig_out=sig, jac_out=jac,
+                                launch=launch)
+
+    for _ in range(args.warmup):
+        step()
+        flush.zero_()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            starts[i].record()
+            step()
+            ends[i].record()
+            flush.zero_()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends, strict=True)]
+    total_s = sum(step_ms) * 1e-3
+    if dist is not None:
+        t = torch.tensor([total_s], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    updates = float(ATOMS) * PULSES * STATES
+    value = updates * args.steps * world / total_s
+    kernel_s = total_s / args.steps
+
+    # Plain form: the reference's call pattern on the GPU -- one forward pass,
+    # then one forward+tangent pass per Jacobian column (torch.func.jvp per
+    # property, model/_signal.py:233-268) -- through the same kernels.
+    plain = None
+    if rank == 0 and not args.skip_plain:
+        one = torch.empty((ATOMS, 1, PULSES), dtype=torch.complex64, device=device)
+        def plain_step():
+            engine.forward(program, tissue, STATES, out=sig)
+            for name in names:
+                engine.forward_tangents(program, tissue, STATES, (name,), sig_out=sig,
+                                        jac_out=one)
+        plain_step()
+        torch.cuda.synchronize()
+        ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ps.record()
+        for _ in range(max(1, args.steps // 2)):
+            plain_step()
+        pe.record()
+        pe.synchronize()
+        plain_s = ps.elapsed_time(pe) * 1e-3 / max(1, args.steps // 2)
+        plain = {"value": updates / plain_s, "ms_per_step": plain_s * 1e3,
+                 "launches_per_step": 4,
+                 "form": "forward + one forward-and-tangent pass per column (T1, T2, B1)"}
+        del one
+
+    # End to end through the public API: pinned host tissue in, pinned host
+    # signal and Jacobian out, copies inside the timed region.
+    e2e = None
+    if rank == 0:
+        host_t = [torch.from_numpy(a).pin_memory() for a in (t1, t2, b1)]
+        host_sig = torch.empty((ATOMS, PULSES), dtype=torch.complex64).pin_memory()
+        host_jac = torch.empty((ATOMS, 3, PULSES), dtype=torch.complex64).pin_memory()
+
+        def e2e_step():
+            dev_t = [h.to(device, non_blocking=True) for h in host_t]
+            maps = engine.TissueMaps(dev_t[0], dev_t[1], None, dev_t[2], None)
+            engine.forward_tangents(program, maps, STATES, names, sig_out=sig, jac_out=jac,
+                                    launch=launch)
+            host_sig.copy_(sig, non_blocking=True)
+            host_jac.copy_(jac, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        n_e2e = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        e2e = {"value": updates / e2e_s, "unit": "updates/s", "ms_per_step": e2e_s * 1e3,
+               "h2d_bytes_per_step": 3 * ATOMS * 4,
+               "d2h_bytes_per_step": int(host_sig.numel() * 8 + host_jac.numel() * 8),
+               "api": "engine.forward_tangents with pinned host tissue and outputs"}
+        del host_sig, host_jac
+
+    if rank != 0:
+        return None
+    peak = fp32_peak(torch, lib, device)
+    flops = float(ATOMS) * PULSES * STATES * FLOPS_PER_UPDATE
+    out_bytes = float(sig.numel() * 8 + jac.numel() * 8)
+    in_bytes = 3.0 * ATOMS * 4
+    hbm_peak = None
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    if peaks_path.exists():
+        hbm_peak = json.loads(peaks_path.read_text()).get("hbm_gbs")
+    hbm_peak = hbm_peak or 6800.0
+    achieved = flops / kernel_s / 1e12
+    traffic = traffic_per_launch()
+    clk = clocks.summary()
+    line = {
+        "metric": "EPG voxel·pulse·state updates/s (fused forward + Jacobian T1/T2/B1)",
+        "value": value,
+        "unit": "updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": kernel_s * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded grid of the named shape)",
+        "config": config(),
+        "roofline": {
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": peak / 1e12,
+            "unit": "TFLOP/s",
+            "frac": achieved * 1e12 / peak,
+            "traffic": traffic,
+            "peak_source": "measured: FP32 FMA probe kernel on this GPU in this run",
+            "flops_per_launch": flops,
+            "hbm": {"achieved_gbs": (out_bytes + in_bytes) / kernel_s / 1e9,
+                    "peak_gbs": hbm_peak,
+                    "frac": (out_bytes + in_bytes) / kernel_s / 1e9 / hbm_peak,
+                    "algorithmic_bytes_per_launch": out_bytes + in_bytes,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
+        },
+        "e2e": e2e,
+        "plain_form": plain,
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "wall_s_timed_region": wall,
+    }
+    if not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
+    return line
+
+
+# ---- CPU baselines ----------------------------------------------------------
+
+
+def _reference_module():
+    """The reference's own compiled CPU kernel (oracle/_ref), if it loads here."""
+    import importlib.util
+
+    for path in sorted((ROOT / "oracle" / "_ref").glob("_epg_cpu*.so")):
+        try:
+            spec = importlib.util.spec_from_file_location("_epg_cpu", path)
+            module = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(module)
+            return module
+        except (ImportError, OSError):
+            continue
+    return None
+
+
+def cpu_run(sample: int, threads: int):
+    """Forward + one tangent pass per Jacobian column (the reference's call
+    pattern) over the first `sample` atoms of the grid. Returns (seconds, kind)."""
+    from torchsim_gb300.sequence import mrf_events
+
+    t1, t2, b1 = (a[:sample].copy() for a in dictionary_grid())
+    ev = mrf_events(mrf_schedule(), 10.0)
+    ref = _reference_module()
+    if ref is not None:
+        E = ev.events
+        zeros = np.zeros(sample, np.float32)
+        ones = np.ones(sample, np.float32)
+        tissue = [t1, t2, ones, b1, zeros, zeros, ones, *([zeros] * 10)]
+        events = [np.ascontiguousarray(ev.duration[0]), ev.kind, np.ascontiguousarray(ev.flip[0]),
+                  np.ascontiguousarray(ev.phase[0]), ev.action, ev.output_index,
+                  np.zeros(E, np.int32), np.zeros(E, np.float32), np.zeros(E, np.float32)]
+        out_r = np.zeros((sample, PULSES), np.float32)
+        out_i = np.zeros((sample, PULSES), np.float32)
+        features = 8  # transmit only: m0 and inversion at identity
+        common = (sample, 1, E, STATES, PULSES, threads, 1, 0.0, 0.0, 1, 1, 0, 1.0, 0, 1.0, 0,
+                  features, 0, 0, 0)
+        t0 = time.perf_counter()
+        ref.simulate([a.ctypes.data for a in (*tissue, *events, out_r, out_i)] + [0] * 13, *common)
+        for col in (0, 1, 3):
+            tan = [zeros] * 17 + [np.zeros(E, np.float32)] * 3
+            tan = list(tan)
+            tan[col] = ones
+            ref.simulate_jvp([a.ctypes.data for a in (*tissue, *events, *tan, out_r, out_i)]
+                             + [0] * 13, *common)
+        return time.perf_counter() - t0, "reference"
+    from oracle import oracle as O
+
+    p = O.Packed(t1, t2, ev.duration, ev.kind, ev.flip, ev.action, ev.output_index, STATES, b1=b1)
+    t0 = time.perf_counter()
+    O.forward(p, "f32", threads=threads)
+    for key in ("t1_ms", "t2_ms", "b1"):
+        O.tangent(p, "f32", threads=threads, **{key: 1.0})
+    return time.perf_counter() - t0, "port"
+
+
+def cpu_baseline(sample: int) -> dict:
+    from oracle import oracle as O
+
+    threads = O.cpu_threads()
+    seconds, kind = cpu_run(sample, threads)
+    return {"value": float(sample) * PULSES * STATES / seconds, "unit": "updates/s",
+            "cores": threads, "kind": kind,
+            "sample": f"first {sample} of the {ATOMS} grid atoms, forward + 3 tangent passes "
+                      f"(the reference's per-column call pattern), {seconds:.2f} s"}
+
+
+def run_reference(args, rank: int) -> dict | None:
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+
+    threads = O.cpu_threads()
+    cpu_run(min(args.cpu_sample, 1024), threads)  # warm the pages and caches
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_run(min(args.cpu_sample, 2048), threads)
+    times = []
+    kind = "port"
+    for _ in range(args.steps):
+        seconds, kind = cpu_run(args.cpu_sample, threads)
+        times.append(seconds)
+    total = sum(times)
+    value = float(args.cpu_sample) * PULSES * STATES * args.steps / total
+    return {
+        "impl": "reference",
+        "metric": "EPG voxel·pulse·state updates/s (fused forward + Jacobian T1/T2/B1)",
+        "value": value,
+        "unit": "updates/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded grid of the named shape)",
+        "config": config({"sample_atoms_per_step": args.cpu_sample}),
+        "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": kind,
+                         "sample": f"{args.cpu_sample} of {ATOMS} atoms per step, forward + "
+                                   "3 tangent passes"},
+        "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--launch", type=int, nargs=3, metavar=("LANES", "ORDERS", "WARPS"))
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group("nccl")
+        dist = tdist
+    line = run_gpu(args, rank, world, dist)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/*
+ * torchsim_gb300 — C ABI of the GB300 (sm_103a) extended-phase-graph kernels.
+ *
+ * Two families of entry points:
+ *
+ *  1. Drop-ins for the reference's own native boundary, the CPython functions
+ *     of src/torchsim/_epg_cpu.cpp (module table at :11757). They take the
+ *     same pointer sequences in the same order — the packed buffers of
+ *     sequence/_parameters.py:105-195, then the output/tangent/gradient
+ *     slots — as HOST pointers, copy to the device, run, and copy back before
+ *     returning, so a caller that binds _epg_cpu.simulate can bind these
+ *     instead. Only the real-subspace, single-pool, instant-RF subset is
+ *     served (real_axis == 1; no pools, tables, per-voxel pulses, diffusion,
+ *     flow); anything else returns TSG_ERR_UNSUPPORTED.
+ *
+ *  2. Device-resident entry points used by the Python package: a compiled
+ *     pulse program (tsg_program) plus DEVICE pointers and a CUDA stream.
+ *     They are stream-ordered and do not synchronise the host.
+ *
+ * Every function returns TSG_OK (0) or a negative TSG_ERR_* code; the message
+ * of the last failure on the calling thread is tsg_last_error().
+ */
+#ifndef TORCHSIM_GB300_H
+#define TORCHSIM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    TSG_OK = 0,
+    TSG_ERR_ARGUMENT = -1,    /* bad sizes or null pointers: the reference's ValueError */
+    TSG_ERR_UNSUPPORTED = -2, /* outside the real-subspace single-pool subset */
+    TSG_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+    TSG_ERR_CAPACITY = -4     /* a size beyond a stated maximum */
+};
+
+/* Output layouts of the device entry points. */
+enum {
+    /* Two float planes (real, imaginary) as the reference's kernels write
+     * them: real plane 0, imaginary plane m0*F+[0] (_epg_cpu.cpp:3111-3115). */
+    TSG_LAYOUT_PLANES = 0,
+    /* One interleaved complex64 array holding 1j * signal, which is what
+     * MRFSimulator.evaluate returns (simulators/mrf.py:84): (-m0*F+[0], 0). */
+    TSG_LAYOUT_COMPLEX_IJ = 1
+};
+
+/* Structured forward-mode directions the fused kernel carries in one pass. */
+enum {
+    TSG_TANGENT_T1 = 1,
+    TSG_TANGENT_T2 = 2,
+    TSG_TANGENT_B1 = 4,
+    TSG_TANGENT_INVERSION = 8
+};
+
+/* Per-voxel tissue, DEVICE pointers, atom_count floats each. m0, b1 and
+ * inversion may be null for their identity value 1, as the reference's
+ * feature mask leaves an undeclared property out (_epg_cpu.cpp:91-104). */
+typedef struct {
+    const float* t1_ms;
+    const float* t2_ms;
+    const float* m0;
+    const float* b1;
+    const float* inversion;
+} tsg_tissue;
+
+/* One general forward-mode direction (DEVICE pointers, all nullable):
+ * per atom t1/t2/m0/b1/inversion, per (train, event) duration/flip. The
+ * same directions simulate_real_jvp_range follows (_epg_cpu.cpp:3136-3285). */
+typedef struct {
+    const float* t1_ms;
+    const float* t2_ms;
+    const float* m0;
+    const float* b1;
+    const float* inversion;
+    const float* duration_s;
+    const float* flip_rad;
+} tsg_direction;
+
+/* Gradients the adjoint adds into (DEVICE pointers, nullable). Per atom:
+ * t1/t2/m0/b1/inversion; per (train, event): flip and duration. The slots
+ * simulate_real_vjp_range fills (_epg_cpu.cpp:6223-6231, 6180, 6217). */
+typedef struct {
+    float* t1_ms;
+    float* t2_ms;
+    float* m0;
+    float* b1;
+    float* inversion;
+    float* flip_rad;
+    float* duration_s;
+} tsg_gradients;
+
+/* Launch shape. Zero fields are chosen by the built-in heuristic (or the
+ * tuned table installed with tsg_tune_set). lanes_per_voxel spreads the
+ * F+/F-/Z orders of one voxel over that many warp lanes; orders_per_lane is
+ * how many orders each lane keeps in registers; warps_per_block sets the
+ * voxels per CTA. */
+typedef struct {
+    int lanes_per_voxel;
+    int orders_per_lane;
+    int warps_per_block;
+} tsg_launch;
+
+typedef struct tsg_program tsg_program;
+
+/* ---- diagnostics ------------------------------------------------------- */
+
+const char* tsg_last_error(void);
+int tsg_version(void);
+
+/* Launches an FP32 FMA-throughput probe (blocks x threads, each running
+ * eight independent FMA chains for 32*iters steps) on `stream`, and reports
+ * the FLOPs it performs; timed by the caller with events, it gives the
+ * FP32 CUDA-core peak that bounds the sweep kernels. `out` (blocks floats,
+ * device) is written only to keep the chains live. No reference
+ * counterpart: a measurement aid. */
+int tsg_probe_fp32(int64_t blocks, int threads, int iters, float* out, void* stream,
+                   double* flops);
+
+/* ---- pulse programs ---------------------------------------------------- */
+
+/* Compiles the reference's packed event stream (HOST pointers) into a device
+ * pulse program. Layout as _pack_events writes it (sequence/_accelerators.py:
+ * 913-1170): duration_s and flip_rad are (train_count, event_count); kind,
+ * action and output_index are (event_count). Events with zero duration are
+ * folded into the op before them (exact: exp(0) = 1). unmerged != 0 keeps one
+ * op per event with its relaxation step, which the per-event duration
+ * gradients of tsg_epg_simulate_vjp need. duration_tangent (nullable, HOST,
+ * train_count*event_count) keeps an op boundary wherever a zero-duration
+ * event carries a duration direction. Allocates device memory. */
+int tsg_program_create(const float* duration_s, const int32_t* kind, const float* flip_rad,
+                       const uint8_t* action, const int32_t* output_index,
+                       int64_t train_count, int64_t event_count, int unmerged,
+                       const float* duration_tangent, tsg_program** out);
+int tsg_program_destroy(tsg_program* program);
+/* The same compilation on the host only, for inspection: writes the op
+ * count per train, the output count and up to `capacity` ops (all trains,
+ * train-major) as dt, flip, record index and micro-step code words (bit
+ * layout: relax 0, shifts-before-RF 1-2, RF kind 3-4 (1 rotate, 2 invert),
+ * shifts-after-RF 5-6, spoil 7, record 8, shifts-after-record 9-10,
+ * spoil 11). Needs no GPU. */
+int tsg_program_plan(const float* duration_s, const int32_t* kind, const float* flip_rad,
+                     const uint8_t* action, const int32_t* output_index, int64_t train_count,
+                     int64_t event_count, int unmerged, const float* duration_tangent,
+                     int64_t* op_count, int64_t* output_count, float* dt_out, float* flip_out,
+                     int32_t* record_out, uint32_t* code_out, int64_t capacity);
+/* op_count: ops per train; output_count: recorded samples per train. */
+int tsg_program_info(const tsg_program* program, int64_t* train_count, int64_t* op_count,
+                     int64_t* output_count, int64_t* event_count);
+
+/* ---- device-resident kernels ------------------------------------------- */
+
+/* Forward. Signal layout (train, atom, output); see TSG_LAYOUT_*. For
+ * TSG_LAYOUT_PLANES out_b is the imaginary plane; for COMPLEX_IJ out_b is
+ * unused. Follows simulate_real_range (_epg_cpu.cpp:3041-3128). */
+int tsg_epg_forward(const tsg_program* program, const tsg_tissue* tissue, int64_t atom_count,
+                    int64_t state_count, int layout, float* out_a, float* out_b,
+                    const tsg_launch* launch, void* stream);
+
+/* Fused forward plus structured tangents in ONE pass (replaces the
+ * reference's k x (forward + jvp) launches of model/_signal.py:233-268).
+ * tangent_mask: TSG_TANGENT_* bits. columns[5]: Jacobian column of the T1, T2,
+ * B1, inversion and M0 derivatives (-1 = not stored); column_count = K. The
+ * signal goes to sig_a/sig_b (nullable), the Jacobian to jac_a/jac_b as
+ * (train, atom, K, output). */
+int tsg_epg_forward_tangents(const tsg_program* program, const tsg_tissue* tissue,
+                             int64_t atom_count, int64_t state_count, unsigned tangent_mask,
+                             const int32_t* columns, int32_t column_count, int layout,
+                             float* sig_a, float* sig_b, float* jac_a, float* jac_b,
+                             const tsg_launch* launch, void* stream);
+
+/* One general direction (the reference's simulate_jvp): writes the tangent
+ * of the recorded samples only, planes layout, (train, atom, output). The
+ * program must have been compiled with this direction's duration tangent. */
+int tsg_epg_tangent(const tsg_program* program, const tsg_tissue* tissue, int64_t atom_count,
+                    int64_t state_count, const tsg_direction* direction, float* out_real,
+                    float* out_imag, const tsg_launch* launch, void* stream);
+
+/* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */
+
+/* _epg_cpu.simulate (src/torchsim/_epg_cpu.cpp:10740-10926): pointers holds
+ * the 26 packed buffers, the two output planes and the 13 tail slots (41
+ * entries, :10794). Synchronous. */
+int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, int64_t atom_count,
+                     int64_t train_count, int64_t event_count, int64_t state_count,
+                     int64_t output_count, int real_axis, int features);
+
+/* _epg_cpu.simulate_jvp (src/torchsim/_epg_cpu.cpp:11017-11148): 26 packed
+ * buffers, 20 tangents (the differentiable inputs, FLOAT_INPUTS order of
+ * sequence/_parameters.py:206), two output planes, 13 tail slots (61). */
+int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
+                         int64_t train_count, int64_t event_count, int64_t state_count,
+                         int64_t output_count, int real_axis, int features);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHSIM_GB300_H */

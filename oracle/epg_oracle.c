@@ -1,0 +1,506 @@
+/*
+ * ORACLE — test infrastructure only. Nothing in the product links or calls
+ * this file; only tests/, the smoke check and bench.py's CPU-baseline leg do,
+ * and only as the checker or the timed CPU baseline.
+ *
+ * A plain-C restatement of torchsim's real-subspace extended-phase-graph
+ * (EPG) state machine over the reference's packed event buffers. It is
+ * compiled twice from this one source:
+ *
+ *   REAL=double  the FP64 oracle every CUDA result is judged against;
+ *   REAL=float   an FP32 port that keeps the reference's statement order so
+ *                that, built with -ffp-contract=off like the reference
+ *                (CMakeLists.txt:48-53), it reproduces the reference's own CPU
+ *                kernel; it is the "port" CPU baseline where the reference
+ *                cannot be built (the GPU host).
+ *
+ * What each function follows in the reference (src/torchsim/_epg_cpu.cpp):
+ *   shift                 shift_real                       3010-3027
+ *   shift_adjoint         shift_real_adjoint               5950-5971
+ *   run_forward           simulate_real_range              3041-3128
+ *   run_tangent           simulate_real_jvp_range          3136-3285
+ *   run_adjoint           simulate_real_vjp_range          5985-6232
+ * Action bits are the packed action word (_epg_cpu.cpp:36-41,
+ * sequence/_accelerators.py:77-84). Event kinds: 0 wait, 1 RF, 2 ADC
+ * (sequence/_description.py:31-36). The work range enumerates (train, atom)
+ * train-major and the output row of a work item is (train*atoms+atom)
+ * (_epg_cpu.cpp:278-296).
+ *
+ * Out of scope, as in the real-subspace kernels: diffusion damping, flow,
+ * pools, shaped/dynamic RF, off-resonance and RF phase (which leave the real
+ * subspace). Null tissue pointers stand for the identity value (m0 = b1 =
+ * inversion efficiency = 1), as the reference's feature mask does.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef REAL
+#define REAL double
+#endif
+#ifndef SUFFIX
+#define SUFFIX f64
+#endif
+#define GLUE2(a, b) a##_##b
+#define GLUE(a, b) GLUE2(a, b)
+#define NAME(x) GLUE(x, SUFFIX)
+
+#if defined(REAL_IS_FLOAT)
+#define EXP expf
+#define COS cosf
+#define SIN sinf
+#define LIT(x) x##F
+#else
+#define EXP exp
+#define COS cos
+#define SIN sin
+#define LIT(x) x
+#endif
+
+enum {
+    A_PRE_SHIFT = 1,
+    A_POST_SHIFT = 2,
+    A_INVERSION = 4,
+    A_SPOIL_AFTER = 8,
+    A_SHIFT_AFTER = 16,
+    A_RECORD = 32,
+};
+
+/* The inputs one run reads. Tissue arrays have atom_count entries; duration
+ * and flip have train_count*event_count; kind, action and output_index have
+ * event_count. */
+typedef struct {
+    const float* t1_ms;
+    const float* t2_ms;
+    const float* m0;         /* nullable: 1 */
+    const float* b1;         /* nullable: 1 */
+    const float* inversion;  /* nullable: 1 */
+    const float* duration_s;
+    const int32_t* kind;
+    const float* flip_rad;
+    const uint8_t* action;
+    const int32_t* output_index;
+    int64_t atom_count;
+    int64_t train_count;
+    int64_t event_count;
+    int64_t state_count;
+    int64_t output_count;
+} oracle_case;
+
+/* One forward-mode direction: each pointer nullable (zero direction). */
+typedef struct {
+    const float* t1_ms;
+    const float* t2_ms;
+    const float* m0;
+    const float* b1;
+    const float* inversion;
+    const float* duration_s;
+    const float* flip_rad;
+} oracle_direction;
+
+static inline REAL tissue(const float* p, int64_t atom, REAL identity) {
+    return p ? (REAL)p[atom] : identity;
+}
+
+/* F+ takes order k-1, F- takes order k+1, the top F- order is lost and
+ * F+[0] is the conjugate of the new F-[0], which in the real subspace is its
+ * negative (_epg_cpu.cpp:3010-3027). */
+static void shift(REAL* plus, REAL* minus, int64_t states) {
+    for (int64_t s = 0; s + 1 < states; ++s) minus[s] = minus[s + 1];
+    minus[states - 1] = LIT(0.0);
+    for (int64_t s = states - 1; s > 0; --s) plus[s] = plus[s - 1];
+    plus[0] = -minus[0];
+}
+
+/* Transpose of shift (_epg_cpu.cpp:5950-5971). */
+static void shift_adjoint(REAL* plus_bar, REAL* minus_bar, int64_t states) {
+    const REAL carry = -plus_bar[0];
+    for (int64_t s = 0; s + 1 < states; ++s) plus_bar[s] = plus_bar[s + 1];
+    plus_bar[states - 1] = LIT(0.0);
+    for (int64_t s = states - 1; s > 0; --s) minus_bar[s] = minus_bar[s - 1];
+    minus_bar[0] = LIT(0.0);
+    if (states > 1) minus_bar[1] += carry;
+}
+
+/* Forward over work items [begin, end). Output planes as the reference's:
+ * real plane written 0, imaginary plane m0*F+[0]. */
+static void run_forward(const oracle_case* c, int64_t begin, int64_t end,
+                        REAL* out_real, REAL* out_imag) {
+    const int64_t S = c->state_count;
+    REAL* plus = (REAL*)calloc((size_t)(3 * S), sizeof(REAL));
+    REAL* minus = plus + S;
+    REAL* lon = minus + S;
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / c->atom_count;
+        const int64_t atom = work % c->atom_count;
+        const float* duration = c->duration_s + train * c->event_count;
+        const float* flip = c->flip_rad + train * c->event_count;
+        const int64_t out_base = (train * c->atom_count + atom) * c->output_count;
+        memset(plus, 0, sizeof(REAL) * (size_t)(3 * S));
+        lon[0] = LIT(1.0);
+        const REAL r1 = LIT(1000.0) / (REAL)c->t1_ms[atom];
+        const REAL r2 = LIT(1000.0) / (REAL)c->t2_ms[atom];
+        const REAL b1 = tissue(c->b1, atom, LIT(1.0));
+        const REAL m0 = tissue(c->m0, atom, LIT(1.0));
+        const REAL eff = tissue(c->inversion, atom, LIT(1.0));
+        for (int64_t e = 0; e < c->event_count; ++e) {
+            const REAL dt = (REAL)duration[e];
+            const REAL e1 = EXP(-r1 * dt);
+            const REAL e2 = EXP(-r2 * dt);
+            for (int64_t s = 0; s < S; ++s) {
+                plus[s] *= e2;
+                minus[s] *= e2;
+                lon[s] *= e1;
+            }
+            lon[0] += LIT(1.0) - e1;
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) shift(plus, minus, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    const REAL f = -eff;
+                    for (int64_t s = 0; s < S; ++s) lon[s] *= f;
+                } else {
+                    const REAL alpha = (REAL)flip[e] * b1;
+                    const REAL co = COS(alpha);
+                    const REAL si = SIN(alpha);
+                    const REAL ch = LIT(0.5) * (LIT(1.0) + co);
+                    const REAL sh = LIT(0.5) * (LIT(1.0) - co);
+                    const REAL hs = LIT(0.5) * si;
+                    for (int64_t s = 0; s < S; ++s) {
+                        const REAL p = plus[s], m = minus[s], z = lon[s];
+                        plus[s] = ch * p + sh * m - si * z;
+                        minus[s] = sh * p + ch * m + si * z;
+                        lon[s] = hs * p - hs * m + co * z;
+                    }
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                const int64_t idx = out_base + c->output_index[e];
+                out_real[idx] = LIT(0.0);
+                out_imag[idx] = m0 * plus[0];
+            }
+            if (a & A_POST_SHIFT) shift(plus, minus, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) plus[s] = minus[s] = LIT(0.0);
+            } else if (a & A_SHIFT_AFTER) {
+                shift(plus, minus, S);
+            }
+        }
+    }
+    free(plus);
+}
+
+/* One forward-mode tangent, written as the tangent of the recorded sample
+ * only (_epg_cpu.cpp:3136-3285). */
+static void run_tangent(const oracle_case* c, const oracle_direction* d,
+                        int64_t begin, int64_t end, REAL* out_real, REAL* out_imag) {
+    const int64_t S = c->state_count;
+    REAL* buf = (REAL*)calloc((size_t)(6 * S), sizeof(REAL));
+    REAL *plus = buf, *minus = buf + S, *lon = buf + 2 * S;
+    REAL *dp_ = buf + 3 * S, *dm_ = buf + 4 * S, *dz_ = buf + 5 * S;
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / c->atom_count;
+        const int64_t atom = work % c->atom_count;
+        const int64_t ebase = train * c->event_count;
+        const float* duration = c->duration_s + ebase;
+        const float* flip = c->flip_rad + ebase;
+        const int64_t out_base = (train * c->atom_count + atom) * c->output_count;
+        memset(buf, 0, sizeof(REAL) * (size_t)(6 * S));
+        lon[0] = LIT(1.0);
+        const REAL t1 = (REAL)c->t1_ms[atom];
+        const REAL t2 = (REAL)c->t2_ms[atom];
+        const REAL r1 = LIT(1000.0) / t1;
+        const REAL r2 = LIT(1000.0) / t2;
+        const REAL b1 = tissue(c->b1, atom, LIT(1.0));
+        const REAL m0 = tissue(c->m0, atom, LIT(1.0));
+        const REAL eff = tissue(c->inversion, atom, LIT(1.0));
+        const REAL dt1 = tissue(d->t1_ms, atom, LIT(0.0));
+        const REAL dt2 = tissue(d->t2_ms, atom, LIT(0.0));
+        const REAL db1 = c->b1 ? tissue(d->b1, atom, LIT(0.0)) : LIT(0.0);
+        const REAL dm0 = tissue(d->m0, atom, LIT(0.0));
+        const REAL deff = c->inversion ? tissue(d->inversion, atom, LIT(0.0)) : LIT(0.0);
+        for (int64_t e = 0; e < c->event_count; ++e) {
+            const REAL dt = (REAL)duration[e];
+            const REAL ddt = d->duration_s ? (REAL)d->duration_s[ebase + e] : LIT(0.0);
+            const REAL e1 = EXP(-r1 * dt);
+            const REAL e2 = EXP(-r2 * dt);
+            const REAL e1t = e1 * (LIT(1000.0) * dt * dt1 / (t1 * t1) - r1 * ddt);
+            const REAL e2t = e2 * (LIT(1000.0) * dt * dt2 / (t2 * t2) - r2 * ddt);
+            for (int64_t s = 0; s < S; ++s) {
+                dp_[s] = dp_[s] * e2 + plus[s] * e2t;
+                plus[s] *= e2;
+                dm_[s] = dm_[s] * e2 + minus[s] * e2t;
+                minus[s] *= e2;
+                dz_[s] = dz_[s] * e1 + lon[s] * e1t;
+                lon[s] *= e1;
+            }
+            lon[0] += LIT(1.0) - e1;
+            dz_[0] -= e1t;
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) {
+                shift(plus, minus, S);
+                shift(dp_, dm_, S);
+            }
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    const REAL f = -eff;
+                    const REAL ft = -deff;
+                    for (int64_t s = 0; s < S; ++s) {
+                        dz_[s] = dz_[s] * f + lon[s] * ft;
+                        lon[s] *= f;
+                    }
+                } else {
+                    const REAL fl = (REAL)flip[e];
+                    const REAL dfl = d->flip_rad ? (REAL)d->flip_rad[ebase + e] : LIT(0.0);
+                    const REAL alpha = fl * b1;
+                    const REAL at = dfl * b1 + fl * db1;
+                    const REAL co = COS(alpha), si = SIN(alpha);
+                    const REAL ch = LIT(0.5) * (LIT(1.0) + co);
+                    const REAL sh = LIT(0.5) * (LIT(1.0) - co);
+                    const REAL hs = LIT(0.5) * si;
+                    const REAL cot = -si * at, sit = co * at;
+                    const REAL cht = LIT(-0.5) * si * at;
+                    const REAL sht = LIT(0.5) * si * at;
+                    const REAL hst = LIT(0.5) * co * at;
+                    for (int64_t s = 0; s < S; ++s) {
+                        const REAL p = plus[s], m = minus[s], z = lon[s];
+                        const REAL dp = dp_[s], dm = dm_[s], dz = dz_[s];
+                        dp_[s] = ch * dp + cht * p + sh * dm + sht * m - si * dz - sit * z;
+                        dm_[s] = sh * dp + sht * p + ch * dm + cht * m + si * dz + sit * z;
+                        dz_[s] = hs * dp + hst * p - hs * dm - hst * m + co * dz + cot * z;
+                        plus[s] = ch * p + sh * m - si * z;
+                        minus[s] = sh * p + ch * m + si * z;
+                        lon[s] = hs * p - hs * m + co * z;
+                    }
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                const int64_t idx = out_base + c->output_index[e];
+                out_real[idx] = LIT(0.0);
+                out_imag[idx] = dm0 * plus[0] + m0 * dp_[0];
+            }
+            if (a & A_POST_SHIFT) {
+                shift(plus, minus, S);
+                shift(dp_, dm_, S);
+            }
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) plus[s] = minus[s] = dp_[s] = dm_[s] = LIT(0.0);
+            } else if (a & A_SHIFT_AFTER) {
+                shift(plus, minus, S);
+                shift(dp_, dm_, S);
+            }
+        }
+    }
+    free(buf);
+}
+
+/* First-order adjoint (_epg_cpu.cpp:5985-6232): the entry state of every
+ * event is recorded, then the events are swept backwards. Gradients add into
+ * the given arrays: per atom for t1, t2, m0, b1, inversion; per (train,
+ * event) for flip and duration. Only the imaginary seed plane acts. */
+static void run_adjoint(const oracle_case* c, const float* seed_imag,
+                        int64_t begin, int64_t end,
+                        REAL* g_t1, REAL* g_t2, REAL* g_m0, REAL* g_b1, REAL* g_inv,
+                        REAL* g_flip, REAL* g_duration) {
+    const int64_t S = c->state_count;
+    const int64_t E = c->event_count;
+    REAL* traj = (REAL*)malloc(sizeof(REAL) * (size_t)(E > 0 ? E : 1) * (size_t)(3 * S));
+    REAL* buf = (REAL*)calloc((size_t)(9 * S), sizeof(REAL));
+    REAL *plus = buf, *minus = buf + S, *lon = buf + 2 * S;
+    REAL *pb = buf + 3 * S, *mb = buf + 4 * S, *zb = buf + 5 * S;
+    REAL *ps = buf + 6 * S, *ms = buf + 7 * S, *zs = buf + 8 * S;
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / c->atom_count;
+        const int64_t atom = work % c->atom_count;
+        const int64_t ebase = train * E;
+        const float* duration = c->duration_s + ebase;
+        const float* flip = c->flip_rad + ebase;
+        const int64_t out_base = (train * c->atom_count + atom) * c->output_count;
+        const REAL t1 = (REAL)c->t1_ms[atom];
+        const REAL t2 = (REAL)c->t2_ms[atom];
+        const REAL m0 = tissue(c->m0, atom, LIT(1.0));
+        const REAL b1 = tissue(c->b1, atom, LIT(1.0));
+        const REAL eff = tissue(c->inversion, atom, LIT(1.0));
+        const REAL r1 = LIT(1000.0) / t1;
+        const REAL r2 = LIT(1000.0) / t2;
+        memset(buf, 0, sizeof(REAL) * (size_t)(9 * S));
+        lon[0] = LIT(1.0);
+        for (int64_t e = 0; e < E; ++e) {
+            REAL* slot = traj + e * 3 * S;
+            memcpy(slot, plus, sizeof(REAL) * (size_t)(3 * S));
+            const REAL dt = (REAL)duration[e];
+            const REAL e1 = EXP(-r1 * dt), e2 = EXP(-r2 * dt);
+            for (int64_t s = 0; s < S; ++s) {
+                plus[s] *= e2;
+                minus[s] *= e2;
+                lon[s] *= e1;
+            }
+            lon[0] += LIT(1.0) - e1;
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) shift(plus, minus, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    for (int64_t s = 0; s < S; ++s) lon[s] *= -eff;
+                } else {
+                    const REAL alpha = (REAL)flip[e] * b1;
+                    const REAL co = COS(alpha), si = SIN(alpha);
+                    const REAL ch = LIT(0.5) * (LIT(1.0) + co);
+                    const REAL sh = LIT(0.5) * (LIT(1.0) - co);
+                    const REAL hs = LIT(0.5) * si;
+                    for (int64_t s = 0; s < S; ++s) {
+                        const REAL p = plus[s], m = minus[s], z = lon[s];
+                        plus[s] = ch * p + sh * m - si * z;
+                        minus[s] = sh * p + ch * m + si * z;
+                        lon[s] = hs * p - hs * m + co * z;
+                    }
+                }
+            }
+            if (a & A_POST_SHIFT) shift(plus, minus, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) plus[s] = minus[s] = LIT(0.0);
+            } else if (a & A_SHIFT_AFTER) {
+                shift(plus, minus, S);
+            }
+        }
+        for (int64_t s = 0; s < 3 * S; ++s) pb[s] = LIT(0.0);
+        REAL gt1 = 0, gt2 = 0, gm0 = 0, gb1 = 0, ginv = 0;
+        for (int64_t e = E - 1; e >= 0; --e) {
+            const REAL* slot = traj + e * 3 * S;
+            const uint8_t a = c->action[e];
+            const REAL dt = (REAL)duration[e];
+            const REAL e1 = EXP(-r1 * dt), e2 = EXP(-r2 * dt);
+            for (int64_t s = 0; s < S; ++s) {
+                ps[s] = slot[s] * e2;
+                ms[s] = slot[S + s] * e2;
+                zs[s] = slot[2 * S + s] * e1;
+            }
+            zs[0] += LIT(1.0) - e1;
+            if (a & A_PRE_SHIFT) shift(ps, ms, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) pb[s] = mb[s] = LIT(0.0);
+            } else if (a & A_SHIFT_AFTER) {
+                shift_adjoint(pb, mb, S);
+            }
+            if (a & A_POST_SHIFT) shift_adjoint(pb, mb, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    for (int64_t s = 0; s < S; ++s) {
+                        ginv -= zb[s] * zs[s];
+                        zb[s] *= -eff;
+                    }
+                } else {
+                    const REAL fl = (REAL)flip[e];
+                    const REAL alpha = fl * b1;
+                    const REAL co = COS(alpha), si = SIN(alpha);
+                    const REAL ch = LIT(0.5) * (LIT(1.0) + co);
+                    const REAL sh = LIT(0.5) * (LIT(1.0) - co);
+                    const REAL hs = LIT(0.5) * si;
+                    REAL ga = LIT(0.0);
+                    for (int64_t s = 0; s < S; ++s) {
+                        const REAL p = ps[s], m = ms[s], z = zs[s];
+                        const REAL pbs = pb[s], mbs = mb[s], zbs = zb[s];
+                        ga += pbs * (hs * m - hs * p - co * z)
+                            + mbs * (hs * p - hs * m + co * z)
+                            + zbs * (LIT(0.5) * co * p - LIT(0.5) * co * m - si * z);
+                        pb[s] = ch * pbs + sh * mbs + hs * zbs;
+                        mb[s] = sh * pbs + ch * mbs - hs * zbs;
+                        zb[s] = -si * pbs + si * mbs + co * zbs;
+                    }
+                    g_flip[ebase + e] += ga * b1;
+                    gb1 += ga * fl;
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                const REAL sd = (REAL)seed_imag[out_base + c->output_index[e]];
+                gm0 += sd * ps[0];
+                pb[0] += sd * m0;
+            }
+            if (a & A_PRE_SHIFT) shift_adjoint(pb, mb, S);
+            REAL ge1 = -zb[0];
+            REAL ge2 = LIT(0.0);
+            for (int64_t s = 0; s < S; ++s) {
+                ge2 += pb[s] * slot[s] + mb[s] * slot[S + s];
+                ge1 += zb[s] * slot[2 * S + s];
+                pb[s] *= e2;
+                mb[s] *= e2;
+                zb[s] *= e1;
+            }
+            gt1 += ge1 * (e1 * dt * (LIT(1000.0) / (t1 * t1)));
+            gt2 += ge2 * (e2 * dt * (LIT(1000.0) / (t2 * t2)));
+            g_duration[ebase + e] += -ge1 * (r1 * e1) - ge2 * (r2 * e2);
+        }
+        g_t1[atom] += gt1;
+        g_t2[atom] += gt2;
+        g_m0[atom] += gm0;
+        g_b1[atom] += gb1;
+        g_inv[atom] += ginv;
+    }
+    free(buf);
+    free(traj);
+}
+
+/* ---- threaded drivers -------------------------------------------------- */
+
+typedef struct {
+    const oracle_case* c;
+    const oracle_direction* d;
+    int64_t begin, end;
+    REAL* out_real;
+    REAL* out_imag;
+} job;
+
+static void* forward_job(void* p) {
+    job* j = (job*)p;
+    run_forward(j->c, j->begin, j->end, j->out_real, j->out_imag);
+    return NULL;
+}
+
+static void* tangent_job(void* p) {
+    job* j = (job*)p;
+    run_tangent(j->c, j->d, j->begin, j->end, j->out_real, j->out_imag);
+    return NULL;
+}
+
+static void run_threads(void* (*fn)(void*), const oracle_case* c,
+                        const oracle_direction* d, REAL* out_real, REAL* out_imag,
+                        int threads) {
+    const int64_t work = c->atom_count * c->train_count;
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
+    if (work < threads) threads = work > 0 ? (int)work : 1;
+    pthread_t tid[256];
+    job jobs[256];
+    const int64_t block = (work + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        jobs[t].c = c;
+        jobs[t].d = d;
+        jobs[t].begin = t * block < work ? t * block : work;
+        jobs[t].end = (t + 1) * block < work ? (t + 1) * block : work;
+        jobs[t].out_real = out_real;
+        jobs[t].out_imag = out_imag;
+    }
+    if (threads == 1) {
+        fn(&jobs[0]);
+        return;
+    }
+    for (int t = 0; t < threads; ++t) pthread_create(&tid[t], NULL, fn, &jobs[t]);
+    for (int t = 0; t < threads; ++t) pthread_join(tid[t], NULL);
+}
+
+/* Output planes are (train_count, atom_count, output_count) in REAL. */
+void NAME(oracle_forward)(const oracle_case* c, REAL* out_real, REAL* out_imag,
+                          int threads) {
+    run_threads(forward_job, c, NULL, out_real, out_imag, threads);
+}
+
+void NAME(oracle_tangent)(const oracle_case* c, const oracle_direction* d,
+                          REAL* out_real, REAL* out_imag, int threads) {
+    run_threads(tangent_job, c, d, out_real, out_imag, threads);
+}
+
+/* Single-threaded adjoint; gradient arrays must be zeroed by the caller. */
+void NAME(oracle_adjoint)(const oracle_case* c, const float* seed_imag,
+                          REAL* g_t1, REAL* g_t2, REAL* g_m0, REAL* g_b1, REAL* g_inv,
+                          REAL* g_flip, REAL* g_duration) {
+    run_adjoint(c, seed_imag, 0, c->atom_count * c->train_count,
+                g_t1, g_t2, g_m0, g_b1, g_inv, g_flip, g_duration);
+}

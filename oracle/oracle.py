@@ -1,0 +1,236 @@
+"""ORACLE — test infrastructure only.
+
+Python face of ``oracle/epg_oracle.c``: the CPU restatement of the
+reference's real-subspace EPG recursion (src/torchsim/_epg_cpu.cpp:3010-3285,
+5950-6232). Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
+CPU-baseline leg import this module; the product never does.
+
+Every function takes the reference's packed buffers (the tissue properties
+and the event stream, as ``sequence/_accelerators.py:_pack_events`` lays them
+out) as NumPy arrays and returns NumPy arrays. ``precision`` picks the FP64
+oracle (``"f64"``) or the FP32 port that keeps the reference's statement
+order (``"f32"``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIBRARY = HERE / "_lib" / "libepg_oracle.so"
+
+
+class _Case(ctypes.Structure):
+    _fields_ = [
+        ("t1_ms", ctypes.c_void_p),
+        ("t2_ms", ctypes.c_void_p),
+        ("m0", ctypes.c_void_p),
+        ("b1", ctypes.c_void_p),
+        ("inversion", ctypes.c_void_p),
+        ("duration_s", ctypes.c_void_p),
+        ("kind", ctypes.c_void_p),
+        ("flip_rad", ctypes.c_void_p),
+        ("action", ctypes.c_void_p),
+        ("output_index", ctypes.c_void_p),
+        ("atom_count", ctypes.c_int64),
+        ("train_count", ctypes.c_int64),
+        ("event_count", ctypes.c_int64),
+        ("state_count", ctypes.c_int64),
+        ("output_count", ctypes.c_int64),
+    ]
+
+
+class _Direction(ctypes.Structure):
+    _fields_ = [
+        ("t1_ms", ctypes.c_void_p),
+        ("t2_ms", ctypes.c_void_p),
+        ("m0", ctypes.c_void_p),
+        ("b1", ctypes.c_void_p),
+        ("inversion", ctypes.c_void_p),
+        ("duration_s", ctypes.c_void_p),
+        ("flip_rad", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def build() -> Path:
+    """Compile the oracle library with its Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIBRARY
+
+
+def _library() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIBRARY.exists():
+            build()
+        _lib = ctypes.CDLL(str(LIBRARY))
+    return _lib
+
+
+@dataclass
+class Packed:
+    """One run's packed inputs (the reference's buffer ABI, real subset)."""
+
+    t1_ms: np.ndarray
+    t2_ms: np.ndarray
+    duration_s: np.ndarray  # (events,) or (trains, events)
+    kind: np.ndarray
+    flip_rad: np.ndarray  # (events,) or (trains, events)
+    action: np.ndarray
+    output_index: np.ndarray
+    state_count: int
+    m0: np.ndarray | None = None
+    b1: np.ndarray | None = None
+    inversion: np.ndarray | None = None
+
+    @property
+    def atom_count(self) -> int:
+        return int(np.asarray(self.t1_ms).size)
+
+    @property
+    def event_count(self) -> int:
+        return int(np.asarray(self.kind).size)
+
+    @property
+    def train_count(self) -> int:
+        d = np.asarray(self.duration_s)
+        return 1 if d.ndim == 1 else int(d.shape[0])
+
+    @property
+    def output_count(self) -> int:
+        oi = np.asarray(self.output_index)
+        return int(oi.max()) + 1 if oi.size and oi.max() >= 0 else 0
+
+
+def _f32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _case(p: Packed, keep: list) -> _Case:
+    arrays = {
+        "t1_ms": _f32(p.t1_ms),
+        "t2_ms": _f32(p.t2_ms),
+        "m0": _f32(p.m0),
+        "b1": _f32(p.b1),
+        "inversion": _f32(p.inversion),
+        "duration_s": _f32(np.broadcast_to(p.duration_s, (p.train_count, p.event_count))),
+        "kind": np.ascontiguousarray(p.kind, dtype=np.int32),
+        "flip_rad": _f32(np.broadcast_to(p.flip_rad, (p.train_count, p.event_count))),
+        "action": np.ascontiguousarray(p.action, dtype=np.uint8),
+        "output_index": np.ascontiguousarray(p.output_index, dtype=np.int32),
+    }
+    keep.append(arrays)
+    c = _Case()
+    for name, value in arrays.items():
+        setattr(c, name, _ptr(value))
+    c.atom_count = p.atom_count
+    c.train_count = p.train_count
+    c.event_count = p.event_count
+    c.state_count = int(p.state_count)
+    c.output_count = p.output_count
+    return c
+
+
+def _dtype(precision: str):
+    if precision not in ("f64", "f32"):
+        raise ValueError(f"precision must be 'f64' or 'f32', got {precision!r}")
+    return (np.float64, ctypes.c_double) if precision == "f64" else (np.float32, ctypes.c_float)
+
+
+def _shape(p: Packed):
+    return (p.atom_count, p.output_count) if p.train_count == 1 else (
+        p.train_count, p.atom_count, p.output_count)
+
+
+def forward(p: Packed, precision: str = "f64", threads: int = 1) -> np.ndarray:
+    """Recorded samples' imaginary plane, ``m0 * F+[0]`` (the real plane is 0).
+
+    Follows ``simulate_real_range`` (src/torchsim/_epg_cpu.cpp:3041-3128).
+    """
+    dtype, _ = _dtype(precision)
+    keep: list = []
+    c = _case(p, keep)
+    real = np.zeros(_shape(p), dtype=dtype)
+    imag = np.zeros(_shape(p), dtype=dtype)
+    fn = getattr(_library(), f"oracle_forward_{precision}")
+    fn(ctypes.byref(c), ctypes.c_void_p(real.ctypes.data), ctypes.c_void_p(imag.ctypes.data),
+       ctypes.c_int(threads))
+    return imag
+
+
+def tangent(p: Packed, precision: str = "f64", threads: int = 1, **direction) -> np.ndarray:
+    """One forward-mode tangent of the recorded samples' imaginary plane.
+
+    ``direction`` names any of ``t1_ms, t2_ms, m0, b1, inversion`` (per atom)
+    and ``duration_s, flip_rad`` (per event or per train and event). Follows
+    ``simulate_real_jvp_range`` (src/torchsim/_epg_cpu.cpp:3136-3285).
+    """
+    dtype, _ = _dtype(precision)
+    keep: list = []
+    c = _case(p, keep)
+    d = _Direction()
+    shape = (p.train_count, p.event_count)
+    for name in ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s", "flip_rad"):
+        value = direction.pop(name, None)
+        if value is None:
+            continue
+        if name in ("duration_s", "flip_rad"):
+            value = np.broadcast_to(np.asarray(value, np.float32), shape)
+        else:
+            value = np.broadcast_to(np.asarray(value, np.float32), (p.atom_count,))
+        value = _f32(value)
+        keep.append(value)
+        setattr(d, name, _ptr(value))
+    if direction:
+        raise ValueError(f"unknown tangent directions {sorted(direction)}")
+    real = np.zeros(_shape(p), dtype=dtype)
+    imag = np.zeros(_shape(p), dtype=dtype)
+    fn = getattr(_library(), f"oracle_tangent_{precision}")
+    fn(ctypes.byref(c), ctypes.byref(d), ctypes.c_void_p(real.ctypes.data),
+       ctypes.c_void_p(imag.ctypes.data), ctypes.c_int(threads))
+    return imag
+
+
+def adjoint(p: Packed, seed_imag: np.ndarray, precision: str = "f64") -> dict[str, np.ndarray]:
+    """First-order adjoint for a seed on the imaginary output plane.
+
+    Returns per-atom gradients ``t1_ms, t2_ms, m0, b1, inversion`` and per
+    (train, event) gradients ``flip_rad, duration_s``. Follows
+    ``simulate_real_vjp_range`` (src/torchsim/_epg_cpu.cpp:5985-6232).
+    """
+    dtype, _ = _dtype(precision)
+    keep: list = []
+    c = _case(p, keep)
+    seed = _f32(np.broadcast_to(seed_imag, _shape(p)))
+    grads = {n: np.zeros(p.atom_count, dtype=dtype) for n in ("t1_ms", "t2_ms", "m0", "b1", "inversion")}
+    grads["flip_rad"] = np.zeros((p.train_count, p.event_count), dtype=dtype)
+    grads["duration_s"] = np.zeros((p.train_count, p.event_count), dtype=dtype)
+    fn = getattr(_library(), f"oracle_adjoint_{precision}")
+    order = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")
+    fn(ctypes.byref(c), ctypes.c_void_p(seed.ctypes.data),
+       *[ctypes.c_void_p(grads[n].ctypes.data) for n in order])
+    if p.train_count == 1:
+        grads["flip_rad"] = grads["flip_rad"][0]
+        grads["duration_s"] = grads["duration_s"][0]
+    return grads
+
+
+def cpu_threads() -> int:
+    """Host cores this process may use."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:  # pragma: no cover
+        return os.cpu_count() or 1

@@ -1,0 +1,292 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Run in a container that has the reference checkout (default /root/reference)
+and a C++ compiler:
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+It builds the reference's own CPU kernel with ``oracle/build_ref.sh``, imports
+the reference's Python package from a temporary copy, runs its public calls
+(``torchsim.mrf_sim``, ``MRFSimulator``, ``FSESimulator``) on small seeded
+cases, and records, per case:
+
+* the packed buffers the reference hands its kernel (tissue and the nine event
+  buffers), captured at ``_run_packed`` / ``_run_packed_jvp`` /
+  ``_run_packed_vjp`` (``src/torchsim/sequence/_accelerators.py:3262, 3933,
+  3452``) together with the real-subspace verdict and the raw output planes;
+* the public outputs: signal, Jacobian, and gradients of a loss.
+
+The fixtures are what pins the oracle (``oracle/``) and this package's event
+builders to the reference. Nothing at test time reads the reference.
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+
+
+def _import_reference(root: Path):
+    subprocess.run(["bash", str(REPO / "oracle" / "build_ref.sh"), str(root)], check=True)
+    built = sorted((REPO / "oracle" / "_ref").glob("_epg_cpu*.so"))
+    if not built:
+        raise SystemExit("reference CPU kernel did not build")
+    scratch = Path(tempfile.mkdtemp(prefix="torchsim_ref_"))
+    shutil.copytree(root / "src" / "torchsim", scratch / "torchsim")
+    shutil.copy(built[-1], scratch / "torchsim")
+    sys.path.insert(0, str(scratch))
+    import torchsim  # noqa: PLC0415
+
+    return torchsim
+
+
+class _Recorder:
+    """Wraps the three packed-run routes and keeps what they were given."""
+
+    def __init__(self, accelerators) -> None:
+        self.calls: list[dict] = []
+        self.acc = accelerators
+        self._orig = {}
+        self.verdicts: list = []
+        for name in ("_auto_real_axis", "_auto_real_axis_adjoint"):
+            self._orig[name] = getattr(accelerators, name)
+            setattr(accelerators, name, self._verdict(name))
+        for name in ("_run_packed", "_run_packed_jvp", "_run_packed_vjp"):
+            self._orig[name] = getattr(accelerators, name)
+            setattr(accelerators, name, self._wrap(name))
+
+    def _wrap(self, name):
+        original = self._orig[name]
+
+        def wrapped(*args, **kwargs):
+            result = original(*args, **kwargs)
+            self.calls.append({"route": name, "args": args, "kwargs": kwargs, "result": result})
+            return result
+
+        return wrapped
+
+    def _verdict(self, name):
+        original = self._orig[name]
+
+        def wrapped(*args, **kwargs):
+            result = original(*args, **kwargs)
+            self.verdicts.append(result)
+            return result
+
+        return wrapped
+
+    def axis(self, call: dict) -> int:
+        """The real-subspace verdict a forward call ran under (-1: complex)."""
+        args, kwargs = call["args"], call["kwargs"]
+        given = args[5] if len(args) > 5 else kwargs.get("real_axis")
+        if given is None and self.verdicts:
+            given = self.verdicts[0]
+        return -1 if given is None else int(given)
+
+    def clear(self) -> None:
+        self.calls.clear()
+        self.verdicts.clear()
+
+
+def _np(value):
+    import torch
+
+    if torch.is_tensor(value):
+        value = value.detach().cpu()
+        if value.is_complex():
+            return value.numpy().astype(np.complex64 if value.dtype == torch.complex64 else np.complex128)
+        return value.numpy()
+    return np.asarray(value)
+
+
+EVENT_NAMES = (
+    "duration", "kind", "flip", "phase", "action", "output_index",
+    "shim_index", "saturation", "rf_frequency_hz",
+)
+TISSUE_NAMES = (
+    "t1_ms", "t2_ms", "m0", "b1", "b1_phase_rad", "b0_hz", "inversion_efficiency",
+    "diffusion_um2_per_ms", "velocity_m_per_s", "bound_fraction", "bound_exchange_hz",
+    "t1_bound_ms", "pool_b_fraction", "pool_b_exchange_hz", "t1_pool_b_ms",
+    "t2_pool_b_ms", "pool_b_shift_hz",
+)
+
+
+def _packed(call: dict, prefix: str) -> dict:
+    args = call["args"]
+    tissue, events = args[0], args[1]
+    out = {}
+    for name, value in zip(TISSUE_NAMES, tissue, strict=True):
+        out[f"{prefix}tissue_{name}"] = _np(value)
+    for name, value in zip(EVENT_NAMES, events, strict=True):
+        out[f"{prefix}event_{name}"] = _np(value)
+    return out
+
+
+def mrf_schedule() -> np.ndarray:
+    return np.concatenate(
+        [np.linspace(5, 60, 300), np.linspace(60, 2, 300), np.full(280, 2.0)]
+    ).astype(np.float32)
+
+
+def draw_tissue(rng: np.random.Generator, n: int):
+    t1 = np.exp(rng.uniform(np.log(100), np.log(3000), n)).astype(np.float32)
+    t2 = np.exp(rng.uniform(np.log(10), np.log(300), n)).astype(np.float32)
+    t2 = np.minimum(t2, np.float32(0.999) * t1).astype(np.float32)
+    b1 = rng.uniform(0.8, 1.2, n).astype(np.float32)
+    return t1, t2, b1
+
+
+def case_mrf880(ts, rec) -> dict:
+    import torch
+
+    rng = np.random.default_rng(0)
+    t1, t2, b1 = draw_tissue(rng, 8)
+    flip = mrf_schedule()
+    rec.clear()
+    sig = ts.mrf_sim(torch.from_numpy(flip), 10.0, torch.from_numpy(t1), torch.from_numpy(t2),
+                     B1=torch.from_numpy(b1), states=10)
+    fwd = [c for c in rec.calls if c["route"] == "_run_packed"][0]
+    out = {"flip_deg": flip, "tr_ms": np.float32(10.0), "t1": t1, "t2": t2, "b1": b1,
+           "states": np.int64(10), "signal": _np(sig)}
+    out.update(_packed(fwd, ""))
+    out["real_axis"] = np.int64(rec.axis(fwd))
+    out["raw_forward"] = _np(fwd["result"])
+    rec.clear()
+    sig2, jac = ts.mrf_sim(torch.from_numpy(flip), 10.0, torch.from_numpy(t1), torch.from_numpy(t2),
+                           B1=torch.from_numpy(b1), states=10, diff=("T1", "T2", "B1", "M0"))
+    out["signal_jac"] = _np(sig2)
+    out["jacobian"] = _np(jac)
+    out["jacobian_names"] = np.array(["T1", "T2", "B1", "M0"])
+    return out
+
+
+def case_mrf_prep(ts, rec) -> dict:
+    import torch
+
+    rng = np.random.default_rng(1)
+    n = 5
+    t1, t2, b1 = draw_tissue(rng, n)
+    m0 = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    inv = rng.uniform(0.85, 1.0, n).astype(np.float32)
+    flip = rng.uniform(5, 70, 60).astype(np.float32)
+    tr = rng.uniform(8, 15, 60).astype(np.float32)
+    kw = dict(B1=torch.from_numpy(b1), M0=torch.from_numpy(m0), inv_efficiency=torch.from_numpy(inv),
+              TI=20.0, states=7, nreps=2)
+    rec.clear()
+    sig = ts.mrf_sim(torch.from_numpy(flip), torch.from_numpy(tr), torch.from_numpy(t1),
+                     torch.from_numpy(t2), **kw)
+    fwd = [c for c in rec.calls if c["route"] == "_run_packed"][0]
+    out = {"flip_deg": flip, "tr_ms": tr, "t1": t1, "t2": t2, "b1": b1, "m0": m0, "inv": inv,
+           "ti_ms": np.float32(20.0), "nreps": np.int64(2), "states": np.int64(7),
+           "signal": _np(sig)}
+    out.update(_packed(fwd, ""))
+    out["real_axis"] = np.int64(rec.axis(fwd))
+    out["raw_forward"] = _np(fwd["result"])
+    names = ("T1", "T2", "B1", "M0", "inv_efficiency")
+    _, jac = ts.mrf_sim(torch.from_numpy(flip), torch.from_numpy(tr), torch.from_numpy(t1),
+                        torch.from_numpy(t2), diff=names, **kw)
+    out["jacobian"] = _np(jac)
+    out["jacobian_names"] = np.array(names)
+    return out
+
+
+def case_fse(ts, rec) -> dict:
+    import torch
+    from torchsim.simulators import FSESimulator
+
+    rng = np.random.default_rng(2)
+    n, etl = 6, 12
+    t1 = rng.uniform(300, 3000, n).astype(np.float32)
+    t2 = rng.uniform(10, 300, n).astype(np.float32)
+    b1 = rng.uniform(0.7, 1.3, n).astype(np.float32)
+    flip = rng.uniform(100, 180, etl).astype(np.float32)
+    esp = 8.0
+    sim = FSESimulator(flip=torch.from_numpy(flip), ESP=esp, phases=90.0, states=2 * etl)
+    rec.clear()
+    sig = sim.simulate(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2), B1=torch.from_numpy(b1))
+    fwd = [c for c in rec.calls if c["route"] == "_run_packed"][0]
+    out = {"flip_deg": flip, "esp_ms": np.float32(esp), "t1": t1, "t2": t2, "b1": b1,
+           "states": np.int64(2 * etl), "signal": _np(sig)}
+    out.update(_packed(fwd, ""))
+    out["real_axis"] = np.int64(rec.axis(fwd))
+    out["raw_forward"] = _np(fwd["result"])
+    names = ("T1", "T2", "B1")
+    _, jac = sim.jacobian(names, T1=torch.from_numpy(t1), T2=torch.from_numpy(t2), B1=torch.from_numpy(b1))
+    out["jacobian"] = _np(jac)
+    out["jacobian_names"] = np.array(names)
+    return out
+
+
+def case_adjoint(ts, rec) -> dict:
+    import torch
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(3)
+    n, pulses = 4, 40
+    t1, t2, b1 = draw_tissue(rng, n)
+    flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    target_flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    target_tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    tissue = dict(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2), B1=torch.from_numpy(b1))
+    with torch.no_grad():
+        target = MRFSimulator(flip=torch.from_numpy(target_flip), TR=torch.from_numpy(target_tr),
+                              states=8).simulate(**tissue)
+    theta = torch.from_numpy(flip).clone().requires_grad_(True)
+    tau = torch.from_numpy(tr).clone().requires_grad_(True)
+    t1t = torch.from_numpy(t1).clone().requires_grad_(True)
+    t2t = torch.from_numpy(t2).clone().requires_grad_(True)
+    b1t = torch.from_numpy(b1).clone().requires_grad_(True)
+    rec.clear()
+    sig = MRFSimulator(flip=theta, TR=tau, states=8).simulate(T1=t1t, T2=t2t, B1=b1t)
+    loss = (sig - target).abs().square().sum()
+    loss.backward()
+    out = {"flip_deg": flip, "tr_ms": tr, "t1": t1, "t2": t2, "b1": b1, "states": np.int64(8),
+           "target": _np(target), "signal": _np(sig), "loss": _np(loss),
+           "grad_flip_deg": _np(theta.grad), "grad_tr_ms": _np(tau.grad),
+           "grad_t1": _np(t1t.grad), "grad_t2": _np(t2t.grad), "grad_b1": _np(b1t.grad)}
+    out["adjoint_verdicts"] = np.array([-1 if v is None else int(v) for v in rec.verdicts])
+    vjp = [c for c in rec.calls if c["route"] == "_run_packed_vjp"]
+    if vjp:
+        call = vjp[0]
+        out.update(_packed(call, "vjp_"))
+        out["vjp_seed"] = _np(call["args"][2])
+        names = (*TISSUE_NAMES, "duration", "flip", "phase")
+        for name, value in zip(names, call["result"], strict=True):
+            if value is not None:
+                out[f"vjp_grad_{name}"] = _np(value)
+    return out
+
+
+def main() -> None:
+    root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    ts = _import_reference(root)
+    import torch
+
+    torch.manual_seed(0)
+    from torchsim.sequence import _accelerators
+
+    # Reach for the real-subspace verdict however small the case, as the
+    # reference's own tests do (tests/conftest.py:6-17), so the fixtures come
+    # from the kernels this package restates.
+    _accelerators.detection = lambda kind, device: 0.0
+    rec = _Recorder(_accelerators)
+    for name, fn in (("mrf880", case_mrf880), ("mrf_prep", case_mrf_prep),
+                     ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint)):
+        data = fn(ts, rec)
+        np.savez_compressed(HERE / f"{name}.npz", **data)
+        print(f"wrote {name}.npz with {len(data)} arrays")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,93 @@
+"""The oracle pinned to the reference: its FP32 port reproduces the
+reference's own compiled CPU kernel on the committed fixtures, and the FP64
+oracle agrees with it to FP32 rounding."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import max_rel, packed_from_golden
+
+FORWARD_CASES = ["mrf880", "mrf_prep", "fse_cpmg"]
+KEYS = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1", "M0": "m0", "inv_efficiency": "inversion"}
+
+
+@pytest.mark.parametrize("name", FORWARD_CASES)
+def test_fp32_port_is_bitwise_the_reference_kernel(golden, name):
+    d = golden(name)
+    assert int(d["real_axis"]) == 1
+    raw = d["raw_forward"]
+    out = O.forward(packed_from_golden(d), "f32")
+    assert np.array_equal(out, raw.imag)
+    assert not raw.real.any()
+
+
+@pytest.mark.parametrize("name", FORWARD_CASES)
+def test_fp64_oracle_matches_reference(golden, name):
+    d = golden(name)
+    out = O.forward(packed_from_golden(d), "f64")
+    assert max_rel(out, d["raw_forward"].imag) < 5e-6
+
+
+@pytest.mark.parametrize("name", ["mrf880", "mrf_prep"])
+def test_oracle_tangents_match_reference_jacobian(golden, name):
+    d = golden(name)
+    p = packed_from_golden(d)
+    for col, prop in enumerate(d["jacobian_names"]):
+        ref = -d["jacobian"][:, col].real  # the API returns 1j * (i * tangent)
+        for precision, tol in (("f32", 1e-6), ("f64", 5e-6)):
+            t = O.tangent(p, precision, **{KEYS[str(prop)]: 1.0})
+            assert max_rel(t, ref) < tol, (prop, precision)
+
+
+def test_public_signal_is_minus_raw_plane(golden):
+    d = golden("mrf880")
+    # MRFSimulator.evaluate returns 1j * signal (simulators/mrf.py:84).
+    np.testing.assert_array_equal(d["signal"].real, -d["raw_forward"].imag)
+
+
+@pytest.mark.parametrize("precision,tol", [("f32", 0.0), ("f64", 1e-6)])
+def test_oracle_adjoint_matches_reference_vjp(golden, precision, tol):
+    d = golden("mrf_adjoint")
+    p = packed_from_golden(d, "vjp_")
+    g = O.adjoint(p, d["vjp_seed"].imag, precision)
+    pairs = {"t1_ms": "vjp_grad_t1_ms", "t2_ms": "vjp_grad_t2_ms", "b1": "vjp_grad_b1",
+             "m0": "vjp_grad_m0", "flip_rad": "vjp_grad_flip",
+             "duration_s": "vjp_grad_duration"}
+    for mine, ref in pairs.items():
+        assert max_rel(g[mine], d[ref]) <= tol, mine
+
+
+def test_oracle_adjoint_is_transpose_of_tangent():
+    """<seed, J v> == <J^T seed, v> on a small seeded case (FP64)."""
+    from torchsim_gb300.sequence import mrf_events
+
+    rng = np.random.default_rng(7)
+    flips = rng.uniform(5, 70, 12).astype(np.float32)
+    trs = rng.uniform(8, 15, 12).astype(np.float32)
+    ev = mrf_events(flips, trs, TI_ms=5.0)
+    t1 = np.array([800.0, 300.0], np.float32)
+    t2 = np.array([60.0, 40.0], np.float32)
+    b1 = np.array([0.9, 1.1], np.float32)
+    p = O.Packed(t1, t2, ev.duration, ev.kind, ev.flip, ev.action, ev.output_index, 6, b1=b1)
+    seed = rng.standard_normal((2, ev.outputs)).astype(np.float32)
+    g = O.adjoint(p, seed, "f64")
+    v_flip = rng.standard_normal(ev.duration.shape).astype(np.float32)
+    v_dur = rng.standard_normal(ev.duration.shape).astype(np.float32) * 1e-3
+    v_t1 = rng.standard_normal(2).astype(np.float32)
+    jv = O.tangent(p, "f64", flip_rad=v_flip, duration_s=v_dur, t1_ms=v_t1)
+    lhs = float((seed.astype(np.float64) * jv).sum())
+    rhs = float((g["flip_rad"] * v_flip[0]).sum() + (g["duration_s"] * v_dur[0]).sum()
+                + (g["t1_ms"] * v_t1).sum())
+    assert abs(lhs - rhs) <= 1e-9 * max(1.0, abs(lhs))
+
+
+def test_oracle_planted_mistake_is_caught(golden):
+    """A wrong shift rule in the checker must show up against the fixture."""
+    d = golden("mrf880")
+    p = packed_from_golden(d)
+    p.state_count = 9  # truncating one order early changes the answer
+    out = O.forward(p, "f64")
+    assert max_rel(out, d["raw_forward"].imag) > 1e-5

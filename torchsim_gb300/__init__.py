@@ -1,0 +1,15 @@
+"""torchsim_gb300 — the extended-phase-graph hot path of torchsim on GB300.
+
+Public API kept from the reference (FiRMLAB-Pisa/torchsim):
+
+* ``mrf_sim``, ``fse_sim`` — functional simulators with ``diff=`` Jacobians;
+* ``MRFSimulator``, ``FSESimulator`` — ``simulate`` / ``jacobian``.
+
+All compute runs in hand-written sm_103a CUDA kernels behind the C ABI in
+``include/torchsim_gb300.h``; there is no CPU fallback.
+"""
+
+from .simulators import FSESimulator, MRFSimulator, fse_sim, mrf_sim
+
+__all__ = ["FSESimulator", "MRFSimulator", "fse_sim", "mrf_sim"]
+__version__ = "0.1.0"

@@ -1,0 +1,129 @@
+"""ctypes binding of ``libtorchsim_gb300.so`` (the C ABI in ``include/``).
+
+The library is the only compute path: if it is missing or cannot load, every
+call raises. There is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+PACKAGE = Path(__file__).resolve().parent
+LIBRARY = PACKAGE / "_lib" / "libtorchsim_gb300.so"
+
+TSG_OK = 0
+TSG_ERR_ARGUMENT = -1
+TSG_ERR_UNSUPPORTED = -2
+TSG_ERR_CUDA = -3
+TSG_ERR_CAPACITY = -4
+
+LAYOUT_PLANES = 0
+LAYOUT_COMPLEX_IJ = 1
+
+TANGENT_T1 = 1
+TANGENT_T2 = 2
+TANGENT_B1 = 4
+TANGENT_INVERSION = 8
+
+
+class NativeError(RuntimeError):
+    """A failure reported by the CUDA library."""
+
+    def __init__(self, code: int, message: str) -> None:
+        super().__init__(f"torchsim_gb300 error {code}: {message}")
+        self.code = code
+
+
+class Tissue(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("t1_ms", "t2_ms", "m0", "b1", "inversion")]
+
+
+class Direction(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s", "flip_rad")]
+
+
+class Gradients(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")]
+
+
+class Launch(ctypes.Structure):
+    _fields_ = [("lanes_per_voxel", ctypes.c_int), ("orders_per_lane", ctypes.c_int),
+                ("warps_per_block", ctypes.c_int)]
+
+
+_i64 = ctypes.c_int64
+_vp = ctypes.c_void_p
+_int = ctypes.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES: dict[str, tuple] = {
+    "tsg_last_error": (ctypes.c_char_p, []),
+    "tsg_version": (_int, []),
+    "tsg_probe_fp32": (_int, [_i64, _int, _int, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),
+    "tsg_program_create": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _int, _vp,
+                                  ctypes.POINTER(_vp)]),
+    "tsg_program_destroy": (_int, [_vp]),
+    "tsg_program_plan": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _int, _vp,
+                                ctypes.POINTER(_i64), ctypes.POINTER(_i64), _vp, _vp, _vp, _vp,
+                                _i64]),
+    "tsg_program_info": (_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                                ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "tsg_epg_forward": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _int, _vp, _vp,
+                               ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_forward_tangents": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.c_uint,
+                                        ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, _int,
+                                        _vp, _vp, _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_tangent": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.POINTER(Direction),
+                               _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,
+                                _int]),
+    "tsg_epg_simulate_jvp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
+                                    _int, _int]),
+}
+
+_lib: ctypes.CDLL | None = None
+
+
+def library() -> ctypes.CDLL:
+    """Load the CUDA library (once), raising if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIBRARY.exists():
+            raise NativeError(
+                TSG_ERR_UNSUPPORTED,
+                f"{LIBRARY} is missing; build it with torchsim_gb300._build.build()",
+            )
+        lib = ctypes.CDLL(str(LIBRARY))
+        for name, (restype, argtypes) in SIGNATURES.items():
+            if not hasattr(lib, name):
+                continue
+            fn = getattr(lib, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        _lib = lib
+    return _lib
+
+
+def check(code: int) -> None:
+    """Raise the library's last error for a non-zero return code."""
+    if code != TSG_OK:
+        message = library().tsg_last_error()
+        text = message.decode() if message else "unknown error"
+        if code == TSG_ERR_ARGUMENT:
+            raise ValueError(text)
+        raise NativeError(code, text)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(library(), name)(*args))
+
+
+def launch_shape(shape) -> ctypes.POINTER(Launch) | None:
+    """A Launch struct from a (lanes, orders, warps) tuple, or None for auto."""
+    if shape is None:
+        return None
+    lanes, orders, warps = shape
+    return ctypes.pointer(Launch(int(lanes), int(orders), int(warps)))

@@ -1,0 +1,595 @@
+// The C ABI: program management, launch selection, the device-resident
+// sweep entry points and the host-buffer drop-ins for the reference's
+// _epg_cpu.simulate / simulate_jvp (src/torchsim/_epg_cpu.cpp:10740, 11017).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "tsg_internal.h"
+
+namespace tsg {
+
+namespace {
+
+struct Table {
+    const SweepEntry* entries;
+    int count;
+};
+
+Table table_for(int mode) {
+    switch (mode) {
+        case MODE_FORWARD: return {kSweepForward, kSweepForwardCount};
+        case MODE_T12: return {kSweepT12, kSweepT12Count};
+        case MODE_T12B: return {kSweepT12B, kSweepT12BCount};
+        case MODE_T12BI: return {kSweepT12BI, kSweepT12BICount};
+        case MODE_GENERAL: return {kSweepGeneral, kSweepGeneralCount};
+    }
+    return {nullptr, 0};
+}
+
+int sm_count() {
+    static int count = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
+    return count;
+}
+
+// Built-in launch heuristic: the fewest padded orders (L*R >= states), then
+// enough lanes in flight to fill the GPU, then the fewest lanes per voxel
+// (each lane of a voxel repeats the per-pulse exp/sincos).
+const SweepEntry* choose(int mode, int states, int64_t work_items, const tsg_launch* want,
+                         int* warps) {
+    Table t = table_for(mode);
+    *warps = (want && want->warps_per_block > 0) ? want->warps_per_block : 4;
+    if (want && want->lanes_per_voxel > 0 && want->orders_per_lane > 0) {
+        for (int i = 0; i < t.count; ++i)
+            if (t.entries[i].lanes_per_voxel == want->lanes_per_voxel &&
+                t.entries[i].orders_per_lane == want->orders_per_lane &&
+                want->lanes_per_voxel * want->orders_per_lane >= states)
+                return &t.entries[i];
+        return nullptr;
+    }
+    const int64_t target_lanes = int64_t(sm_count()) * 1024;
+    const SweepEntry* best = nullptr;
+    double best_score = 1e300;
+    for (int i = 0; i < t.count; ++i) {
+        const SweepEntry& e = t.entries[i];
+        const int padded = e.lanes_per_voxel * e.orders_per_lane;
+        if (padded < states) continue;
+        if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
+        const double waste = double(padded) / states;
+        const double lanes = double(work_items) * e.lanes_per_voxel;
+        const double fill = std::min(1.0, lanes / double(target_lanes));
+        // Time ~ padded orders x lane redundancy / GPU fill.
+        const double redundancy = 1.0 + 0.15 * (e.lanes_per_voxel - 1) / e.orders_per_lane;
+        const double score = waste * redundancy / std::max(fill, 1e-3);
+        if (score < best_score) {
+            best_score = score;
+            best = &e;
+        }
+    }
+    return best;
+}
+
+int mode_for_mask(unsigned mask) {
+    if (mask == 0) return MODE_FORWARD;
+    if ((mask & ~3u) == 0) return MODE_T12;
+    if ((mask & ~7u) == 0) return MODE_T12B;
+    if ((mask & ~15u) == 0) return MODE_T12BI;
+    return -1;
+}
+
+int launch(int mode, const tsg_program* prog, const SweepArgs& args, int64_t atoms, int states,
+           const tsg_launch* want, cudaStream_t stream) {
+    int warps = 4;
+    const SweepEntry* e = choose(mode, states, atoms * prog->host.trains, want, &warps);
+    if (!e) return fail(TSG_ERR_UNSUPPORTED, "no sweep kernel for this state count / launch shape");
+    if (warps < 1 || warps > 8) return fail(TSG_ERR_ARGUMENT, "warps_per_block must be 1..8");
+    if (atoms == 0 || prog->host.ops == 0) return TSG_OK;
+    const int64_t vpb = int64_t(warps) * (32 / e->lanes_per_voxel);
+    const int64_t blocks = (atoms + vpb - 1) / vpb;
+    if (blocks > 0x7fffffffLL) return fail(TSG_ERR_CAPACITY, "too many voxels for one launch");
+    if (prog->host.trains > 65535) return fail(TSG_ERR_CAPACITY, "more than 65535 trains");
+    dim3 grid(unsigned(blocks), unsigned(prog->host.trains));
+    e->launch(args, grid, dim3(32 * warps), 0, stream);
+    TSG_CUDA(cudaGetLastError());
+    return TSG_OK;
+}
+
+SweepArgs base_args(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms,
+                    int64_t states) {
+    SweepArgs a{};
+    a.ops = prog->d_ops;
+    a.n_ops = int(prog->host.ops);
+    a.atoms = atoms;
+    a.states = int(states);
+    a.outputs = int(prog->host.outputs);
+    a.t1 = tissue->t1_ms;
+    a.t2 = tissue->t2_ms;
+    a.m0 = tissue->m0;
+    a.b1 = tissue->b1;
+    a.inv = tissue->inversion;
+    a.col_t1 = a.col_t2 = a.col_b1 = a.col_inv = a.col_m0 = a.col_gen = -1;
+    a.ckpt_every = 1;
+    return a;
+}
+
+int check_common(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms, int64_t states) {
+    if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
+    if (!tissue || (atoms > 0 && (!tissue->t1_ms || !tissue->t2_ms)))
+        return fail(TSG_ERR_ARGUMENT, "t1 and t2 are required");
+    if (atoms < 0 || states < 1) return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
+    if (states > 256) return fail(TSG_ERR_CAPACITY, "more than 256 states");
+    return TSG_OK;
+}
+
+}  // namespace
+
+}  // namespace tsg
+
+using namespace tsg;
+
+extern "C" int tsg_version(void) { return 1; }
+
+extern "C" int tsg_program_create(const float* duration_s, const int32_t* kind,
+                                  const float* flip_rad, const uint8_t* action,
+                                  const int32_t* output_index, int64_t train_count,
+                                  int64_t event_count, int unmerged,
+                                  const float* duration_tangent, tsg_program** out) {
+    if (!out) return fail(TSG_ERR_ARGUMENT, "null output handle");
+    *out = nullptr;
+    auto* prog = new tsg_program();
+    int rc = compile_program(duration_s, kind, flip_rad, action, output_index, train_count,
+                             event_count, unmerged != 0, duration_tangent, &prog->host);
+    if (rc != TSG_OK) {
+        delete prog;
+        return rc;
+    }
+    cudaGetDevice(&prog->device);
+    const size_t n = prog->host.op.size();
+    if (n > 0) {
+        cudaError_t e1 = cudaMalloc(&prog->d_ops, n * sizeof(Op));
+        cudaError_t e2 = cudaMalloc(&prog->d_src, n * sizeof(OpSource));
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            cudaFree(prog->d_ops);
+            cudaFree(prog->d_src);
+            delete prog;
+            return cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaMalloc(program)");
+        }
+        cudaError_t e3 = cudaMemcpy(prog->d_ops, prog->host.op.data(), n * sizeof(Op),
+                                    cudaMemcpyHostToDevice);
+        cudaError_t e4 = cudaMemcpy(prog->d_src, prog->host.src.data(), n * sizeof(OpSource),
+                                    cudaMemcpyHostToDevice);
+        if (e3 != cudaSuccess || e4 != cudaSuccess) {
+            cudaFree(prog->d_ops);
+            cudaFree(prog->d_src);
+            delete prog;
+            return cuda_fail(e3 != cudaSuccess ? e3 : e4, "cudaMemcpy(program)");
+        }
+    }
+    *out = prog;
+    return TSG_OK;
+}
+
+extern "C" int tsg_program_plan(const float* duration_s, const int32_t* kind,
+                                const float* flip_rad, const uint8_t* action,
+                                const int32_t* output_index, int64_t train_count,
+                                int64_t event_count, int unmerged, const float* duration_tangent,
+                                int64_t* op_count, int64_t* output_count, float* dt_out,
+                                float* flip_out, int32_t* record_out, uint32_t* code_out,
+                                int64_t capacity) {
+    HostProgram host;
+    int rc = compile_program(duration_s, kind, flip_rad, action, output_index, train_count,
+                             event_count, unmerged != 0, duration_tangent, &host);
+    if (rc) return rc;
+    if (op_count) *op_count = host.ops;
+    if (output_count) *output_count = host.outputs;
+    const int64_t n = std::min<int64_t>(capacity, int64_t(host.op.size()));
+    for (int64_t i = 0; i < n; ++i) {
+        if (dt_out) dt_out[i] = host.op[i].dt;
+        if (flip_out) flip_out[i] = host.op[i].flip;
+        if (record_out) record_out[i] = host.op[i].record;
+        if (code_out) code_out[i] = host.op[i].code;
+    }
+    return TSG_OK;
+}
+
+extern "C" int tsg_program_destroy(tsg_program* program) {
+    if (!program) return TSG_OK;
+    cudaFree(program->d_ops);
+    cudaFree(program->d_src);
+    delete program;
+    return TSG_OK;
+}
+
+extern "C" int tsg_program_info(const tsg_program* p, int64_t* trains, int64_t* ops,
+                                int64_t* outputs, int64_t* events) {
+    if (!p) return fail(TSG_ERR_ARGUMENT, "null program");
+    if (trains) *trains = p->host.trains;
+    if (ops) *ops = p->host.ops;
+    if (outputs) *outputs = p->host.outputs;
+    if (events) *events = p->host.events;
+    return TSG_OK;
+}
+
+extern "C" int tsg_epg_forward(const tsg_program* program, const tsg_tissue* tissue,
+                               int64_t atom_count, int64_t state_count, int layout,
+                               float* out_a, float* out_b, const tsg_launch* launch_shape,
+                               void* stream) {
+    int rc = check_common(program, tissue, atom_count, state_count);
+    if (rc) return rc;
+    if (layout == TSG_LAYOUT_PLANES ? !out_b : !out_a)
+        return fail(TSG_ERR_ARGUMENT, "null output buffer");
+    SweepArgs a = base_args(program, tissue, atom_count, state_count);
+    a.layout = layout;
+    a.sig_a = out_a;
+    a.sig_b = out_b;
+    return launch(MODE_FORWARD, program, a, atom_count, int(state_count), launch_shape,
+                  static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tsg_epg_forward_tangents(const tsg_program* program, const tsg_tissue* tissue,
+                                        int64_t atom_count, int64_t state_count,
+                                        unsigned tangent_mask, const int32_t* columns,
+                                        int32_t column_count, int layout, float* sig_a,
+                                        float* sig_b, float* jac_a, float* jac_b,
+                                        const tsg_launch* launch_shape, void* stream) {
+    int rc = check_common(program, tissue, atom_count, state_count);
+    if (rc) return rc;
+    if (!columns || column_count < 0) return fail(TSG_ERR_ARGUMENT, "null column map");
+    const int mode = mode_for_mask(tangent_mask);
+    if (mode < 0) return fail(TSG_ERR_UNSUPPORTED, "unknown tangent bits");
+    for (int i = 0; i < 5; ++i)
+        if (columns[i] >= column_count) return fail(TSG_ERR_ARGUMENT, "column out of range");
+    const unsigned bits[4] = {TSG_TANGENT_T1, TSG_TANGENT_T2, TSG_TANGENT_B1, TSG_TANGENT_INVERSION};
+    for (int i = 0; i < 4; ++i)
+        if (columns[i] >= 0 && !(tangent_mask & bits[i]))
+            return fail(TSG_ERR_ARGUMENT, "column given for a tangent not in the mask");
+    const bool any_col = columns[0] >= 0 || columns[1] >= 0 || columns[2] >= 0 ||
+                         columns[3] >= 0 || columns[4] >= 0;
+    if (any_col && (layout == TSG_LAYOUT_PLANES ? !jac_b : !jac_a))
+        return fail(TSG_ERR_ARGUMENT, "null Jacobian buffer");
+    SweepArgs a = base_args(program, tissue, atom_count, state_count);
+    a.layout = layout;
+    a.sig_a = sig_a;
+    a.sig_b = sig_b;
+    if (layout == TSG_LAYOUT_PLANES && !sig_b) a.sig_a = nullptr;
+    a.jac_a = jac_a;
+    a.jac_b = jac_b;
+    a.jac_cols = column_count;
+    a.col_t1 = columns[0];
+    a.col_t2 = columns[1];
+    a.col_b1 = columns[2];
+    a.col_inv = columns[3];
+    a.col_m0 = columns[4];
+    return launch(mode, program, a, atom_count, int(state_count), launch_shape,
+                  static_cast<cudaStream_t>(stream));
+}
+
+namespace tsg {
+namespace {
+
+// (d dt, d flip) per op from per-event directions, through the op sources.
+__global__ void gather_directions(const OpSource* src, int64_t n_ops, int64_t trains,
+                                  int64_t events, const float* ddur, const float* dflip,
+                                  float2* out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n_ops * trains) return;
+    const int64_t t = i / n_ops;
+    const OpSource s = src[i];
+    float a = 0.f, b = 0.f;
+    if (ddur && s.dt_event >= 0) a = ddur[t * events + s.dt_event];
+    if (dflip && s.rf_event >= 0) b = dflip[t * events + s.rf_event];
+    out[i] = make_float2(a, b);
+}
+
+}  // namespace
+}  // namespace tsg
+
+extern "C" int tsg_epg_tangent(const tsg_program* program, const tsg_tissue* tissue,
+                               int64_t atom_count, int64_t state_count,
+                               const tsg_direction* direction, float* out_real, float* out_imag,
+                               const tsg_launch* launch_shape, void* stream) {
+    int rc = check_common(program, tissue, atom_count, state_count);
+    if (rc) return rc;
+    if (!direction || !out_imag) return fail(TSG_ERR_ARGUMENT, "null direction or output");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t n = program->host.ops * program->host.trains;
+    float2* dirs = nullptr;
+    if (n > 0) {
+        TSG_CUDA(cudaMallocAsync(&dirs, size_t(n) * sizeof(float2), s));
+        gather_directions<<<unsigned((n + 255) / 256), 256, 0, s>>>(
+            program->d_src, program->host.ops, program->host.trains, program->host.events,
+            direction->duration_s, direction->flip_rad, dirs);
+    }
+    SweepArgs a = base_args(program, tissue, atom_count, state_count);
+    a.op_dir = dirs;
+    a.g_t1 = direction->t1_ms;
+    a.g_t2 = direction->t2_ms;
+    a.g_m0 = direction->m0;
+    a.g_b1 = direction->b1;
+    a.g_inv = direction->inversion;
+    a.layout = TSG_LAYOUT_PLANES;
+    a.jac_a = out_real;
+    a.jac_b = out_imag;
+    a.jac_cols = 1;
+    a.col_gen = 0;
+    rc = launch(MODE_GENERAL, program, a, atom_count, int(state_count), launch_shape, s);
+    if (dirs) cudaFreeAsync(dirs, s);
+    return rc;
+}
+
+// ---- host-buffer drop-ins --------------------------------------------------
+
+namespace tsg {
+namespace {
+
+constexpr int TISSUE_COUNT = 17, EVENT_COUNT = 9, PACKED_COUNT = 26, FLOAT_COUNT = 20,
+              TAIL_COUNT = 13;
+// Feature bits of the reference's mask (src/torchsim/_epg_cpu.cpp:91-98).
+constexpr int F_OFF_AXIS = 1, F_MOVING = 2, F_DIFFUSING = 4, F_TRANSMIT = 8, F_DENSITY = 16,
+              F_INVERTING = 32;
+
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+// Copies n host floats to a fresh device allocation.
+int upload(const void* host, size_t bytes, std::vector<void*>& owned, void** out,
+           cudaStream_t s) {
+    *out = nullptr;
+    if (!host || bytes == 0) return TSG_OK;
+    void* d = nullptr;
+    TSG_CUDA(cudaMallocAsync(&d, bytes, s));
+    owned.push_back(d);
+    TSG_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, s));
+    *out = d;
+    return TSG_OK;
+}
+
+int dense_device(size_t bytes, std::vector<void*>& owned, void** out, cudaStream_t s) {
+    void* d = nullptr;
+    TSG_CUDA(cudaMallocAsync(&d, bytes ? bytes : 4, s));
+    owned.push_back(d);
+    *out = d;
+    return TSG_OK;
+}
+
+void free_all(std::vector<void*>& owned, cudaStream_t s) {
+    for (void* p : owned) cudaFreeAsync(p, s);
+    owned.clear();
+}
+
+// The checks the real-subspace, single-pool subset needs of a pointer
+// sequence in the reference's order.
+int check_subset(void* const* ptrs, int64_t count, int64_t expected, int tail_begin,
+                 int64_t atoms, int real_axis, int features, int64_t trains) {
+    if (!ptrs || count != expected) return fail(TSG_ERR_ARGUMENT, "wrong number of buffer pointers");
+    if (real_axis != 1)
+        return fail(TSG_ERR_UNSUPPORTED, "only the real-subspace path (real_axis == 1) is built");
+    for (int i = 0; i < TAIL_COUNT; ++i)
+        if (ptrs[tail_begin + i] != nullptr)
+            return fail(TSG_ERR_UNSUPPORTED, "transition tables, pools and per-voxel pulses are not built");
+    if (features & F_MOVING) return fail(TSG_ERR_UNSUPPORTED, "flow is not built");
+    if (features & F_OFF_AXIS) {
+        // The caller established the real subspace; off-axis terms must be
+        // zero for that verdict, so they are only checked here.
+        for (int idx : {4, 5}) {
+            const float* v = static_cast<const float*>(ptrs[idx]);
+            if (v)
+                for (int64_t i = 0; i < atoms; ++i)
+                    if (v[i] != 0.f)
+                        return fail(TSG_ERR_UNSUPPORTED, "off-resonance / transmit phase leave the real subspace");
+        }
+    }
+    if (features & F_DIFFUSING) {
+        const float* d = static_cast<const float*>(ptrs[7]);
+        if (d)
+            for (int64_t i = 0; i < atoms; ++i)
+                if (d[i] != 0.f) return fail(TSG_ERR_UNSUPPORTED, "diffusion is not built");
+    }
+    for (int idx : {9, 12}) {  // bound_fraction, pool_b_fraction gate the second pools
+        const float* v = static_cast<const float*>(ptrs[idx]);
+        if (v)
+            for (int64_t i = 0; i < atoms; ++i)
+                if (v[i] != 0.f) return fail(TSG_ERR_UNSUPPORTED, "second pools are not built");
+    }
+    const int32_t* shim = static_cast<const int32_t*>(ptrs[TISSUE_COUNT + 6]);
+    (void)shim;  // a real-subspace run is single-shim: every index is row 0
+    (void)trains;
+    return TSG_OK;
+}
+
+std::mutex g_dropin_mutex;
+
+}  // namespace
+}  // namespace tsg
+
+extern "C" int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, int64_t atom_count,
+                                int64_t train_count, int64_t event_count, int64_t state_count,
+                                int64_t output_count, int real_axis, int features) {
+    constexpr int64_t expected = PACKED_COUNT + 2 + TAIL_COUNT;
+    if (atom_count < 0 || train_count < 1 || event_count < 0 || state_count < 1 || output_count < 0)
+        return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
+    int rc = check_subset(pointers, pointer_count, expected, PACKED_COUNT + 2, atom_count,
+                          real_axis, features, train_count);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> guard(g_dropin_mutex);
+    const float* duration = static_cast<const float*>(pointers[TISSUE_COUNT + 0]);
+    const int32_t* kind = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 1]);
+    const float* flip = static_cast<const float*>(pointers[TISSUE_COUNT + 2]);
+    const uint8_t* action = static_cast<const uint8_t*>(pointers[TISSUE_COUNT + 4]);
+    const int32_t* oindex = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 5]);
+    float* out_real = static_cast<float*>(pointers[PACKED_COUNT]);
+    float* out_imag = static_cast<float*>(pointers[PACKED_COUNT + 1]);
+    if (!out_real || !out_imag) return fail(TSG_ERR_ARGUMENT, "null output plane");
+    tsg_program* prog = nullptr;
+    rc = tsg_program_create(duration, kind, flip, action, oindex, train_count, event_count, 0,
+                            nullptr, &prog);
+    if (rc) return rc;
+    if (prog->host.outputs > output_count) {
+        tsg_program_destroy(prog);
+        return fail(TSG_ERR_ARGUMENT, "output index beyond output_count");
+    }
+    cudaStream_t s = nullptr;
+    std::vector<void*> owned;
+    const size_t abytes = size_t(atom_count) * sizeof(float);
+    void *t1, *t2, *m0 = nullptr, *b1 = nullptr, *inv = nullptr, *dr, *di;
+    rc = upload(pointers[0], abytes, owned, &t1, s);
+    if (!rc) rc = upload(pointers[1], abytes, owned, &t2, s);
+    if (!rc && (features & F_DENSITY)) rc = upload(pointers[2], abytes, owned, &m0, s);
+    if (!rc && (features & F_TRANSMIT)) rc = upload(pointers[3], abytes, owned, &b1, s);
+    if (!rc && (features & F_INVERTING)) rc = upload(pointers[6], abytes, owned, &inv, s);
+    const size_t obytes = size_t(train_count) * size_t(atom_count) * size_t(output_count) * 4;
+    if (!rc) rc = dense_device(obytes, owned, &dr, s);
+    if (!rc) rc = dense_device(obytes, owned, &di, s);
+    if (!rc && obytes) {
+        cudaMemsetAsync(dr, 0, obytes, s);
+        cudaMemsetAsync(di, 0, obytes, s);
+    }
+    if (!rc) {
+        // The kernels index outputs by the program's output count; the caller
+        // may give a wider row.
+        tsg_tissue tissue{static_cast<float*>(t1), static_cast<float*>(t2),
+                          static_cast<float*>(m0), static_cast<float*>(b1),
+                          static_cast<float*>(inv)};
+        prog->host.outputs = output_count;
+        rc = tsg_epg_forward(prog, &tissue, atom_count, state_count, TSG_LAYOUT_PLANES,
+                             static_cast<float*>(dr), static_cast<float*>(di), nullptr, s);
+    }
+    if (!rc && obytes) {
+        cudaError_t e1 = cudaMemcpyAsync(out_real, dr, obytes, cudaMemcpyDeviceToHost, s);
+        cudaError_t e2 = cudaMemcpyAsync(out_imag, di, obytes, cudaMemcpyDeviceToHost, s);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            rc = cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaMemcpyAsync(outputs)");
+    }
+    free_all(owned, s);
+    cudaError_t es = cudaStreamSynchronize(s);
+    if (!rc && es != cudaSuccess) rc = cuda_fail(es, "cudaStreamSynchronize");
+    tsg_program_destroy(prog);
+    return rc;
+}
+
+extern "C" int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count,
+                                    int64_t atom_count, int64_t train_count, int64_t event_count,
+                                    int64_t state_count, int64_t output_count, int real_axis,
+                                    int features) {
+    constexpr int64_t expected = PACKED_COUNT + FLOAT_COUNT + 2 + TAIL_COUNT;
+    if (atom_count < 0 || train_count < 1 || event_count < 0 || state_count < 1 || output_count < 0)
+        return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
+    int rc = check_subset(pointers, pointer_count, expected, PACKED_COUNT + FLOAT_COUNT + 2,
+                          atom_count, real_axis, features, train_count);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> guard(g_dropin_mutex);
+    void* const* tan = pointers + PACKED_COUNT;  // FLOAT_INPUTS order
+    const float* duration = static_cast<const float*>(pointers[TISSUE_COUNT + 0]);
+    const int32_t* kind = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 1]);
+    const float* flip = static_cast<const float*>(pointers[TISSUE_COUNT + 2]);
+    const uint8_t* action = static_cast<const uint8_t*>(pointers[TISSUE_COUNT + 4]);
+    const int32_t* oindex = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 5]);
+    const float* dur_tangent = static_cast<const float*>(tan[TISSUE_COUNT + 0]);
+    float* out_real = static_cast<float*>(pointers[PACKED_COUNT + FLOAT_COUNT]);
+    float* out_imag = static_cast<float*>(pointers[PACKED_COUNT + FLOAT_COUNT + 1]);
+    if (!out_real || !out_imag) return fail(TSG_ERR_ARGUMENT, "null output plane");
+    tsg_program* prog = nullptr;
+    rc = tsg_program_create(duration, kind, flip, action, oindex, train_count, event_count, 0,
+                            dur_tangent, &prog);
+    if (rc) return rc;
+    if (prog->host.outputs > output_count) {
+        tsg_program_destroy(prog);
+        return fail(TSG_ERR_ARGUMENT, "output index beyond output_count");
+    }
+    cudaStream_t s = nullptr;
+    std::vector<void*> owned;
+    const size_t abytes = size_t(atom_count) * sizeof(float);
+    const size_t ebytes = size_t(train_count) * size_t(event_count) * sizeof(float);
+    void *t1, *t2, *m0 = nullptr, *b1 = nullptr, *inv = nullptr;
+    void *g[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void *dr, *di;
+    rc = upload(pointers[0], abytes, owned, &t1, s);
+    if (!rc) rc = upload(pointers[1], abytes, owned, &t2, s);
+    if (!rc && (features & F_DENSITY)) rc = upload(pointers[2], abytes, owned, &m0, s);
+    if (!rc && (features & F_TRANSMIT)) rc = upload(pointers[3], abytes, owned, &b1, s);
+    if (!rc && (features & F_INVERTING)) rc = upload(pointers[6], abytes, owned, &inv, s);
+    // Tangents: t1, t2, m0, b1 (index 3), inversion (6); duration, flip.
+    const int tissue_idx[5] = {0, 1, 2, 3, 6};
+    for (int k = 0; k < 5 && !rc; ++k) rc = upload(tan[tissue_idx[k]], abytes, owned, &g[k], s);
+    if (!rc) rc = upload(tan[TISSUE_COUNT + 0], ebytes, owned, &g[5], s);
+    if (!rc) rc = upload(tan[TISSUE_COUNT + 1], ebytes, owned, &g[6], s);
+    const size_t obytes = size_t(train_count) * size_t(atom_count) * size_t(output_count) * 4;
+    if (!rc) rc = dense_device(obytes, owned, &dr, s);
+    if (!rc) rc = dense_device(obytes, owned, &di, s);
+    if (!rc && obytes) {
+        cudaMemsetAsync(dr, 0, obytes, s);
+        cudaMemsetAsync(di, 0, obytes, s);
+    }
+    if (!rc) {
+        tsg_tissue tissue{static_cast<float*>(t1), static_cast<float*>(t2),
+                          static_cast<float*>(m0), static_cast<float*>(b1),
+                          static_cast<float*>(inv)};
+        tsg_direction dir{static_cast<float*>(g[0]), static_cast<float*>(g[1]),
+                          static_cast<float*>(g[2]), static_cast<float*>(g[3]),
+                          static_cast<float*>(g[4]), static_cast<float*>(g[5]),
+                          static_cast<float*>(g[6])};
+        prog->host.outputs = output_count;
+        rc = tsg_epg_tangent(prog, &tissue, atom_count, state_count, &dir,
+                             static_cast<float*>(dr), static_cast<float*>(di), nullptr, s);
+    }
+    if (!rc && obytes) {
+        cudaError_t e1 = cudaMemcpyAsync(out_real, dr, obytes, cudaMemcpyDeviceToHost, s);
+        cudaError_t e2 = cudaMemcpyAsync(out_imag, di, obytes, cudaMemcpyDeviceToHost, s);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            rc = cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaMemcpyAsync(outputs)");
+    }
+    free_all(owned, s);
+    cudaError_t es = cudaStreamSynchronize(s);
+    if (!rc && es != cudaSuccess) rc = cuda_fail(es, "cudaStreamSynchronize");
+    tsg_program_destroy(prog);
+    return rc;
+}
+
+// ---- measurement ------------------------------------------------------------
+
+namespace tsg {
+namespace {
+
+// Eight independent FMA chains per thread: the FP32 CUDA-core issue rate with
+// nothing else in the way, the denominator of the sweep kernels' roofline.
+__global__ void fp32_probe_kernel(float* out, int iters, float seed) {
+    float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+    float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+    const float b = 0.999999f, c = 1e-6f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+            a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+        }
+    }
+    const float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 123456.f) out[blockIdx.x] = s;  // keeps the chains live
+}
+
+}  // namespace
+}  // namespace tsg
+
+extern "C" int tsg_probe_fp32(int64_t blocks, int threads, int iters, float* out, void* stream,
+                              double* flops) {
+    if (blocks < 1 || threads < 32 || threads > 1024 || iters < 1 || !out)
+        return fail(TSG_ERR_ARGUMENT, "invalid probe shape");
+    fp32_probe_kernel<<<unsigned(blocks), threads, 0, static_cast<cudaStream_t>(stream)>>>(
+        out, iters, 1.0f);
+    TSG_CUDA(cudaGetLastError());
+    if (flops) *flops = double(blocks) * threads * double(iters) * 4.0 * 8.0 * 2.0;
+    return TSG_OK;
+}

@@ -1,0 +1,16 @@
+// Forward plus the T1, T2 and B1 tangents in one pass (dictionary Jacobian).
+#include "epg_sweep.cuh"
+
+namespace tsg {
+const SweepEntry kSweepT12B[] = {
+    TSG_SWEEP_ENTRY(MODE_T12B, 5, 2, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 3, 4, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 4, 4, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 5, 4, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 3, 8, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 4, 8, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 4, 16, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 4, 32, 7, false),
+};
+const int kSweepT12BCount = sizeof(kSweepT12B) / sizeof(kSweepT12B[0]);
+}  // namespace tsg

@@ -1,0 +1,157 @@
+// Internal definitions shared by the kernels and the C ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/torchsim_gb300.h"
+
+namespace tsg {
+
+// The packed action word (src/torchsim/_epg_cpu.cpp:36-41).
+constexpr uint8_t A_PRE_SHIFT = 1;
+constexpr uint8_t A_POST_SHIFT = 2;
+constexpr uint8_t A_INVERSION = 4;
+constexpr uint8_t A_SPOIL_AFTER = 8;
+constexpr uint8_t A_SHIFT_AFTER = 16;
+constexpr uint8_t A_RECORD = 32;
+
+// One op of a compiled pulse program: a fixed template of micro-steps that
+// one or more consecutive events reduce to, run in this order:
+//   relax(dt) | shift x n1 | rf (rotate or invert) | shift x n2 | spoil |
+//   record | shift x n3 | spoil
+// An MRF repetition (pulse, sample, unbalanced gradient, delay) is one op.
+struct __align__(16) Op {
+    float dt;        // relaxation interval in seconds (RELAX set)
+    float flip;      // flip angle in radians (rotate)
+    int32_t record;  // output index (RECORD set)
+    uint32_t code;   // micro-step bits below
+};
+
+constexpr uint32_t OP_RELAX = 1u << 0;
+constexpr uint32_t OP_SHIFT1_SHIFT = 1;   // bits 1-2
+constexpr uint32_t OP_RF_SHIFT = 3;       // bits 3-4: 0 none, 1 rotate, 2 invert
+constexpr uint32_t OP_SHIFT2_SHIFT = 5;   // bits 5-6
+constexpr uint32_t OP_SPOIL1 = 1u << 7;
+constexpr uint32_t OP_RECORD = 1u << 8;
+constexpr uint32_t OP_SHIFT3_SHIFT = 9;   // bits 9-10
+constexpr uint32_t OP_SPOIL2 = 1u << 11;
+constexpr int RF_NONE = 0, RF_ROTATE = 1, RF_INVERT = 2;
+
+__host__ __device__ inline int op_shift1(uint32_t c) { return (c >> OP_SHIFT1_SHIFT) & 3; }
+__host__ __device__ inline int op_rf(uint32_t c) { return (c >> OP_RF_SHIFT) & 3; }
+__host__ __device__ inline int op_shift2(uint32_t c) { return (c >> OP_SHIFT2_SHIFT) & 3; }
+__host__ __device__ inline int op_shift3(uint32_t c) { return (c >> OP_SHIFT3_SHIFT) & 3; }
+
+// Where each op's dt and flip came from in the event stream, for the
+// per-event gradients of the adjoint and the per-event directions of a
+// general tangent. -1: the op has no such step.
+struct OpSource {
+    int32_t dt_event;
+    int32_t rf_event;
+};
+
+struct HostProgram {
+    int64_t trains = 0;
+    int64_t events = 0;
+    int64_t ops = 0;       // per train (trains padded to the longest)
+    int64_t outputs = 0;   // recorded samples per train
+    bool sequential_records = true;  // records appear as 0,1,2,... in op order
+    std::vector<Op> op;              // [train][ops]
+    std::vector<OpSource> src;       // [train][ops]
+};
+
+}  // namespace tsg
+
+struct tsg_program {
+    tsg::HostProgram host;
+    tsg::Op* d_ops = nullptr;
+    tsg::OpSource* d_src = nullptr;
+    int device = 0;
+};
+
+namespace tsg {
+
+// Sets the thread's last error and returns code.
+int fail(int code, const std::string& message);
+int cuda_fail(cudaError_t err, const char* where);
+#define TSG_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return ::tsg::cuda_fail(_e, #call); \
+    } while (0)
+
+int compile_program(const float* duration, const int32_t* kind, const float* flip,
+                    const uint8_t* action, const int32_t* output_index, int64_t trains,
+                    int64_t events, bool unmerged, const float* duration_tangent,
+                    HostProgram* out);
+
+// Arguments of one sweep launch (forward, fused tangents, general tangent).
+struct SweepArgs {
+    const Op* ops;
+    const float2* op_dir;  // general tangent: (d dt, d flip) per op, [train][ops]
+    int n_ops;
+    int64_t atoms;
+    int states;
+    int outputs;
+    const float* t1;
+    const float* t2;
+    const float* m0;
+    const float* b1;
+    const float* inv;
+    const float* g_t1;
+    const float* g_t2;
+    const float* g_m0;
+    const float* g_b1;
+    const float* g_inv;
+    int layout;
+    float* sig_a;
+    float* sig_b;
+    float* jac_a;
+    float* jac_b;
+    int jac_cols;
+    int col_t1, col_t2, col_b1, col_inv, col_m0, col_gen;
+    // Optional state checkpoints for the adjoint: every ckpt_every ops the
+    // state entering that op is stored, [train][atom][k][3*states].
+    float* ckpt;
+    int ckpt_every;
+    int ckpt_count;
+};
+
+using SweepLaunch = void (*)(const SweepArgs&, dim3 grid, dim3 block, size_t smem,
+                             cudaStream_t stream);
+
+// Kernel families (which tangent systems a sweep carries).
+enum SweepMode : int {
+    MODE_FORWARD = 0,   // primal only
+    MODE_T12 = 3,       // T1, T2
+    MODE_T12B = 7,      // T1, T2, B1
+    MODE_T12BI = 15,    // T1, T2, B1, inversion
+    MODE_GENERAL = 16,  // one general direction
+};
+
+struct SweepEntry {
+    int mode;
+    int orders_per_lane;  // R
+    int lanes_per_voxel;  // L
+    SweepLaunch launch;
+};
+
+// Tables defined by the per-mode translation units.
+extern const SweepEntry kSweepForward[];
+extern const int kSweepForwardCount;
+extern const SweepEntry kSweepT12[];
+extern const int kSweepT12Count;
+extern const SweepEntry kSweepT12B[];
+extern const int kSweepT12BCount;
+extern const SweepEntry kSweepT12BI[];
+extern const int kSweepT12BICount;
+extern const SweepEntry kSweepGeneral[];
+extern const int kSweepGeneralCount;
+
+constexpr int kOpChunk = 1024;  // ops staged in shared memory at a time
+
+}  // namespace tsg

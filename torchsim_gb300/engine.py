@@ -1,0 +1,198 @@
+"""Device-side calls into the CUDA library with torch tensors.
+
+This is the layer the reference's ``_run_packed`` / ``_run_packed_jvp``
+(``src/torchsim/sequence/_accelerators.py:3262, 3933``) occupy: it takes the
+tissue maps and a compiled pulse program and launches the sweep kernels on the
+current CUDA stream. Everything stays on the device; nothing synchronises the
+host.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections.abc import Sequence
+from dataclasses import dataclass
+
+import torch
+
+from . import _native
+from .sequence import Program
+
+# Public property names -> (tangent bit or None for the free M0 column, kernel slot).
+DIFFERENTIABLE = {
+    "T1": (_native.TANGENT_T1, 0),
+    "T2": (_native.TANGENT_T2, 1),
+    "B1": (_native.TANGENT_B1, 2),
+    "inv_efficiency": (_native.TANGENT_INVERSION, 3),
+    "M0": (0, 4),
+}
+
+
+def require_cuda(device: torch.device | None = None) -> torch.device:
+    """The CUDA device to run on; raises when there is none (no CPU path)."""
+    if not torch.cuda.is_available():
+        raise RuntimeError("torchsim_gb300 runs on a CUDA GPU only; none is available")
+    if device is None or device.type != "cuda":
+        return torch.device("cuda", torch.cuda.current_device())
+    return device
+
+
+@dataclass
+class TissueMaps:
+    """Flat per-voxel tissue on the device (float32, contiguous)."""
+
+    t1: torch.Tensor
+    t2: torch.Tensor
+    m0: torch.Tensor | None = None
+    b1: torch.Tensor | None = None
+    inv: torch.Tensor | None = None
+
+    @property
+    def voxels(self) -> int:
+        return int(self.t1.numel())
+
+    def struct(self) -> _native.Tissue:
+        def ptr(t):
+            return None if t is None else t.data_ptr()
+
+        return _native.Tissue(ptr(self.t1), ptr(self.t2), ptr(self.m0), ptr(self.b1),
+                              ptr(self.inv))
+
+
+# The reference clamps relaxation times away from zero before any kernel sees
+# them (sequence/_simulation.py:59, _prepare_tissue 661-737).
+MINIMUM_RELAXATION_TIME_MS = 1e-6
+
+
+def tissue_maps(device: torch.device, voxels: int, T1, T2, M0=None, B1=None,
+                inv=None) -> TissueMaps:
+    """Broadcast each property to ``voxels`` float32 entries on ``device``.
+
+    A property left at ``None`` is not given to the kernel, which then uses
+    its identity value (1), as the reference's feature mask does.
+    """
+
+    def flat(value, clamp=False):
+        if value is None:
+            return None
+        t = torch.as_tensor(value, dtype=torch.float32, device=device)
+        t = t.reshape(-1) if t.numel() == voxels else t.reshape(()).expand(voxels)
+        if clamp:
+            t = t.clamp_min(MINIMUM_RELAXATION_TIME_MS)
+        return t.contiguous()
+
+    return TissueMaps(flat(T1, True), flat(T2, True), flat(M0), flat(B1), flat(inv))
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def forward(program: Program, tissue: TissueMaps, states: int, *, planes: bool = False,
+            launch=None, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Recorded signal, ``1j * i*m0*F+[0]`` as complex64 ``(trains*voxels, outputs)``.
+
+    With ``planes`` the reference's two float planes are returned instead,
+    stacked as ``(2, trains*voxels, outputs)``.
+    """
+    rows = program.trains * tissue.voxels
+    device = tissue.t1.device
+    lib = _native.library()
+    t = tissue.struct()
+    if planes:
+        res = torch.empty((2, rows, program.outputs), dtype=torch.float32, device=device)
+        _native.check(lib.tsg_epg_forward(program.handle, ctypes.byref(t), tissue.voxels, states,
+                                          _native.LAYOUT_PLANES, res[0].data_ptr(),
+                                          res[1].data_ptr(), _native.launch_shape(launch),
+                                          _stream()))
+        return res
+    res = out if out is not None else torch.empty((rows, program.outputs), dtype=torch.complex64,
+                                                  device=device)
+    _native.check(lib.tsg_epg_forward(program.handle, ctypes.byref(t), tissue.voxels, states,
+                                      _native.LAYOUT_COMPLEX_IJ, res.data_ptr(), None,
+                                      _native.launch_shape(launch), _stream()))
+    return res
+
+
+def plan_tangents(names: Sequence[str]) -> tuple[int, list[int]]:
+    """Tangent mask and the 5-slot column map for an ordered list of names."""
+    mask = 0
+    columns = [-1] * 5
+    for col, name in enumerate(names):
+        if name not in DIFFERENTIABLE:
+            raise ValueError(f"{name!r} does not carry a derivative on this path; "
+                             f"choose from {sorted(DIFFERENTIABLE)}")
+        bit, slot = DIFFERENTIABLE[name]
+        if columns[slot] >= 0:
+            raise ValueError(f"{name!r} is named twice")
+        mask |= bit
+        columns[slot] = col
+    return mask, columns
+
+
+def forward_tangents(program: Program, tissue: TissueMaps, states: int, names: Sequence[str], *,
+                     with_signal: bool = True, planes: bool = False, launch=None,
+                     sig_out: torch.Tensor | None = None, jac_out: torch.Tensor | None = None):
+    """Signal and Jacobian columns ``names`` in ONE fused pass.
+
+    Returns ``(signal (rows, P), jacobian (rows, k, P))`` complex64 holding
+    ``1j * i*m0*F+[0]`` and its derivatives (or planes with ``planes``).
+    """
+    mask, columns = plan_tangents(names)
+    rows = program.trains * tissue.voxels
+    k = len(names)
+    device = tissue.t1.device
+    lib = _native.library()
+    t = tissue.struct()
+    cols = (ctypes.c_int32 * 5)(*columns)
+    if planes:
+        sig = torch.empty((2, rows, program.outputs), dtype=torch.float32, device=device)
+        jac = torch.empty((2, rows, k, program.outputs), dtype=torch.float32, device=device)
+        _native.check(lib.tsg_epg_forward_tangents(
+            program.handle, ctypes.byref(t), tissue.voxels, states, mask, cols, k,
+            _native.LAYOUT_PLANES, sig[0].data_ptr(), sig[1].data_ptr(), jac[0].data_ptr(),
+            jac[1].data_ptr(), _native.launch_shape(launch), _stream()))
+        return sig, jac
+    sig = None
+    if with_signal:
+        sig = sig_out if sig_out is not None else torch.empty(
+            (rows, program.outputs), dtype=torch.complex64, device=device)
+    jac = jac_out if jac_out is not None else torch.empty(
+        (rows, k, program.outputs), dtype=torch.complex64, device=device)
+    _native.check(lib.tsg_epg_forward_tangents(
+        program.handle, ctypes.byref(t), tissue.voxels, states, mask, cols, k,
+        _native.LAYOUT_COMPLEX_IJ, None if sig is None else sig.data_ptr(), None,
+        jac.data_ptr(), None, _native.launch_shape(launch), _stream()))
+    return sig, jac
+
+
+def tangent(program: Program, tissue: TissueMaps, states: int, *, t1=None, t2=None, m0=None,
+            b1=None, inv=None, duration=None, flip=None, launch=None) -> torch.Tensor:
+    """One general forward-mode direction; returns the tangent's imaginary
+    plane ``(rows, P)`` (the real plane is zero), as ``simulate_jvp`` does.
+
+    ``duration``/``flip`` directions are per (train, event) of the program's
+    event stream; the program must have been compiled with ``duration``.
+    """
+    device = tissue.t1.device
+    rows = program.trains * tissue.voxels
+    keep = []
+
+    def ptr(v, n):
+        if v is None:
+            return None
+        t = torch.as_tensor(v, dtype=torch.float32, device=device).reshape(-1)
+        t = (t if t.numel() == n else t.expand(n)).contiguous()
+        keep.append(t)
+        return t.data_ptr()
+
+    ev = program.trains * program.events.events
+    d = _native.Direction(ptr(t1, tissue.voxels), ptr(t2, tissue.voxels), ptr(m0, tissue.voxels),
+                          ptr(b1, tissue.voxels), ptr(inv, tissue.voxels), ptr(duration, ev),
+                          ptr(flip, ev))
+    res = torch.empty((2, rows, program.outputs), dtype=torch.float32, device=device)
+    ts = tissue.struct()
+    _native.check(_native.library().tsg_epg_tangent(
+        program.handle, ctypes.byref(ts), tissue.voxels, states, ctypes.byref(d),
+        res[0].data_ptr(), res[1].data_ptr(), _native.launch_shape(launch), _stream()))
+    return res[1]

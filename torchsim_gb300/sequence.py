@@ -1,0 +1,309 @@
+"""Event streams for the sequences on the accelerated path, packed as the
+reference packs them, and compiled into device pulse programs.
+
+The packed layout is the reference's kernel ABI
+(``src/torchsim/sequence/_accelerators.py:_pack_events``, 913-1170): per event
+a ``duration`` (seconds since the previous event, read off a clock by one
+difference), a ``kind`` (0 wait, 1 RF, 2 ADC), a ``flip`` and ``phase`` in
+radians, an ``action`` bit word and an ``output_index`` (-1 if not recorded).
+
+The builders below lay out the same events, in the same order and with the
+same clock arithmetic, as the reference's simulators:
+
+* :func:`mrf_events` — ``MRFSimulator.layout`` (``simulators/mrf.py:46-77``):
+  an inversion, then per repetition an excitation and an SSFP-FID readout
+  (sample, unbalanced gradient, delay of TR), the last playing recorded.
+* :func:`fse_events` — ``FSESimulator._train`` (``simulators/fse.py:75-104``):
+  an excitation, then per echo a crushed refocusing pulse at (j - 1/2) ESP
+  and a sample at j ESP.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import math
+import threading
+from dataclasses import dataclass, field
+from typing import Any
+
+import numpy as np
+import torch
+
+from . import _native
+
+# The packed action word (sequence/_accelerators.py:77-84).
+PRE_SHIFT = 1
+POST_SHIFT = 2
+INVERSION = 4
+SPOIL_AFTER = 8
+SHIFT_AFTER = 16
+RECORD = 32
+EXCITATION = 64
+REFOCUSING = 128
+
+WAIT, RF, ADC = 0, 1, 2
+
+# The time integral of the reference's default hard-pulse envelope on its
+# 1 us raster (``RfDefinition.integral``, sequence/_description.py:463-510).
+# A pulse's flip is stored as an amplitude and read back as
+# 2*pi*|amplitude*area| in float32 (``flip_angle``, :542-568), which is what
+# puts its last bit where the reference has it.
+_HARD_PULSE_AREA = 0.15915493667125702
+
+
+def _played_flip(angles: torch.Tensor) -> np.ndarray:
+    amplitude = angles.to(torch.float32)
+    return (2.0 * torch.pi * torch.abs(amplitude * _HARD_PULSE_AREA)).numpy()
+
+
+@dataclass
+class PackedEvents:
+    """One event stream in the reference's packed layout (NumPy, host)."""
+
+    duration: np.ndarray  # float32 (trains, events)
+    kind: np.ndarray  # int32 (events,)
+    flip: np.ndarray  # float32 (trains, events)
+    phase: np.ndarray  # float32 (trains, events)
+    action: np.ndarray  # uint8 (events,)
+    output_index: np.ndarray  # int32 (events,)
+    time_us: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+
+    @property
+    def trains(self) -> int:
+        return int(self.duration.shape[0])
+
+    @property
+    def events(self) -> int:
+        return int(self.kind.shape[0])
+
+    @property
+    def outputs(self) -> int:
+        recorded = self.output_index[self.output_index >= 0]
+        return int(recorded.max()) + 1 if recorded.size else 0
+
+    def key(self) -> str:
+        h = hashlib.sha1()
+        for a in (self.duration, self.kind, self.flip, self.action, self.output_index):
+            h.update(np.ascontiguousarray(a).tobytes())
+            h.update(str(a.shape).encode())
+        return h.hexdigest()
+
+    def real_axis(self, tol: float = 0.0) -> int:
+        """1 when the stream stays in the real subspace, else -1.
+
+        The real subspace holds when every non-inversion RF pulse and every
+        recorded sample share one phase (the kernel records i*m0*F+[0] in
+        that frame), which is the condition the reference's real kernels
+        assume (src/torchsim/_epg_cpu.cpp:3031-3039).
+        """
+        turning = (self.kind == RF) & ((self.action & INVERSION) == 0)
+        sampled = (self.kind == ADC) & ((self.action & RECORD) != 0)
+        phases = np.concatenate([self.phase[:, turning].ravel(), self.phase[:, sampled].ravel()])
+        if phases.size == 0:
+            return 1
+        return 1 if np.all(np.abs(phases - phases[0]) <= tol) else -1
+
+
+def _clock_to_durations(clock: torch.Tensor) -> np.ndarray:
+    """Intervals as the reference reads them off its clock: one difference,
+    scaled to seconds, narrowed to float32 (_accelerators.py:1125-1128)."""
+    intervals = (torch.diff(clock, prepend=clock.new_zeros(1)) * 1e-6).to(torch.float32)
+    return intervals.numpy()
+
+
+def _as_tensor(value: Any) -> torch.Tensor:
+    if isinstance(value, torch.Tensor):
+        return value.detach().cpu()
+    return torch.as_tensor(np.asarray(value) if not isinstance(value, (int, float)) else value)
+
+
+def _matched(value: Any, reference: torch.Tensor) -> torch.Tensor:
+    held = _as_tensor(value).to(reference.dtype)
+    if held.numel() == 1:
+        return held.reshape(()).expand(reference.shape)
+    if held.shape != reference.shape:
+        raise ValueError(
+            f"expected one value per event or a single one, got {tuple(held.shape)} "
+            f"against {tuple(reference.shape)}"
+        )
+    return held
+
+
+def mrf_events(flip_deg: Any, TR_ms: Any, TI_ms: Any = 0.0, phases_deg: Any = 0.0,
+               repetitions: int = 1) -> PackedEvents:
+    """The MRF train of ``MRFSimulator.layout`` (simulators/mrf.py:46-77).
+
+    Per repetition: an ideal inversion (held TI), then for each flip an
+    excitation followed by a sample, one unbalanced gradient and the rest of
+    the TR. Only the last playing is recorded (``_pack_events``'s
+    ``repetitions``).
+    """
+    angles = torch.deg2rad(torch.atleast_1d(_as_tensor(flip_deg)))
+    if angles.ndim != 1:
+        raise ValueError("flip must be one angle per repetition")
+    turns = torch.deg2rad(_matched(phases_deg, angles))
+    spacing_s = _matched(TR_ms, angles) * 1e-3
+    n = int(angles.numel())
+    # Clock as compose() walks it: the inversion at 0, each repetition's
+    # events at the cursor, the cursor moved on by the readout's duration.
+    ti = TI_ms * 1e-3 if isinstance(TI_ms, (int, float)) else _as_tensor(TI_ms) * 1e-3
+    cursor: Any = 0.0 + ti
+    starts: list[Any] = []
+    for index in range(n):
+        starts.append(cursor)
+        cursor = cursor + spacing_s[index]
+    played_s = cursor
+    stamps: list[Any] = [1e6 * 0.0]
+    for start in starts:
+        stamp = 1e6 * start
+        stamps.extend([stamp, stamp, stamp, stamp])
+    per_rep = 1 + 4 * n
+    clock: list[Any] = []
+    tr_us = 1e6 * played_s
+    for rep in range(repetitions):
+        for stamp in stamps:
+            clock.append(tr_us * rep + stamp if rep else stamp)
+    if any(isinstance(v, torch.Tensor) for v in clock):
+        clock_t = torch.stack([torch.as_tensor(v, dtype=torch.float32).reshape(()) for v in clock])
+    else:
+        clock_t = torch.tensor(clock, dtype=torch.float64)
+    kind = np.zeros(per_rep, np.int32)
+    action = np.zeros(per_rep, np.uint8)
+    flip = np.zeros(per_rep, np.float32)
+    phase = np.zeros(per_rep, np.float32)
+    kind[0] = RF
+    action[0] = INVERSION
+    a32 = _played_flip(angles)
+    p32 = turns.to(torch.float32).numpy()
+    exc = 1 + 4 * np.arange(n)
+    kind[exc] = RF
+    action[exc] = EXCITATION
+    flip[exc] = a32
+    phase[exc] = p32
+    kind[exc + 1] = ADC
+    phase[exc + 1] = p32
+    action[exc + 2] = POST_SHIFT
+    kind_all = np.tile(kind, repetitions)
+    action_all = np.tile(action, repetitions)
+    flip_all = np.tile(flip, repetitions)
+    phase_all = np.tile(phase, repetitions)
+    output_index = np.full(per_rep * repetitions, -1, np.int32)
+    last = (repetitions - 1) * per_rep
+    output_index[last + exc + 1] = np.arange(n, dtype=np.int32)
+    action_all[last + exc + 1] |= RECORD
+    duration = _clock_to_durations(clock_t)
+    recorded = output_index >= 0
+    return PackedEvents(
+        duration=duration[None, :].copy(),
+        kind=kind_all,
+        flip=flip_all[None, :].copy(),
+        phase=phase_all[None, :].copy(),
+        action=action_all,
+        output_index=output_index,
+        time_us=clock_t.to(torch.float32).numpy()[recorded],
+    )
+
+
+def fse_events(flip_deg: Any, ESP_ms: float, phases_deg: Any = 0.0, exc_flip: float = 90.0,
+               exc_phase: float = 90.0) -> PackedEvents:
+    """The refocused train of ``FSESimulator._train`` (simulators/fse.py:75-104)."""
+    angles = torch.deg2rad(torch.atleast_1d(_as_tensor(flip_deg)))
+    turns = torch.deg2rad(_matched(phases_deg, angles))
+    if angles.ndim != 1:
+        raise ValueError("flip must be one angle per echo")
+    n = int(angles.numel())
+    spacing_s = float(ESP_ms) * 1e-3
+    events = 1 + 3 * n
+    kind = np.zeros(events, np.int32)
+    action = np.zeros(events, np.uint8)
+    flip = np.zeros(events, np.float32)
+    phase = np.zeros(events, np.float32)
+    output_index = np.full(events, -1, np.int32)
+    clock = [0.0]
+    kind[0] = RF
+    action[0] = EXCITATION
+    flip[0] = _played_flip(torch.tensor([math.pi / 180.0 * exc_flip]))[0]
+    phase[0] = np.float32(math.pi / 180.0 * exc_phase)
+    a32 = _played_flip(angles)
+    p32 = turns.to(torch.float32).numpy()
+    for index in range(n):
+        echo_s = (index + 1) * spacing_s
+        base = 1 + 3 * index
+        kind[base] = RF
+        action[base] = REFOCUSING | PRE_SHIFT | POST_SHIFT
+        flip[base] = a32[index]
+        phase[base] = p32[index]
+        kind[base + 1] = ADC
+        action[base + 1] = RECORD
+        phase[base + 1] = p32[index]
+        output_index[base + 1] = index
+        clock.extend([1e6 * (echo_s - 0.5 * spacing_s), 1e6 * echo_s, 1e6 * echo_s])
+    clock_t = torch.tensor(clock, dtype=torch.float64)
+    recorded = output_index >= 0
+    return PackedEvents(
+        duration=_clock_to_durations(clock_t)[None, :].copy(),
+        kind=kind,
+        flip=flip[None, :].copy(),
+        phase=phase[None, :].copy(),
+        action=action,
+        output_index=output_index,
+        time_us=clock_t.to(torch.float32).numpy()[recorded],
+    )
+
+
+class Program:
+    """A compiled pulse program resident on the current CUDA device."""
+
+    def __init__(self, events: PackedEvents, unmerged: bool = False,
+                 duration_tangent: np.ndarray | None = None) -> None:
+        lib = _native.library()
+        self.events = events
+        dur = np.ascontiguousarray(events.duration, np.float32)
+        kind = np.ascontiguousarray(events.kind, np.int32)
+        flip = np.ascontiguousarray(events.flip, np.float32)
+        action = np.ascontiguousarray(events.action, np.uint8)
+        oi = np.ascontiguousarray(events.output_index, np.int32)
+        tangent = None if duration_tangent is None else np.ascontiguousarray(
+            np.broadcast_to(duration_tangent, dur.shape), np.float32)
+        handle = _native.ctypes.c_void_p()
+        _native.check(lib.tsg_program_create(
+            dur.ctypes.data, kind.ctypes.data, flip.ctypes.data, action.ctypes.data,
+            oi.ctypes.data, events.trains, events.events, int(unmerged),
+            None if tangent is None else tangent.ctypes.data, _native.ctypes.byref(handle)))
+        self.handle = handle
+        i64 = _native.ctypes.c_int64
+        trains, ops, outputs, nev = i64(), i64(), i64(), i64()
+        _native.check(lib.tsg_program_info(handle, _native.ctypes.byref(trains),
+                                           _native.ctypes.byref(ops), _native.ctypes.byref(outputs),
+                                           _native.ctypes.byref(nev)))
+        self.trains = trains.value
+        self.ops = ops.value
+        self.outputs = outputs.value
+
+    def __del__(self) -> None:
+        handle = getattr(self, "handle", None)
+        if handle is not None and handle.value:
+            try:
+                _native.library().tsg_program_destroy(handle)
+            except Exception:  # pragma: no cover - interpreter shutdown
+                pass
+            self.handle = None
+
+
+_cache: dict[tuple, Program] = {}
+_cache_lock = threading.Lock()
+
+
+def program_for(events: PackedEvents, device: torch.device | None = None) -> Program:
+    """The compiled program of a stream, cached by content and device."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    key = (events.key(), device.index)
+    with _cache_lock:
+        hit = _cache.get(key)
+        if hit is None:
+            with torch.cuda.device(device):
+                hit = Program(events)
+            if len(_cache) > 64:
+                _cache.pop(next(iter(_cache)))
+            _cache[key] = hit
+    return hit

@@ -1,0 +1,268 @@
+"""The reference's simulator API on the GB300 path.
+
+``MRFSimulator`` / ``FSESimulator`` keep the reference's call shape
+(``src/torchsim/model/_signal.py:158-240``): properties and protocol are
+given together, ``simulate(**values)`` returns the signal with the voxel axes
+of the properties, and ``jacobian(diff, **values)`` returns ``(signal,
+jacobian)`` with the parameter axis stacked before the samples (collapsed for
+a single name). Unlike the reference, whose Jacobian is k separate
+``torch.func.jvp`` calls each paying a forward and a tangent pass
+(``model/_signal.py:233-268``), every column here comes out of ONE fused
+kernel pass together with the signal.
+
+``mrf_sim`` / ``fse_sim`` are the functional wrappers
+(``_functional/_mrf.py:12-85``, ``_functional/_fse.py:12-96``).
+"""
+
+from __future__ import annotations
+
+from collections.abc import Sequence
+from typing import Any
+
+import numpy as np
+import torch
+
+from . import engine
+from .sequence import PackedEvents, fse_events, mrf_events, program_for
+
+
+def _tensorish(value: Any) -> bool:
+    return isinstance(value, (torch.Tensor, np.ndarray, list, tuple))
+
+
+def _as_tensor(value: Any) -> torch.Tensor:
+    if isinstance(value, torch.Tensor):
+        return value
+    return torch.as_tensor(np.asarray(value, dtype=np.float32))
+
+
+def _batch(held: dict[str, Any]) -> tuple[int, ...]:
+    shapes = [tuple(_as_tensor(v).shape) for v in held.values() if v is not None]
+    return tuple(torch.broadcast_shapes(*shapes)) if shapes else ()
+
+
+def _numel(shape: tuple[int, ...]) -> int:
+    n = 1
+    for s in shape:
+        n *= s
+    return n
+
+
+def _home(values: dict[str, Any]) -> torch.device:
+    """Where results go back to: the first tensor argument's device."""
+    for v in values.values():
+        if isinstance(v, torch.Tensor):
+            return v.device
+    return torch.device("cpu")
+
+
+class _EpgSimulator:
+    """Shared mechanics: split properties from protocol, run, reshape."""
+
+    properties: dict[str, str] = {}
+    states = 10
+
+    def __init__(self, **protocol: Any) -> None:
+        self.protocol = dict(protocol)
+
+    # -- to be provided by a sequence ------------------------------------
+    def events(self, **protocol: Any) -> PackedEvents:  # pragma: no cover - abstract
+        raise NotImplementedError
+
+    def _kernel_maps(self, held: dict[str, Any]) -> dict[str, Any]:
+        return {
+            "T1": held.get("T1"),
+            "T2": held.get("T2"),
+            "M0": held.get("M0"),
+            "B1": held.get("B1"),
+            "inv": held.get("inv_efficiency"),
+        }
+
+    def _post(self, signal, jacobian, names, held, protocol, device):
+        return signal, jacobian
+
+    # -- machinery ---------------------------------------------------------
+    def _split(self, values: dict[str, Any]):
+        merged = {**self.protocol, **values}
+        held = {k: merged.pop(k) for k in list(merged) if k in self.properties}
+        states = int(merged.pop("states", self.states))
+        device = merged.pop("device", None)
+        repetitions = int(merged.pop("repetitions", merged.pop("nreps", 1)))
+        return held, merged, states, device, repetitions
+
+    def _run(self, values: dict[str, Any], names: Sequence[str] | None):
+        held, protocol, states, device, repetitions = self._split(values)
+        for required in ("T1", "T2"):
+            if required not in held:
+                raise ValueError(f"{required} is required")
+        home = _home(values)
+        dev = engine.require_cuda(torch.device(device) if device is not None else
+                                  (home if home.type == "cuda" else None))
+        events = self.events(repetitions=repetitions, **protocol)
+        if events.real_axis() != 1:
+            raise NotImplementedError(
+                "only the real-subspace path is built on this accelerator: every RF pulse and "
+                "recorded sample must share one phase")
+        batch = _batch(held)
+        voxels = _numel(batch)
+        maps = self._kernel_maps(held)
+        if names:
+            for name in names:
+                if name not in held:
+                    raise ValueError(
+                        f"{name!r} is not among the properties this call gave "
+                        f"{type(self).__name__}: {sorted(held)}")
+        # Identity-valued scalars are left out of the kernel, as the
+        # reference's feature mask does.
+        def declared(key, value):
+            if value is None:
+                return None
+            if key in {"M0", "B1", "inv"} and not _tensorish(value) and float(value) == 1.0:
+                return None
+            return value
+
+        with torch.cuda.device(dev):
+            tissue = engine.tissue_maps(dev, voxels, maps["T1"], maps["T2"],
+                                        declared("M0", maps["M0"]), declared("B1", maps["B1"]),
+                                        declared("inv", maps["inv"]))
+            program = program_for(events, dev)
+            kernel_names = self._kernel_names(names) if names else None
+            if kernel_names:
+                signal, jac = engine.forward_tangents(program, tissue, states, kernel_names)
+            else:
+                signal, jac = engine.forward(program, tissue, states), None
+            signal, jac = self._post(signal, jac, names, held, protocol, dev)
+        signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
+        if jac is not None:
+            jac = jac.reshape(*batch, *jac.shape[-2:]) if batch else jac.reshape(jac.shape[-2:])
+        if home.type != "cuda":
+            signal = signal.to(home)
+            jac = None if jac is None else jac.to(home)
+        return signal, jac
+
+    def _kernel_names(self, names: Sequence[str]) -> list[str]:
+        return list(names)
+
+    def simulate(self, **values: Any) -> torch.Tensor:
+        """Return the recorded signal, ``(*voxels, samples)`` complex64."""
+        signal, _ = self._run(values, None)
+        return signal
+
+    def jacobian(self, diff: str | Sequence[str], **values: Any):
+        """Return ``(signal, jacobian)``; the Jacobian is ``(*voxels, k, samples)``
+        (``(*voxels, samples)`` for a single name given as a string)."""
+        names = (diff,) if isinstance(diff, str) else tuple(diff)
+        signal, jac = self._run(values, names)
+        if isinstance(diff, str):
+            jac = jac[..., 0, :]
+        return signal, jac
+
+
+class MRFSimulator(_EpgSimulator):
+    """Inversion-prepared unbalanced-SSFP MR fingerprinting
+    (``simulators/mrf.py:17-84``): protocol ``flip`` (deg), ``TR`` (ms),
+    ``TI`` (ms), ``phases`` (deg); properties T1, T2, M0, B1,
+    inv_efficiency. The signal is ``1j * i*m0*F+[0]`` at every repetition of
+    the last playing."""
+
+    properties = {"T1": "t1_ms", "T2": "t2_ms", "M0": "m0", "B1": "b1",
+                  "inv_efficiency": "inversion_efficiency"}
+    states = 10
+
+    def events(self, *, flip, TR, TI=0.0, phases=0.0, repetitions=1) -> PackedEvents:
+        return mrf_events(flip, TR, TI_ms=TI, phases_deg=phases, repetitions=repetitions)
+
+
+class FSESimulator(_EpgSimulator):
+    """CPMG fast spin echo (``simulators/fse.py:17-133``): protocol ``flip``
+    (refocusing, deg), ``ESP`` (ms), ``phases`` (deg), ``exc_flip``,
+    ``exc_phase`` (deg), ``TR`` (ms); properties T1, T2, M0, B1. M0 and the
+    recovery over what is left of the TR are applied to the recorded echo
+    train afterwards, as the reference's ``evaluate`` does
+    (``fse.py:110-133``); the Jacobian carries them through by the chain
+    rule."""
+
+    properties = {"T1": "t1_ms", "T2": "t2_ms", "M0": None, "B1": "b1"}
+    states = 10
+
+    def events(self, *, flip, ESP, phases=0.0, exc_flip=90.0, exc_phase=90.0, TR=1e6,
+               repetitions=1) -> PackedEvents:
+        if repetitions != 1:
+            raise ValueError("FSESimulator plays a single train")
+        return fse_events(flip, ESP, phases_deg=phases, exc_flip=exc_flip, exc_phase=exc_phase)
+
+    def _kernel_maps(self, held):
+        maps = super()._kernel_maps(held)
+        maps["M0"] = None  # applied after the kernel
+        return maps
+
+    def _kernel_names(self, names):
+        kernel = [n for n in names if n in ("T1", "T2", "B1")]
+        if "T1" not in kernel:
+            kernel.append("T1")  # the recovery term depends on T1 too
+        return kernel
+
+    def _post(self, signal, jacobian, names, held, protocol, device):
+        # The kernel's value is 1j * s_raw; the reference's FSE returns s_raw.
+        s = signal * -1j
+        echoes = s.shape[-1]
+        esp = float(protocol["ESP"])
+        tr = protocol.get("TR", 1e6)
+        t1 = torch.as_tensor(held["T1"], dtype=torch.float32, device=device).reshape(-1)
+        t1 = t1.expand(s.shape[0]) if t1.numel() == 1 else t1
+        left_ms = torch.as_tensor(tr, dtype=torch.float32, device=device) - esp * echoes
+        rec = torch.exp(-1e3 / t1 * left_ms * 1e-3)[:, None]
+        m0v = held.get("M0", 1.0)
+        m0 = torch.as_tensor(m0v, dtype=torch.float32, device=device).reshape(-1)
+        m0 = (m0.expand(s.shape[0]) if m0.numel() == 1 else m0)[:, None]
+        denom = 1 - rec * s
+        out = m0 * s * (1 - rec) / denom
+        if jacobian is None:
+            return out, None
+        kernel = self._kernel_names(names)
+        dj = jacobian * -1j
+        dfds = m0 * (1 - rec) / denom**2
+        dfdrec = m0 * s * (s - 1) / denom**2
+        drec_dt1 = rec * (left_ms * 1e-3 * 1e3) / (t1[:, None] ** 2)
+        cols = []
+        for name in names:
+            if name == "M0":
+                cols.append(s * (1 - rec) / denom)
+                continue
+            col = dfds * dj[:, kernel.index(name)]
+            if name == "T1":
+                col = col + dfdrec * drec_dt1
+            cols.append(col)
+        return out, torch.stack(cols, dim=-2)
+
+
+def mrf_sim(flip, TR, T1, T2, diff: str | tuple[str, ...] | None = None, B1=1.0,
+            inv_efficiency=1.0, M0=1.0, TI: float = 0.0, states: int = 10, nreps: int = 1,
+            device: str | torch.device | None = None):
+    """SSFP MR fingerprinting (``_functional/_mrf.py:12-85``): the signal
+    ``(..., len(flip))`` or ``(signal, jacobian (..., len(diff), len(flip)))``."""
+    model = MRFSimulator()
+    values = dict(T1=T1, T2=T2, M0=M0, B1=B1, inv_efficiency=inv_efficiency, flip=flip, TR=TR,
+                  TI=TI, states=states, repetitions=nreps)
+    if device is not None:
+        values["device"] = device
+    if diff is None:
+        return model.simulate(**values)
+    return model.jacobian(diff, **values)
+
+
+def fse_sim(flip, ESP: float, T1, T2, phases=0.0, TR=1e6, exc_flip: float = 90.0,
+            exc_phase: float = 90.0, diff: str | tuple[str, ...] | None = None, B1=1.0, M0=1.0,
+            states: int = 10, device: str | torch.device | None = None):
+    """Fast spin echo (``_functional/_fse.py:12-96``). The GB300 path is the
+    real subspace, which CPMG reaches with ``phases`` equal to ``exc_phase``
+    (90 deg by default for the excitation)."""
+    model = FSESimulator()
+    values = dict(T1=T1, T2=T2, M0=M0, B1=B1, flip=flip, ESP=ESP, phases=phases, TR=TR,
+                  exc_flip=exc_flip, exc_phase=exc_phase, states=states)
+    if device is not None:
+        values["device"] = device
+    if diff is None:
+        return model.simulate(**values)
+    return model.jacobian(diff, **values)
+
