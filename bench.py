@@ -50,12 +50,13 @@ def mrf_schedule() -> np.ndarray:
     ).astype(np.float32)
 
 
-def dictionary_grid():
+def dictionary_grid(atoms: int = ATOMS):
+    """The first ``atoms`` entries of the T1 x T2 x B1 grid (all of it by default)."""
     t1 = np.geomspace(100, 4000, GRID[0]).astype(np.float32)
     t2 = np.geomspace(5, 500, GRID[1]).astype(np.float32)
     b1 = np.linspace(0.6, 1.4, GRID[2]).astype(np.float32)
     T1, T2, B1 = np.meshgrid(t1, t2, b1, indexing="ij")
-    return T1.ravel().copy(), T2.ravel().copy(), B1.ravel().copy()
+    return T1.ravel()[:atoms].copy(), T2.ravel()[:atoms].copy(), B1.ravel()[:atoms].copy()
 
 
 def config(extra=None):
@@ -187,12 +188,13 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     flip = mrf_schedule()
     events = mrf_events(flip, 10.0)
     program = program_for(events, device)
-    t1, t2, b1 = dictionary_grid()
-    tissue = engine.tissue_maps(device, ATOMS, torch.from_numpy(t1), torch.from_numpy(t2), None,
+    atoms = args.atoms
+    t1, t2, b1 = dictionary_grid(atoms)
+    tissue = engine.tissue_maps(device, atoms, torch.from_numpy(t1), torch.from_numpy(t2), None,
                                 torch.from_numpy(b1), None)
     names = ("T1", "T2", "B1")
-    sig = torch.empty((ATOMS, PULSES), dtype=torch.complex64, device=device)
-    jac = torch.empty((ATOMS, 3, PULSES), dtype=torch.complex64, device=device)
+    sig = torch.empty((atoms, PULSES), dtype=torch.complex64, device=device)
+    jac = torch.empty((atoms, 3, PULSES), dtype=torch.complex64, device=device)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     launch = tuple(args.launch) if args.launch else None
 
@@ -224,7 +226,7 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         t = torch.tensor([total_s], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
-    updates = float(ATOMS) * PULSES * STATES
+    updates = float(atoms) * PULSES * STATES
     value = updates * args.steps * world / total_s
     kernel_s = total_s / args.steps
 
@@ -233,7 +235,7 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     # property, model/_signal.py:233-268) -- through the same kernels.
     plain = None
     if rank == 0 and not args.skip_plain:
-        one = torch.empty((ATOMS, 1, PULSES), dtype=torch.complex64, device=device)
+        one = torch.empty((atoms, 1, PULSES), dtype=torch.complex64, device=device)
         def plain_step():
             engine.forward(program, tissue, STATES, out=sig)
             for name in names:
@@ -256,10 +258,10 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     # End to end through the public API: pinned host tissue in, pinned host
     # signal and Jacobian out, copies inside the timed region.
     e2e = None
-    if rank == 0:
+    if rank == 0 and not args.skip_e2e:
         host_t = [torch.from_numpy(a).pin_memory() for a in (t1, t2, b1)]
-        host_sig = torch.empty((ATOMS, PULSES), dtype=torch.complex64).pin_memory()
-        host_jac = torch.empty((ATOMS, 3, PULSES), dtype=torch.complex64).pin_memory()
+        host_sig = torch.empty((atoms, PULSES), dtype=torch.complex64).pin_memory()
+        host_jac = torch.empty((atoms, 3, PULSES), dtype=torch.complex64).pin_memory()
 
         def e2e_step():
             dev_t = [h.to(device, non_blocking=True) for h in host_t]
@@ -278,7 +280,7 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / n_e2e
         e2e = {"value": updates / e2e_s, "unit": "updates/s", "ms_per_step": e2e_s * 1e3,
-               "h2d_bytes_per_step": 3 * ATOMS * 4,
+               "h2d_bytes_per_step": 3 * atoms * 4,
                "d2h_bytes_per_step": int(host_sig.numel() * 8 + host_jac.numel() * 8),
                "api": "engine.forward_tangents with pinned host tissue and outputs"}
         del host_sig, host_jac
@@ -286,9 +288,9 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     if rank != 0:
         return None
     peak = fp32_peak(torch, lib, device)
-    flops = float(ATOMS) * PULSES * STATES * FLOPS_PER_UPDATE
+    flops = float(atoms) * PULSES * STATES * FLOPS_PER_UPDATE
     out_bytes = float(sig.numel() * 8 + jac.numel() * 8)
-    in_bytes = 3.0 * ATOMS * 4
+    in_bytes = 3.0 * atoms * 4
     hbm_peak = None
     peaks_path = ROOT / "MEASURED_PEAKS.json"
     if peaks_path.exists():
@@ -310,7 +312,7 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded grid of the named shape)",
-        "config": config(),
+        "config": config({"atoms": atoms} if atoms != ATOMS else None),
         "roofline": {
             "bound": "fp32",
             "achieved": achieved,
@@ -448,12 +450,15 @@ def run_reference(args, rank: int) -> dict | None:
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--atoms", type=int, default=ATOMS,
+                    help="first N grid atoms (a smaller case for profiling; default all)")
     ap.add_argument("--launch", type=int, nargs=3, metavar=("LANES", "ORDERS", "WARPS"))
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

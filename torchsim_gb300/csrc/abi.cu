@@ -222,6 +222,7 @@ extern "C" int tsg_epg_forward(const tsg_program* program, const tsg_tissue* tis
                                void* stream) {
     int rc = check_common(program, tissue, atom_count, state_count);
     if (rc) return rc;
+    if (atom_count == 0) return TSG_OK;
     if (layout == TSG_LAYOUT_PLANES ? !out_b : !out_a)
         return fail(TSG_ERR_ARGUMENT, "null output buffer");
     SweepArgs a = base_args(program, tissue, atom_count, state_count);
@@ -241,6 +242,7 @@ extern "C" int tsg_epg_forward_tangents(const tsg_program* program, const tsg_ti
     int rc = check_common(program, tissue, atom_count, state_count);
     if (rc) return rc;
     if (!columns || column_count < 0) return fail(TSG_ERR_ARGUMENT, "null column map");
+    if (atom_count == 0) return TSG_OK;
     const int mode = mode_for_mask(tangent_mask);
     if (mode < 0) return fail(TSG_ERR_UNSUPPORTED, "unknown tangent bits");
     for (int i = 0; i < 5; ++i)
@@ -296,7 +298,9 @@ extern "C" int tsg_epg_tangent(const tsg_program* program, const tsg_tissue* tis
                                const tsg_launch* launch_shape, void* stream) {
     int rc = check_common(program, tissue, atom_count, state_count);
     if (rc) return rc;
-    if (!direction || !out_imag) return fail(TSG_ERR_ARGUMENT, "null direction or output");
+    if (!direction) return fail(TSG_ERR_ARGUMENT, "null direction");
+    if (atom_count == 0) return TSG_OK;
+    if (!out_imag) return fail(TSG_ERR_ARGUMENT, "null output");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int64_t n = program->host.ops * program->host.trains;
     float2* dirs = nullptr;
