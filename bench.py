@@ -334,9 +334,73 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         "clocks": clk,
         "wall_s_timed_region": wall,
     }
+    if not args.skip_adjoint:
+        line["adjoint"] = adjoint_section(torch, device)
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     return line
+
+
+# ---- adjoint sequence-optimisation workload ---------------------------------
+
+
+def adjoint_section(torch, device, repeats: int = 5) -> dict:
+    """Gradient of sum |s - target|^2 over 16,384 voxels w.r.t. 600 flips and
+    600 TRs (and the tissue), nstates 20: the checkpointed adjoint against one
+    plain forward of the same sequence."""
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    rng = np.random.default_rng(0)
+    V, n, S = 16384, 600, 20
+    t1 = np.exp(rng.uniform(np.log(100), np.log(3000), V)).astype(np.float32)
+    t2 = np.minimum(np.exp(rng.uniform(np.log(10), np.log(300), V)), 0.999 * t1).astype(np.float32)
+    b1 = rng.uniform(0.8, 1.2, V).astype(np.float32)
+    flips = rng.uniform(5, 70, n).astype(np.float32)
+    trs = rng.uniform(8, 15, n).astype(np.float32)
+    ev = mrf_events(flips, trs)
+    prog = program_for(ev, device)
+    tissue = engine.tissue_maps(device, V, torch.from_numpy(t1), torch.from_numpy(t2), None,
+                                torch.from_numpy(b1), None)
+    sig = torch.empty((V, n), dtype=torch.complex64, device=device)
+    c, ck, ws = engine.adjoint_plan(prog, V, S)
+    ckpt = torch.empty(ck // 4, dtype=torch.float32, device=device)
+    work = torch.empty(ws, dtype=torch.uint8, device=device)
+    seed = torch.randn((V, n), dtype=torch.complex64, device=device)
+    grads = {k: torch.zeros(V, device=device) for k in ("t1_ms", "t2_ms", "b1")}
+    grads["flip_rad"] = torch.zeros((1, ev.events), device=device)
+    grads["duration_s"] = torch.zeros((1, ev.events), device=device)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(repeats):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e))
+        return best
+
+    fwd = timed(lambda: engine.forward(prog, tissue, S, out=sig))
+    fwd_ck = timed(lambda: engine.forward_checkpointed(prog, tissue, S, c, ckpt, out=sig))
+    bwd = timed(lambda: engine.adjoint(prog, tissue, S, seed, ckpt, c, grads, workspace=work))
+    return {
+        "workload": "MRF adjoint: 16384 voxels, 600 pulses (flip U(5,70) deg, TR U(8,15) ms), "
+                    "nstates 20, loss sum |s - target|^2",
+        "ops_per_checkpoint": c,
+        "checkpoint_bytes": ck,
+        "forward_ms": fwd,
+        "forward_with_checkpoints_ms": fwd_ck,
+        "backward_ms": bwd,
+        "gradient_cost_over_forward": bwd / fwd,
+        "forward_and_backward_over_forward": (fwd_ck + bwd) / fwd,
+        "forward_updates_per_s": V * n * S / (fwd * 1e-3),
+        "timing": "best of 5 after 3 warm-up runs, CUDA events",
+    }
 
 
 # ---- CPU baselines ----------------------------------------------------------
@@ -457,6 +521,7 @@ def main() -> None:
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--atoms", type=int, default=ATOMS,
                     help="first N grid atoms (a smaller case for profiling; default all)")
     ap.add_argument("--launch", type=int, nargs=3, metavar=("LANES", "ORDERS", "WARPS"))

@@ -178,6 +178,37 @@ int tsg_epg_tangent(const tsg_program* program, const tsg_tissue* tissue, int64_
                     int64_t state_count, const tsg_direction* direction, float* out_real,
                     float* out_imag, const tsg_launch* launch, void* stream);
 
+/* Forward (as tsg_epg_forward; outputs nullable) that also stores the state
+ * entering every ops_per_checkpoint-th op into `checkpoints` (DEVICE,
+ * train x atom x ceil(ops/ops_per_checkpoint) x 3 x state_count floats), the
+ * input of tsg_epg_adjoint. */
+int tsg_epg_forward_checkpointed(const tsg_program* program, const tsg_tissue* tissue,
+                                 int64_t atom_count, int64_t state_count, int layout, float* out_a,
+                                 float* out_b, float* checkpoints, int ops_per_checkpoint,
+                                 const tsg_launch* launch, void* stream);
+
+/* Sizes for tsg_epg_adjoint: the segment length it will use (ops between
+ * checkpoints; 0 = as long as the per-block shared-memory budget allows),
+ * and the checkpoint and workspace bytes the caller allocates. */
+int tsg_epg_adjoint_plan(const tsg_program* program, int64_t atom_count, int64_t state_count,
+                         const tsg_launch* launch, int ops_per_checkpoint,
+                         int* resolved_ops_per_checkpoint, int64_t* checkpoint_bytes,
+                         int64_t* workspace_bytes);
+
+/* Checkpointed first-order adjoint (the reference's simulate_real_vjp_range,
+ * _epg_cpu.cpp:5985-6232): reverse sweep over segments of
+ * ops_per_checkpoint ops re-run from the checkpoints of
+ * tsg_epg_forward_checkpointed. `seed` is the cotangent of the recorded
+ * samples: the imaginary plane (TSG_LAYOUT_PLANES) or the complex64 gradient
+ * of 1j*signal (TSG_LAYOUT_COMPLEX_IJ). Gradients ADD into `gradients`
+ * (nullable slots). `workspace` holds per-warp event partials and per-train
+ * tissue partials, summed in a fixed order afterwards (deterministic). */
+int tsg_epg_adjoint(const tsg_program* program, const tsg_tissue* tissue, int64_t atom_count,
+                    int64_t state_count, const float* seed, int seed_layout,
+                    const float* checkpoints, int ops_per_checkpoint,
+                    const tsg_gradients* gradients, void* workspace, int64_t workspace_bytes,
+                    const tsg_launch* launch, void* stream);
+
 /* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */
 
 /* _epg_cpu.simulate (src/torchsim/_epg_cpu.cpp:10740-10926): pointers holds
@@ -191,6 +222,16 @@ int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, int64_t atom_
  * buffers, 20 tangents (the differentiable inputs, FLOAT_INPUTS order of
  * sequence/_parameters.py:206), two output planes, 13 tail slots (61). */
 int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
+                         int64_t train_count, int64_t event_count, int64_t state_count,
+                         int64_t output_count, int real_axis, int features);
+
+/* _epg_cpu.simulate_vjp (src/torchsim/_epg_cpu.cpp:11150-11400): 26 packed
+ * buffers, two seed planes, 20 gradient slots (17 tissue, then flip, phase,
+ * duration, the order of :11243-11253), 13 tail slots (61). The program is
+ * compiled unmerged so that every event's duration gradient is formed.
+ * Gradients are written (not accumulated); phase and the tissue directions
+ * the real subspace divides out are written as zero. Synchronous. */
+int tsg_epg_simulate_vjp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
                          int64_t train_count, int64_t event_count, int64_t state_count,
                          int64_t output_count, int real_axis, int features);
 

@@ -1,0 +1,189 @@
+"""GPU parity of the checkpointed adjoint kernel.
+
+Against the reference's own gradients (the committed fixture of a loss
+backpropagated through its MRF simulator), against the FP64 oracle's adjoint
+(including every event's duration gradient through the host-buffer drop-in),
+and against central finite differences of the FP64 oracle's loss.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.helpers import draw_tissue, max_rel, packed_from_events, packed_from_golden
+
+pytestmark = pytest.mark.gpu
+
+GRAD_TOL = 1e-4
+
+
+def _loss_grads(flip, tr, t1, t2, b1, target, states, device, ops_per_checkpoint=None):
+    from torchsim_gb300 import MRFSimulator
+
+    theta = torch.tensor(flip, device=device, requires_grad=True)
+    tau = torch.tensor(tr, device=device, requires_grad=True)
+    t1t = torch.tensor(t1, device=device, requires_grad=True)
+    t2t = torch.tensor(t2, device=device, requires_grad=True)
+    b1t = torch.tensor(b1, device=device, requires_grad=True)
+    sig = MRFSimulator(flip=theta, TR=tau, states=states).simulate(T1=t1t, T2=t2t, B1=b1t)
+    loss = (sig - torch.as_tensor(target, device=device)).abs().square().sum()
+    loss.backward()
+    return {"loss": loss.item(), "flip": theta.grad.cpu().numpy(), "tr": tau.grad.cpu().numpy(),
+            "t1": t1t.grad.cpu().numpy(), "t2": t2t.grad.cpu().numpy(),
+            "b1": b1t.grad.cpu().numpy(), "signal": sig.detach().cpu().numpy()}
+
+
+def test_adjoint_matches_reference_gradients(cuda, golden):
+    d = golden("mrf_adjoint")
+    g = _loss_grads(d["flip_deg"], d["tr_ms"], d["t1"], d["t2"], d["b1"], d["target"],
+                    int(d["states"]), cuda)
+    assert max_rel(g["signal"], d["signal"]) <= 1e-5
+    assert abs(g["loss"] - float(d["loss"])) <= 1e-4 * abs(float(d["loss"]))
+    for mine, ref in (("flip", "grad_flip_deg"), ("tr", "grad_tr_ms"), ("t1", "grad_t1"),
+                      ("t2", "grad_t2"), ("b1", "grad_b1")):
+        assert max_rel(g[mine], d[ref]) <= GRAD_TOL, mine
+
+
+def test_dropin_vjp_every_event(built_library, cuda, golden):
+    """The host-buffer drop-in of _epg_cpu.simulate_vjp: all 20 gradient slots."""
+    from tests.test_gpu_parity import EVENT_ORDER, FEATURES, TISSUE_ORDER, _pointer_array
+    from torchsim_gb300 import _native
+
+    d = golden("mrf_adjoint")
+    V, P = d["vjp_seed"].shape
+    E = d["vjp_event_kind"].size
+    tissue = [np.ascontiguousarray(d["vjp_tissue_" + n]) for n in TISSUE_ORDER]
+    events = [np.ascontiguousarray(d["vjp_event_" + n]) for n in EVENT_ORDER]
+    seeds = [np.ascontiguousarray(d["vjp_seed"].real), np.ascontiguousarray(d["vjp_seed"].imag)]
+    grads = [np.full(V, 9.0, np.float32) for _ in range(17)] + [np.full(E, 9.0, np.float32)
+                                                                  for _ in range(3)]
+    arrays = [*tissue, *events, *seeds, *grads, *([None] * 13)]
+    _native.check(built_library.tsg_epg_simulate_vjp(_pointer_array(arrays), len(arrays), V, 1, E,
+                                                     int(d["states"]), P, 1, FEATURES))
+    names = [*TISSUE_ORDER, "flip", "phase", "duration"]
+    for name, got in zip(names, grads, strict=True):
+        key = "vjp_grad_" + name
+        if key in d.files and name not in ("b1_phase_rad", "b0_hz", "phase",
+                                           "diffusion_um2_per_ms"):
+            assert max_rel(got, d[key]) <= GRAD_TOL, name
+    # Oracle (FP64): every event's duration gradient, zero-duration events too.
+    ref = O.adjoint(packed_from_golden(d, "vjp_"), d["vjp_seed"].imag, "f64")
+    assert max_rel(grads[19], ref["duration_s"]) <= GRAD_TOL
+    assert max_rel(grads[17], ref["flip_rad"]) <= GRAD_TOL
+    assert not grads[18].any()
+
+
+@pytest.mark.parametrize("ops_per_checkpoint", [1, 3, 7, 64])
+def test_segment_length_does_not_change_gradients(cuda, ops_per_checkpoint):
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    rng = np.random.default_rng(31)
+    flips = rng.uniform(5, 70, 90).astype(np.float32)
+    trs = rng.uniform(8, 15, 90).astype(np.float32)
+    ev = mrf_events(flips, trs, TI_ms=12.0)
+    V, S = 45, 12
+    t1, t2, b1 = draw_tissue(7, V)
+    prog = program_for(ev, cuda)
+    tissue = engine.tissue_maps(cuda, V, t1, t2, None, b1, None)
+    seed = torch.from_numpy(rng.standard_normal((V, ev.outputs)).astype(np.complex64)).to(cuda)
+    c, ck, _ = engine.adjoint_plan(prog, V, S, None, ops_per_checkpoint)
+    assert c == ops_per_checkpoint
+    ckpt = torch.empty(ck // 4, dtype=torch.float32, device=cuda)
+    engine.forward_checkpointed(prog, tissue, S, c, ckpt)
+    grads = {n: torch.zeros(V, device=cuda) for n in ("t1_ms", "t2_ms", "m0", "b1", "inversion")}
+    grads["flip_rad"] = torch.zeros((1, ev.events), device=cuda)
+    grads["duration_s"] = torch.zeros((1, ev.events), device=cuda)
+    engine.adjoint(prog, tissue, S, seed, ckpt, c, grads)
+    p = packed_from_events(ev, t1, t2, S, b1=b1)
+    ref = O.adjoint(p, -seed.real.cpu().numpy(), "f64")
+    for name in ("t1_ms", "t2_ms", "m0", "b1", "flip_rad"):
+        got = grads[name].cpu().numpy().reshape(ref[name].shape)
+        assert max_rel(got, ref[name]) <= GRAD_TOL, name
+    # Zero-duration events fold into the op before them: their duration
+    # gradient is not formed on the merged program; the others agree.
+    dur = grads["duration_s"].cpu().numpy()[0]
+    nz = ev.duration[0] != 0
+    assert max_rel(dur[nz], ref["duration_s"][nz]) <= GRAD_TOL
+
+
+@pytest.mark.parametrize("shape", [(1, 20, 4), (2, 10, 4), (4, 5, 2), (4, 8, 4), (8, 4, 8),
+                                   (16, 4, 4), (32, 4, 4)])
+def test_adjoint_launch_shapes(cuda, shape):
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    lanes, orders, warps = shape
+    rng = np.random.default_rng(lanes * 7 + orders)
+    flips = rng.uniform(5, 70, 60).astype(np.float32)
+    ev = mrf_events(flips, 9.0)
+    V = 50
+    S = max(2, lanes * orders - 2)
+    t1, t2, b1 = draw_tissue(lanes, V)
+    inv = rng.uniform(0.8, 1.0, V).astype(np.float32)
+    prog = program_for(ev, cuda)
+    tissue = engine.tissue_maps(cuda, V, t1, t2, None, b1, inv)
+    seed = torch.from_numpy(rng.standard_normal((V, ev.outputs)).astype(np.complex64)).to(cuda)
+    c, ck, _ = engine.adjoint_plan(prog, V, S, shape, 0)
+    ckpt = torch.empty(ck // 4, dtype=torch.float32, device=cuda)
+    engine.forward_checkpointed(prog, tissue, S, c, ckpt, launch=shape)
+    grads = {n: torch.zeros(V, device=cuda) for n in ("t1_ms", "t2_ms", "b1", "inversion")}
+    grads["flip_rad"] = torch.zeros((1, ev.events), device=cuda)
+    engine.adjoint(prog, tissue, S, seed, ckpt, c, grads, launch=shape)
+    ref = O.adjoint(packed_from_events(ev, t1, t2, S, b1=b1, inv=inv), -seed.real.cpu().numpy(),
+                    "f64")
+    for name in ("t1_ms", "t2_ms", "b1", "inversion", "flip_rad"):
+        got = grads[name].cpu().numpy().reshape(ref[name].shape)
+        assert max_rel(got, ref[name]) <= GRAD_TOL, (shape, name)
+
+
+def test_adjoint_against_central_differences(cuda):
+    """Config-3 shapes in small: 600 pulses, nstates 20; central differences
+    (h = 1e-3 deg / ms) of the FP64 oracle's loss on sampled coordinates."""
+    from torchsim_gb300.sequence import mrf_events
+
+    rng = np.random.default_rng(3)
+    n, V, S = 600, 24, 20
+    t1, t2, b1 = draw_tissue(0, V)
+    flips = rng.uniform(5, 70, n).astype(np.float32)
+    trs = rng.uniform(8, 15, n).astype(np.float32)
+    tgt_flip = rng.uniform(5, 70, n).astype(np.float32)
+    tgt_tr = rng.uniform(8, 15, n).astype(np.float32)
+    ev_t = mrf_events(tgt_flip, tgt_tr)
+    target = -O.forward(packed_from_events(ev_t, t1, t2, S, b1=b1), "f64")
+    g = _loss_grads(flips, trs, t1, t2, b1, target.astype(np.complex64), S, cuda)
+
+    def loss(fl, tr):
+        ev = mrf_events(fl.astype(np.float32), tr.astype(np.float32))
+        s = -O.forward(packed_from_events(ev, t1, t2, S, b1=b1), "f64")
+        return float(((s - target) ** 2).sum())
+
+    picks = [0, 7, 150, 301, 598]
+    for k in picks:
+        h = 1e-3
+        up, dn = flips.astype(np.float64).copy(), flips.astype(np.float64).copy()
+        up[k] += h
+        dn[k] -= h
+        fd = (loss(up, trs) - loss(dn, trs)) / (2 * h)
+        assert abs(g["flip"][k] - fd) <= 1e-3 * max(abs(fd), np.abs(g["flip"]).max() * 1e-2), k
+    for k in [0, 10, 299, 597]:
+        h = 1e-3
+        up, dn = trs.astype(np.float64).copy(), trs.astype(np.float64).copy()
+        up[k] += h
+        dn[k] -= h
+        fd = (loss(flips, up) - loss(flips, dn)) / (2 * h)
+        assert abs(g["tr"][k] - fd) <= 1e-3 * max(abs(fd), np.abs(g["tr"]).max() * 1e-2), k
+    assert g["tr"][-1] == 0.0  # the last TR moves nothing recorded
+
+
+def test_adjoint_deterministic(cuda, golden):
+    d = golden("mrf_adjoint")
+    a = _loss_grads(d["flip_deg"], d["tr_ms"], d["t1"], d["t2"], d["b1"], d["target"], 8, cuda)
+    b = _loss_grads(d["flip_deg"], d["tr_ms"], d["t1"], d["t2"], d["b1"], d["target"], 8, cuda)
+    for k in ("flip", "tr", "t1", "t2", "b1"):
+        assert np.array_equal(a[k], b[k]), k

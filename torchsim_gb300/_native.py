@@ -78,6 +78,16 @@ SIGNATURES: dict[str, tuple] = {
                                         _vp, _vp, _vp, _vp, ctypes.POINTER(Launch), _vp]),
     "tsg_epg_tangent": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.POINTER(Direction),
                                _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_forward_checkpointed": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _int, _vp,
+                                            _vp, _vp, _int, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_adjoint_plan": (_int, [_vp, _i64, _i64, ctypes.POINTER(Launch), _int,
+                                    ctypes.POINTER(_int), ctypes.POINTER(_i64),
+                                    ctypes.POINTER(_i64)]),
+    "tsg_epg_adjoint": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _vp, _int, _vp, _int,
+                               ctypes.POINTER(Gradients), _vp, _i64, ctypes.POINTER(Launch),
+                               _vp]),
+    "tsg_epg_simulate_vjp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
+                                    _int, _int]),
     "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,
                                 _int]),
     "tsg_epg_simulate_jvp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,

@@ -233,6 +233,28 @@ extern "C" int tsg_epg_forward(const tsg_program* program, const tsg_tissue* tis
                   static_cast<cudaStream_t>(stream));
 }
 
+extern "C" int tsg_epg_forward_checkpointed(const tsg_program* program, const tsg_tissue* tissue,
+                                            int64_t atom_count, int64_t state_count, int layout,
+                                            float* out_a, float* out_b, float* checkpoints,
+                                            int ops_per_checkpoint, const tsg_launch* launch_shape,
+                                            void* stream) {
+    int rc = check_common(program, tissue, atom_count, state_count);
+    if (rc) return rc;
+    if (ops_per_checkpoint < 1) return fail(TSG_ERR_ARGUMENT, "ops_per_checkpoint must be >= 1");
+    if (atom_count == 0) return TSG_OK;
+    if (!checkpoints) return fail(TSG_ERR_ARGUMENT, "null checkpoint buffer");
+    SweepArgs a = base_args(program, tissue, atom_count, state_count);
+    a.layout = layout;
+    a.sig_a = out_a;
+    a.sig_b = out_b;
+    if (layout == TSG_LAYOUT_PLANES ? !out_b : !out_a) a.sig_a = a.sig_b = nullptr;
+    a.ckpt = checkpoints;
+    a.ckpt_every = ops_per_checkpoint;
+    a.ckpt_count = int((program->host.ops + ops_per_checkpoint - 1) / ops_per_checkpoint);
+    return launch(MODE_FORWARD, program, a, atom_count, int(state_count), launch_shape,
+                  static_cast<cudaStream_t>(stream));
+}
+
 extern "C" int tsg_epg_forward_tangents(const tsg_program* program, const tsg_tissue* tissue,
                                         int64_t atom_count, int64_t state_count,
                                         unsigned tangent_mask, const int32_t* columns,

@@ -142,13 +142,16 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
             if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
                 // State entering this op, for the adjoint's segments.
                 const int k = (base + i) / a.ckpt_every;
-                const int SL = L * R;
-                float* dst = a.ckpt + (row * a.ckpt_count + k) * (3 * SL) + q * R;
+                const int S = a.states;
+                float* dst = a.ckpt + (row * a.ckpt_count + k) * (3 * int64_t(S));
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    dst[r] = P[r];
-                    dst[SL + r] = M[r];
-                    dst[2 * SL + r] = Z[r];
+                    const int o = q * R + r;
+                    if (o < S) {
+                        dst[o] = P[r];
+                        dst[S + o] = M[r];
+                        dst[2 * S + o] = Z[r];
+                    }
                 }
             }
             float ddt = 0.f, dfl = 0.f;

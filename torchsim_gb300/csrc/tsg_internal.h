@@ -115,7 +115,8 @@ struct SweepArgs {
     int jac_cols;
     int col_t1, col_t2, col_b1, col_inv, col_m0, col_gen;
     // Optional state checkpoints for the adjoint: every ckpt_every ops the
-    // state entering that op is stored, [train][atom][k][3*states].
+    // state entering that op is stored, [train][atom][k][plane][order] with
+    // plane F+, F-, Z and `states` orders.
     float* ckpt;
     int ckpt_every;
     int ckpt_count;
@@ -153,5 +154,42 @@ extern const SweepEntry kSweepGeneral[];
 extern const int kSweepGeneralCount;
 
 constexpr int kOpChunk = 1024;  // ops staged in shared memory at a time
+
+// Arguments of the checkpointed reverse sweep.
+struct AdjointArgs {
+    const Op* ops;
+    int n_ops;
+    int64_t atoms;
+    int states;
+    int outputs;
+    const float* t1;
+    const float* t2;
+    const float* m0;
+    const float* b1;
+    const float* inv;
+    // Cotangent of the recorded samples: the imaginary plane (layout PLANES)
+    // or the complex64 gradient of 1j*signal (layout COMPLEX_IJ).
+    const float* seed;
+    int seed_layout;
+    const float* ckpt;   // [train][atom][k][3][states], written by a forward sweep
+    int ckpt_every;      // ops per segment (C)
+    int ckpt_count;      // segments per row
+    float2* event_partial;   // [train][warp][op]: (flip, duration) gradient partials
+    int64_t warps_per_train;
+    float* tissue_partial;   // [train][atom][5]: t1, t2, m0, b1, inversion
+};
+
+using AdjointLaunch = void (*)(const AdjointArgs&, dim3 grid, dim3 block, size_t smem,
+                               cudaStream_t stream);
+
+struct AdjointEntry {
+    int orders_per_lane;
+    int lanes_per_voxel;
+    AdjointLaunch launch;
+    const void* kernel;  // for the shared-memory attribute
+};
+
+extern const AdjointEntry kAdjoint[];
+extern const int kAdjointCount;
 
 }  // namespace tsg

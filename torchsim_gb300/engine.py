@@ -196,3 +196,106 @@ def tangent(program: Program, tissue: TissueMaps, states: int, *, t1=None, t2=No
         program.handle, ctypes.byref(ts), tissue.voxels, states, ctypes.byref(d),
         res[0].data_ptr(), res[1].data_ptr(), _native.launch_shape(launch), _stream()))
     return res[1]
+
+
+# ---- the checkpointed adjoint ---------------------------------------------
+
+
+def adjoint_plan(program: Program, voxels: int, states: int, launch=None,
+                 ops_per_checkpoint: int = 0) -> tuple[int, int, int]:
+    """(ops per checkpoint, checkpoint bytes, workspace bytes) for the adjoint."""
+    c = ctypes.c_int()
+    ck = ctypes.c_int64()
+    ws = ctypes.c_int64()
+    _native.check(_native.library().tsg_epg_adjoint_plan(
+        program.handle, voxels, states, _native.launch_shape(launch), int(ops_per_checkpoint),
+        ctypes.byref(c), ctypes.byref(ck), ctypes.byref(ws)))
+    return c.value, ck.value, ws.value
+
+
+def forward_checkpointed(program: Program, tissue: TissueMaps, states: int, ops_per_checkpoint: int,
+                         checkpoints: torch.Tensor, out: torch.Tensor | None = None,
+                         launch=None) -> torch.Tensor | None:
+    """Forward (complex64 ``1j * i*m0*F+[0]``) that also writes checkpoints."""
+    t = tissue.struct()
+    _native.check(_native.library().tsg_epg_forward_checkpointed(
+        program.handle, ctypes.byref(t), tissue.voxels, states, _native.LAYOUT_COMPLEX_IJ,
+        None if out is None else out.data_ptr(), None, checkpoints.data_ptr(),
+        int(ops_per_checkpoint), _native.launch_shape(launch), _stream()))
+    return out
+
+
+GRAD_NAMES = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")
+
+
+def adjoint(program: Program, tissue: TissueMaps, states: int, seed: torch.Tensor,
+            checkpoints: torch.Tensor, ops_per_checkpoint: int, grads: dict[str, torch.Tensor],
+            workspace: torch.Tensor | None = None, launch=None) -> dict[str, torch.Tensor]:
+    """Reverse sweep: adds dL/d(tissue) and dL/d(event flip, duration) into ``grads``.
+
+    ``seed`` is the complex64 gradient of the ``(rows, outputs)`` signal.
+    """
+    seed = seed.contiguous()
+    if seed.dtype != torch.complex64:
+        seed = seed.to(torch.complex64)
+    _, _, ws_bytes = adjoint_plan(program, tissue.voxels, states, launch, ops_per_checkpoint)
+    if workspace is None or workspace.numel() < ws_bytes:
+        workspace = torch.empty(max(ws_bytes, 4), dtype=torch.uint8, device=seed.device)
+    g = _native.Gradients(*[grads[n].data_ptr() if grads.get(n) is not None else None
+                            for n in GRAD_NAMES])
+    t = tissue.struct()
+    _native.check(_native.library().tsg_epg_adjoint(
+        program.handle, ctypes.byref(t), tissue.voxels, states, seed.data_ptr(),
+        _native.LAYOUT_COMPLEX_IJ, checkpoints.data_ptr(), int(ops_per_checkpoint), ctypes.byref(g),
+        workspace.data_ptr(), workspace.numel(), _native.launch_shape(launch), _stream()))
+    return grads
+
+
+class EpgFunction(torch.autograd.Function):
+    """Forward sweep whose backward is the checkpointed adjoint kernel.
+
+    The role of the reference's ``_NativeEpg`` (sequence/_accelerators.py:
+    1402-1594): inputs are the flat tissue maps and the event-level flip and
+    duration buffers of the program (for gradient routing only: their values
+    are baked into ``program``); the output is the complex64 signal
+    ``(trains*voxels, outputs)``.
+    """
+
+    @staticmethod
+    def forward(ctx, program, states, launch, t1, t2, m0, b1, inv, flip_events, duration_events):
+        tissue = TissueMaps(t1.detach(), t2.detach(), None if m0 is None else m0.detach(),
+                            None if b1 is None else b1.detach(),
+                            None if inv is None else inv.detach())
+        c, ck_bytes, _ = adjoint_plan(program, tissue.voxels, states, launch)
+        ckpt = torch.empty(max(ck_bytes // 4, 1), dtype=torch.float32, device=t1.device)
+        out = torch.empty((program.trains * tissue.voxels, program.outputs), dtype=torch.complex64,
+                          device=t1.device)
+        forward_checkpointed(program, tissue, states, c, ckpt, out=out, launch=launch)
+        ctx.program, ctx.states, ctx.launch, ctx.c = program, states, launch, c
+        ctx.tissue = tissue
+        ctx.save_for_backward(ckpt)
+        ctx.present = (m0 is not None, b1 is not None, inv is not None)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (ckpt,) = ctx.saved_tensors
+        tissue, program = ctx.tissue, ctx.program
+        need = ctx.needs_input_grad
+        dev = grad_out.device
+        V = tissue.voxels
+        grads: dict[str, torch.Tensor] = {}
+        names = ("t1_ms", "t2_ms", "m0", "b1", "inversion")
+        for k, name in enumerate(names):
+            if need[3 + k]:
+                grads[name] = torch.zeros(V, dtype=torch.float32, device=dev)
+        ev_shape = (program.trains, program.events.events)
+        if need[8]:
+            grads["flip_rad"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
+        if need[9]:
+            grads["duration_s"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
+        adjoint(program, tissue, ctx.states, grad_out, ckpt, ctx.c, grads, launch=ctx.launch)
+        out = [None, None, None]
+        out += [grads.get(n) for n in names]
+        out += [grads.get("flip_rad"), grads.get("duration_s")]
+        return tuple(out)

@@ -204,6 +204,30 @@ def mrf_events(flip_deg: Any, TR_ms: Any, TI_ms: Any = 0.0, phases_deg: Any = 0.
     )
 
 
+def mrf_gradient_map(pulses: int, repetitions: int = 1) -> dict[str, np.ndarray]:
+    """Where the MRF protocol's values land in the packed stream.
+
+    ``flip``: (repetitions, pulses) event indices whose flip is pulse k's;
+    ``tr``: (m, 2) pairs (event, k) whose duration is TR_k; ``ti``: events whose
+    duration is TI. Read off the layout of :func:`mrf_events`: repetition
+    ``r`` starts at ``r*(1+4n)`` with the inversion, pulse k's excitation is
+    at ``1+4k`` and its duration is the previous TR (TI for the first); the
+    inversion of a later repetition follows the last TR.
+    """
+    per_rep = 1 + 4 * pulses
+    exc = 1 + 4 * np.arange(pulses)
+    flip = np.stack([r * per_rep + exc for r in range(repetitions)])
+    tr = [(r * per_rep + exc[k + 1], k) for r in range(repetitions) for k in range(pulses - 1)]
+    tr += [(r * per_rep, pulses - 1) for r in range(1, repetitions)]
+    ti = np.array([r * per_rep + exc[0] for r in range(repetitions)], np.int64)
+    return {"flip": flip.astype(np.int64), "tr": np.array(tr, np.int64).reshape(-1, 2), "ti": ti}
+
+
+def played_flip_torch(flip_deg: torch.Tensor) -> torch.Tensor:
+    """The flip a pulse plays, differentiable: 2*pi*|deg2rad(flip)*area|."""
+    return 2.0 * torch.pi * torch.abs(torch.deg2rad(flip_deg.to(torch.float32)) * _HARD_PULSE_AREA)
+
+
 def fse_events(flip_deg: Any, ESP_ms: float, phases_deg: Any = 0.0, exc_flip: float = 90.0,
                exc_phase: float = 90.0) -> PackedEvents:
     """The refocused train of ``FSESimulator._train`` (simulators/fse.py:75-104)."""

@@ -23,7 +23,8 @@ import numpy as np
 import torch
 
 from . import engine
-from .sequence import PackedEvents, fse_events, mrf_events, program_for
+from .sequence import (PackedEvents, fse_events, mrf_events, mrf_gradient_map, played_flip_torch,
+                       program_for)
 
 
 def _tensorish(value: Any) -> bool:
@@ -144,9 +145,60 @@ class _EpgSimulator:
         return list(names)
 
     def simulate(self, **values: Any) -> torch.Tensor:
-        """Return the recorded signal, ``(*voxels, samples)`` complex64."""
+        """Return the recorded signal, ``(*voxels, samples)`` complex64.
+
+        Differentiable: when a property or a sequence argument requires grad,
+        the result carries a backward that runs the checkpointed adjoint
+        kernel (``engine.EpgFunction``)."""
+        if torch.is_grad_enabled() and any(
+                isinstance(v, torch.Tensor) and v.requires_grad
+                for v in {**self.protocol, **values}.values()):
+            return self._run_differentiable(values)
         signal, _ = self._run(values, None)
         return signal
+
+    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions):
+        """Attach the protocol's differentiable arguments to the event buffers."""
+        if any(isinstance(v, torch.Tensor) and v.requires_grad for v in protocol.values()):
+            raise NotImplementedError(
+                f"{type(self).__name__}: gradients w.r.t. its sequence arguments are not built")
+        return flip_ev, dur_ev
+
+    def _run_differentiable(self, values: dict[str, Any]) -> torch.Tensor:
+        held, protocol, states, device, repetitions = self._split(values)
+        home = _home(values)
+        dev = engine.require_cuda(torch.device(device) if device is not None else
+                                  (home if home.type == "cuda" else None))
+        plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in protocol.items()}
+        events = self.events(repetitions=repetitions, **plain)
+        if events.real_axis() != 1:
+            raise NotImplementedError("only the real-subspace path is built on this accelerator")
+        batch = _batch(held)
+        voxels = _numel(batch)
+        maps = self._kernel_maps(held)
+
+        def flat(value, clamp=False, optional=True):
+            if value is None:
+                return None
+            if optional and not _tensorish(value) and float(value) == 1.0:
+                return None
+            t = value if isinstance(value, torch.Tensor) else torch.as_tensor(
+                np.asarray(value, np.float32))
+            t = t.to(device=dev, dtype=torch.float32)
+            t = t.expand(batch).reshape(-1) if batch else t.reshape(1)
+            return t.clamp_min(engine.MINIMUM_RELAXATION_TIME_MS) if clamp else t
+
+        with torch.cuda.device(dev):
+            program = program_for(events, dev)
+            flip_ev = torch.from_numpy(events.flip).to(dev)
+            dur_ev = torch.from_numpy(events.duration).to(dev)
+            flip_ev, dur_ev = self._event_gradients(protocol, events, flip_ev, dur_ev, repetitions)
+            signal = engine.EpgFunction.apply(
+                program, states, None, flat(maps["T1"], True, False), flat(maps["T2"], True, False),
+                flat(maps["M0"]), flat(maps["B1"]), flat(maps["inv"]), flip_ev, dur_ev)
+            signal, _ = self._post(signal, None, None, held, plain, dev)
+        signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
+        return signal.to(home) if home.type != "cuda" else signal
 
     def jacobian(self, diff: str | Sequence[str], **values: Any):
         """Return ``(signal, jacobian)``; the Jacobian is ``(*voxels, k, samples)``
@@ -171,6 +223,30 @@ class MRFSimulator(_EpgSimulator):
 
     def events(self, *, flip, TR, TI=0.0, phases=0.0, repetitions=1) -> PackedEvents:
         return mrf_events(flip, TR, TI_ms=TI, phases_deg=phases, repetitions=repetitions)
+
+    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions):
+        flip = protocol.get("flip")
+        tr = protocol.get("TR")
+        ti = protocol.get("TI", 0.0)
+        n = int(torch.atleast_1d(torch.as_tensor(
+            flip.detach() if isinstance(flip, torch.Tensor) else np.asarray(flip))).numel())
+        where = mrf_gradient_map(n, repetitions)
+        dev = flip_ev.device
+        if isinstance(flip, torch.Tensor) and flip.requires_grad:
+            played = played_flip_torch(torch.atleast_1d(flip).to(dev))
+            delta = (played - played.detach()).expand(repetitions, n).reshape(-1)
+            idx = torch.from_numpy(where["flip"].reshape(-1)).to(dev)
+            flip_ev = flip_ev.index_add(1, idx, delta[None])
+        if isinstance(tr, torch.Tensor) and tr.requires_grad:
+            spacing = torch.atleast_1d(tr).to(dev, torch.float32).expand(n) * 1e-3
+            pairs = torch.from_numpy(where["tr"]).to(dev)
+            delta = (spacing - spacing.detach())[pairs[:, 1]]
+            dur_ev = dur_ev.index_add(1, pairs[:, 0], delta[None])
+        if isinstance(ti, torch.Tensor) and ti.requires_grad:
+            t = ti.to(dev, torch.float32).reshape(()) * 1e-3
+            idx = torch.from_numpy(where["ti"]).to(dev)
+            dur_ev = dur_ev.index_add(1, idx, (t - t.detach()).expand(idx.numel())[None])
+        return flip_ev, dur_ev
 
 
 class FSESimulator(_EpgSimulator):
