@@ -209,6 +209,32 @@ int tsg_epg_adjoint(const tsg_program* program, const tsg_tissue* tissue, int64_
                     const tsg_gradients* gradients, void* workspace, int64_t workspace_bytes,
                     const tsg_launch* launch, void* stream);
 
+/* Size of the static scratch array behind tsg_epg_adjoint_noalloc. */
+#define TSG_STATIC_SCRATCH_BYTES (32LL * 1024 * 1024)
+
+/* The checkpointed adjoint for callers that cannot allocate device memory:
+ * a service that plans all its memory at start-up, a framework whose caching
+ * allocator owns the GPU, or a code path where an allocation would
+ * synchronise the device. It has no counterpart in the reference, whose
+ * adjoint allocates its trajectory per call. Inputs and outputs as for
+ * tsg_epg_adjoint (gradients ADD into the given slots), but the checkpoints
+ * and gradient partials live in one static device array of
+ * TSG_STATIC_SCRATCH_BYTES (32 MiB) that every GPU loading this library holds
+ * until the process exits; the entry point calls no cudaMalloc, cudaFree or
+ * other allocating routine. A problem whose scratch exceeds the array is
+ * rejected with TSG_ERR_CAPACITY (tsg_epg_adjoint_plan gives the sizes).
+ * The first call on a device resolves the array's device address on that
+ * device (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the one array: calls whose work overlaps on the
+ * GPU (other streams, other host threads) race on it and must be ordered by
+ * the caller. Nothing a previous call left in it is read. */
+int tsg_epg_adjoint_noalloc(const tsg_program* program, const tsg_tissue* tissue,
+                            int64_t atom_count, int64_t state_count, const float* seed,
+                            int seed_layout, const tsg_gradients* gradients,
+                            const tsg_launch* launch, void* stream);
+/* TSG_STATIC_SCRATCH_BYTES, as built into the library. */
+int64_t tsg_static_scratch_bytes(void);
+
 /* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */
 
 /* _epg_cpu.simulate (src/torchsim/_epg_cpu.cpp:10740-10926): pointers holds

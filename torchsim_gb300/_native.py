@@ -86,6 +86,9 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_epg_adjoint": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _vp, _int, _vp, _int,
                                ctypes.POINTER(Gradients), _vp, _i64, ctypes.POINTER(Launch),
                                _vp]),
+    "tsg_epg_adjoint_noalloc": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _vp, _int,
+                                       ctypes.POINTER(Gradients), ctypes.POINTER(Launch), _vp]),
+    "tsg_static_scratch_bytes": (_i64, []),
     "tsg_epg_simulate_vjp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
                                     _int, _int]),
     "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,
