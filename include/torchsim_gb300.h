@@ -44,7 +44,11 @@ enum {
     TSG_LAYOUT_PLANES = 0,
     /* One interleaved complex64 array holding 1j * signal, which is what
      * MRFSimulator.evaluate returns (simulators/mrf.py:84): (-m0*F+[0], 0). */
-    TSG_LAYOUT_COMPLEX_IJ = 1
+    TSG_LAYOUT_COMPLEX_IJ = 1,
+    /* One interleaved complex64 array holding the signal as the reference's
+     * runs return it, complex(real plane, imaginary plane) = (0, m0*F+[0])
+     * (sequence/_accelerators.py:3449). */
+    TSG_LAYOUT_COMPLEX = 2
 };
 
 /* Structured forward-mode directions the fused kernel carries in one pass. */
@@ -234,6 +238,46 @@ int tsg_epg_adjoint_noalloc(const tsg_program* program, const tsg_tissue* tissue
                             const tsg_launch* launch, void* stream);
 /* TSG_STATIC_SCRATCH_BYTES, as built into the library. */
 int64_t tsg_static_scratch_bytes(void);
+
+/* ---- many sequences in one persistent launch ---------------------------- */
+
+/* One sequence of a batch. Its ops are op_count consecutive entries of the
+ * concatenated op array (16-byte ops as tsg_program_plan describes them:
+ * float dt, float flip, int32 record, uint32 code); its voxels are
+ * voxel_count consecutive entries of the tissue arrays from voxel_offset; its
+ * samples are voxel_count x outputs complex64 from output_offset.
+ * lanes_per_voxel = ceil(states / orders_per_lane) <= 32. */
+typedef struct {
+    int32_t op_offset;
+    int32_t op_count;
+    int32_t states;
+    int32_t lanes_per_voxel;
+    int32_t outputs;
+    int32_t voxel_count;
+    int64_t voxel_offset;
+    int64_t output_offset;
+} tsg_batch_sequence;
+
+/* One unit of work: voxel_count voxels of a sequence from voxel_begin (at
+ * most warps_per_block * floor(32 / lanes_per_voxel)). */
+typedef struct {
+    int32_t sequence;
+    int32_t voxel_begin;
+    int32_t voxel_count;
+    int32_t reserved;
+} tsg_batch_unit;
+
+/* Forward of every unit in ONE persistent launch of `blocks` CTAs that take
+ * units from `counter` (DEVICE int32, reset here with a memset on `stream`)
+ * in list order; put the largest units first. All pointers are DEVICE
+ * pointers. The output is TSG_LAYOUT_COMPLEX. orders_per_lane: 2, 4 or 8.
+ * Capturable in a CUDA graph (a memset node and a kernel node). No
+ * counterpart in the reference, which launches one kernel per sequence
+ * (sequence/_epg_triton.py:17120-17300). */
+int tsg_epg_batched_forward(const void* ops, const tsg_batch_sequence* sequences,
+                            const tsg_batch_unit* units, int64_t unit_count, int32_t* counter,
+                            const tsg_tissue* tissue, void* out, int orders_per_lane,
+                            int warps_per_block, int blocks, void* stream);
 
 /* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */
 

@@ -20,6 +20,7 @@ TSG_ERR_CAPACITY = -4
 
 LAYOUT_PLANES = 0
 LAYOUT_COMPLEX_IJ = 1
+LAYOUT_COMPLEX = 2
 
 TANGENT_T1 = 1
 TANGENT_T2 = 2
@@ -47,6 +48,18 @@ class Direction(ctypes.Structure):
 class Gradients(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in
                 ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")]
+
+
+class BatchSequence(ctypes.Structure):
+    _fields_ = [("op_offset", ctypes.c_int32), ("op_count", ctypes.c_int32),
+                ("states", ctypes.c_int32), ("lanes_per_voxel", ctypes.c_int32),
+                ("outputs", ctypes.c_int32), ("voxel_count", ctypes.c_int32),
+                ("voxel_offset", ctypes.c_int64), ("output_offset", ctypes.c_int64)]
+
+
+class BatchUnit(ctypes.Structure):
+    _fields_ = [("sequence", ctypes.c_int32), ("voxel_begin", ctypes.c_int32),
+                ("voxel_count", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Launch(ctypes.Structure):
@@ -89,6 +102,8 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_epg_adjoint_noalloc": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _vp, _int,
                                        ctypes.POINTER(Gradients), ctypes.POINTER(Launch), _vp]),
     "tsg_static_scratch_bytes": (_i64, []),
+    "tsg_epg_batched_forward": (_int, [_vp, _vp, _vp, _i64, _vp, ctypes.POINTER(Tissue), _vp, _int,
+                                       _int, _int, _vp]),
     "tsg_epg_simulate_vjp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
                                     _int, _int]),
     "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,

@@ -223,6 +223,8 @@ extern "C" int tsg_epg_forward(const tsg_program* program, const tsg_tissue* tis
     int rc = check_common(program, tissue, atom_count, state_count);
     if (rc) return rc;
     if (atom_count == 0) return TSG_OK;
+    if (layout < TSG_LAYOUT_PLANES || layout > TSG_LAYOUT_COMPLEX)
+        return fail(TSG_ERR_ARGUMENT, "unknown layout");
     if (layout == TSG_LAYOUT_PLANES ? !out_b : !out_a)
         return fail(TSG_ERR_ARGUMENT, "null output buffer");
     SweepArgs a = base_args(program, tissue, atom_count, state_count);

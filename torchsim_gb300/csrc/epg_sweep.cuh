@@ -68,6 +68,8 @@ __device__ __forceinline__ void put_sample(int layout, float* a, float* b, int64
     if (layout == TSG_LAYOUT_PLANES) {
         if (a) __stcs(a + idx, 0.f);
         __stcs(b + idx, v);
+    } else if (layout == TSG_LAYOUT_COMPLEX) {
+        __stcs(reinterpret_cast<float2*>(a) + idx, make_float2(0.f, v));
     } else {
         __stcs(reinterpret_cast<float2*>(a) + idx, make_float2(-v, 0.f));
     }
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
             }
             if ((code & OP_RECORD) && q == 0 && active) {
                 const int64_t idx = row * a.outputs + op.record;
-                if (a.sig_b != nullptr || a.layout == TSG_LAYOUT_COMPLEX_IJ) {
+                if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
                     if (a.sig_a != nullptr || a.sig_b != nullptr)
                         put_sample(a.layout, a.sig_a, a.sig_b, idx, m0 * P[0]);
                 }
