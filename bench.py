@@ -338,6 +338,8 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         line["adjoint"] = adjoint_section(torch, device)
     if not args.skip_batched:
         line["batched"] = batched_section(torch, device)
+    if not args.skip_gn:
+        line["gn_server"] = gn_section(torch, device)
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     return line
@@ -465,6 +467,91 @@ def batched_section(torch, device, sequences: int = 512, repeats: int = 5) -> di
     }
 
 
+# ---- Gauss-Newton mapping server ---------------------------------------------
+
+
+def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
+    """Poisson arrivals (20 req/s, seeded); each request one slice of
+    round(exp(U(ln 4096, ln 262144))) voxels of the 880-pulse MRF signal at
+    ground-truth T1/T2/B1 (drawn as the 1,024-voxel workload) and M0 U(0.5,1.5)
+    plus complex Gaussian noise at SNR 50 (sigma = mean|s|/50); B1 known;
+    unknowns (T1, T2, M0) bounded (50,5000), (2,1000), (0,5); start at the
+    median of a training draw; <= 10 LM steps with FP64 3x3 solves; 120 GB
+    admission budget. The continuously batched server against the same fused
+    solver serving one request at a time, first come first served."""
+    from torchsim_gb300 import engine
+    from torchsim_gb300.recon import GaussNewton, NonlinearLeastSquares, TrustRegion
+    from torchsim_gb300.sequence import mrf_events, program_for
+    from torchsim_gb300.serving import GNServer, MapRequest, latency_summary, serve_plain
+
+    rng = np.random.default_rng(4)
+    program = program_for(mrf_events(mrf_schedule(), 10.0), device)
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
+    draw_t1 = np.exp(rng.uniform(np.log(100), np.log(3000), 4096))
+    draw_t2 = np.exp(rng.uniform(np.log(10), np.log(300), 4096))
+    draw_m0 = rng.uniform(0.5, 1.5, 4096)
+    est = NonlinearLeastSquares(None, bounds=bounds).fit(
+        parameters=torch.tensor(np.stack([draw_t1, draw_t2, draw_m0], 1)))
+    start = est._start
+    gaps = rng.exponential(1.0 / rate, requests)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    made = []
+    gen = torch.Generator(device=device).manual_seed(4)
+    for i in range(requests):
+        V = int(round(np.exp(rng.uniform(np.log(4096), np.log(262144)))))
+        t1 = np.exp(rng.uniform(np.log(100), np.log(3000), V)).astype(np.float32)
+        t2 = np.minimum(np.exp(rng.uniform(np.log(10), np.log(300), V)), 0.999 * t1).astype(np.float32)
+        b1 = rng.uniform(0.8, 1.2, V).astype(np.float32)
+        m0 = rng.uniform(0.5, 1.5, V).astype(np.float32)
+        tissue = engine.tissue_maps(device, V, t1, t2, m0, b1, None)
+        sig = engine.forward(program, tissue, 10)
+        sigma = sig.abs().mean() / 50
+        sig = sig + sigma * torch.complex(torch.randn(sig.shape, device=device, generator=gen),
+                                          torch.randn(sig.shape, device=device, generator=gen))
+        made.append((sig, torch.from_numpy(b1).to(device), float(arrivals[i]), (t1, t2, m0)))
+    torch.cuda.synchronize()
+    loop = GaussNewton(TrustRegion(), max_iterations=10)
+    total_voxels = sum(m[0].shape[0] for m in made)
+
+    def requests_list():
+        return [MapRequest(s, b, arrival=a, id=i) for i, (s, b, a, _) in enumerate(made)]
+
+    # Warm the kernels and the launch path outside the measured runs.
+    warm = GNServer(program, 10, bounds, start, loop, budget_bytes=2 << 30, device=device)
+    warm.serve([MapRequest(made[0][0][:4096], made[0][1][:4096], id=0)], realtime=False)
+
+    server = GNServer(program, 10, bounds, start, loop, budget_bytes=120 * 2**30, device=device)
+    t0 = time.perf_counter()
+    done = server.serve(requests_list(), realtime=True)
+    torch.cuda.synchronize()
+    span = time.perf_counter() - t0
+    lat = latency_summary(done)
+    # Accuracy against the ground truth (median relative error over voxels).
+    errs = []
+    for r in done:
+        t1, t2, m0 = made[r.id][3]
+        errs.append(np.abs(r.maps["T1"].cpu().numpy() - t1) / t1)
+    err = float(np.median(np.concatenate(errs)))
+
+    plain_reqs = requests_list()
+    t0 = time.perf_counter()
+    plain_done = serve_plain(program, 10, bounds, start, plain_reqs, loop)
+    plain_span = time.perf_counter() - t0
+    plain_lat = latency_summary(plain_done)
+    return {
+        "workload": f"{requests} requests, Poisson {rate}/s, {total_voxels} voxels, 880-pulse "
+                    "MRF, nstates 10, SNR 50, <=10 LM steps, 120 GB budget",
+        "server": {"maps_per_s": total_voxels / span, "makespan_s": span, **lat,
+                   "iterations": server.stats.iterations,
+                   "launches_per_iteration": 3,
+                   "peak_live_voxels": server.stats.peak_live_voxels,
+                   "voxel_iterations": server.stats.voxel_iterations},
+        "plain_one_request_at_a_time": {"maps_per_s": total_voxels / plain_span,
+                                        "makespan_s": plain_span, **plain_lat},
+        "t1_median_relative_error": err,
+    }
+
+
 # ---- CPU baselines ----------------------------------------------------------
 
 
@@ -585,6 +672,7 @@ def main() -> None:
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-gn", action="store_true")
     ap.add_argument("--atoms", type=int, default=ATOMS,
                     help="first N grid atoms (a smaller case for profiling; default all)")
     ap.add_argument("--launch", type=int, nargs=3, metavar=("LANES", "ORDERS", "WARPS"))

@@ -279,6 +279,72 @@ int tsg_epg_batched_forward(const void* ops, const tsg_batch_sequence* sequences
                             const tsg_tissue* tissue, void* out, int orders_per_lane,
                             int warps_per_block, int blocks, void* stream);
 
+/* ---- Gauss-Newton mapping ---------------------------------------------- */
+
+/* One fused evaluation of Gauss-Newton normal equations (one train only):
+ * forward plus the T1 and T2 tangents at the tissue given (natural T1, T2, M0,
+ * and B1), reduced against the measured complex64 samples of the API signal
+ * (row measured_rows[voxel], or the voxel's own row when null) to 10 doubles
+ * per voxel: cost sum|s - y|^2, the upper triangle of J^T J by rows (T1T1,
+ * T1T2, T1M0, T2T2, T2M0, M0M0) and sum dv*(v + Re y) (= J_s^T r), all in
+ * natural parameters. Replaces the reference's forward + one forward+JVP pass
+ * per column and the Jacobian blocks it stores (recon/_gauss_newton.py:
+ * 633-651). */
+int tsg_gn_evaluate(const tsg_program* program, const tsg_tissue* tissue, int64_t atom_count,
+                    int64_t state_count, const void* measured, const int64_t* measured_rows,
+                    double* normal_equations, const tsg_launch* launch, void* stream);
+
+enum { TSG_GN_FIRST = 0, TSG_GN_LIVE = 1, TSG_GN_DONE = 2 };
+
+/* Device-resident per-voxel Levenberg-Marquardt state (all DEVICE arrays of
+ * voxel_count rows): free variables u (3), candidate (3), cost, accepted
+ * normal equations (10, as tsg_gn_evaluate writes them), the candidate's
+ * (10), damping, its rising factor, the predicted decrease, status
+ * (TSG_GN_*), step flags (bit 0 short, bit 1 singular), steps taken, and the
+ * candidate's natural T1, T2, M0 (float) for the next evaluation. */
+typedef struct {
+    double* u;
+    double* cand;
+    double* cost;
+    double* normal;
+    double* trial;
+    double* damping;
+    double* rising;
+    double* predicted;
+    int32_t* status;
+    int32_t* flags;
+    int32_t* iterations;
+    float* t1;
+    float* t2;
+    float* m0;
+} tsg_gn_state;
+
+/* Bounds (low/high per T1, T2, M0; +-inf for none), TrustRegion tau, the
+ * gradient and step tolerances and the step limit (GaussNewton's knobs,
+ * recon/_gauss_newton.py:445-473). */
+typedef struct {
+    double low[3];
+    double high[3];
+    double tau;
+    double gradient_tolerance;
+    double step_tolerance;
+    int32_t max_iterations;
+} tsg_gn_config;
+
+/* Retires flat voxels, solves the damped step (FP64 3x3 Cholesky) and writes
+ * the candidate's natural parameters; FIRST voxels are evaluated where they
+ * stand. */
+int tsg_gn_step(const tsg_gn_state* state, int64_t voxel_count, const tsg_gn_config* config,
+                void* stream);
+/* After tsg_gn_evaluate at the candidates: the gain test and Nielsen damping
+ * update of TrustRegion.judge (recon/_gauss_newton.py:395-411), acceptance,
+ * and retirement on a short step or the step limit. */
+int tsg_gn_judge(const tsg_gn_state* state, int64_t voxel_count, const tsg_gn_config* config,
+                 void* stream);
+/* Natural parameters (voxel_count x 3 floats) of free variables. */
+int tsg_gn_natural(const double* free_variables, int64_t voxel_count, const tsg_gn_config* config,
+                   float* natural, void* stream);
+
 /* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */
 
 /* _epg_cpu.simulate (src/torchsim/_epg_cpu.cpp:10740-10926): pointers holds

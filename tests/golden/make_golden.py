@@ -267,6 +267,37 @@ def case_adjoint(ts, rec) -> dict:
     return out
 
 
+def case_gn(ts, rec) -> dict:
+    """The reference's NonlinearLeastSquares (Levenberg-Marquardt, default
+    loop: TrustRegion, direct, 20 iterations) on noisy MRF signals."""
+    import torch
+    from torchsim import NonlinearLeastSquares
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(4)
+    n, v = 120, 16
+    flip = np.concatenate([np.linspace(5, 60, 60), np.linspace(60, 2, 60)]).astype(np.float32)
+    t1, t2, b1 = draw_tissue(rng, v)
+    m0 = rng.uniform(0.5, 1.5, v).astype(np.float32)
+    sim = MRFSimulator(flip=torch.from_numpy(flip), TR=10.0, states=10)
+    with torch.no_grad():
+        sig = sim.simulate(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2),
+                           B1=torch.from_numpy(b1), M0=torch.from_numpy(m0))
+    sigma = float(sig.abs().mean()) / 50.0
+    noise = (rng.standard_normal(sig.shape) + 1j * rng.standard_normal(sig.shape)) * sigma
+    y = (sig.numpy() + noise).astype(np.complex64)
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
+    est = NonlinearLeastSquares(sim, bounds=bounds)
+    est.fit(T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), known={"B1": (0.8, 1.2)}, seed=0)
+    maps = est.map(torch.from_numpy(y), known={"B1": torch.from_numpy(b1)})
+    return {"flip_deg": flip, "tr_ms": np.float32(10.0), "states": np.int64(10), "t1": t1,
+            "t2": t2, "b1": b1, "m0": m0, "measured": y, "start": est._start.numpy(),
+            "bounds": np.array([bounds[k] for k in ("T1", "T2", "M0")], np.float64),
+            "map_t1": maps["T1"].numpy(), "map_t2": maps["T2"].numpy(),
+            "map_m0": maps["M0"].numpy(), "iterations": np.int64(est.iterations),
+            "unconverged": np.int64(est.unconverged)}
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     os.environ.setdefault("OMP_NUM_THREADS", "1")
@@ -282,7 +313,7 @@ def main() -> None:
     _accelerators.detection = lambda kind, device: 0.0
     rec = _Recorder(_accelerators)
     for name, fn in (("mrf880", case_mrf880), ("mrf_prep", case_mrf_prep),
-                     ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint)):
+                     ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn)):
         data = fn(ts, rec)
         np.savez_compressed(HERE / f"{name}.npz", **data)
         print(f"wrote {name}.npz with {len(data)} arrays")

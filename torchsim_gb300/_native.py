@@ -62,6 +62,18 @@ class BatchUnit(ctypes.Structure):
                 ("voxel_count", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class GNState(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("u", "cand", "cost", "normal", "trial", "damping", "rising", "predicted", "status",
+                 "flags", "iterations", "t1", "t2", "m0")]
+
+
+class GNConfig(ctypes.Structure):
+    _fields_ = [("low", ctypes.c_double * 3), ("high", ctypes.c_double * 3),
+                ("tau", ctypes.c_double), ("gradient_tolerance", ctypes.c_double),
+                ("step_tolerance", ctypes.c_double), ("max_iterations", ctypes.c_int32)]
+
+
 class Launch(ctypes.Structure):
     _fields_ = [("lanes_per_voxel", ctypes.c_int), ("orders_per_lane", ctypes.c_int),
                 ("warps_per_block", ctypes.c_int)]
@@ -104,6 +116,11 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_static_scratch_bytes": (_i64, []),
     "tsg_epg_batched_forward": (_int, [_vp, _vp, _vp, _i64, _vp, ctypes.POINTER(Tissue), _vp, _int,
                                        _int, _int, _vp]),
+    "tsg_gn_evaluate": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _vp, _vp, _vp,
+                               ctypes.POINTER(Launch), _vp]),
+    "tsg_gn_step": (_int, [ctypes.POINTER(GNState), _i64, ctypes.POINTER(GNConfig), _vp]),
+    "tsg_gn_judge": (_int, [ctypes.POINTER(GNState), _i64, ctypes.POINTER(GNConfig), _vp]),
+    "tsg_gn_natural": (_int, [_vp, _i64, ctypes.POINTER(GNConfig), _vp, _vp]),
     "tsg_epg_simulate_vjp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
                                     _int, _int]),
     "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,

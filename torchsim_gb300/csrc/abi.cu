@@ -24,6 +24,7 @@ Table table_for(int mode) {
         case MODE_T12B: return {kSweepT12B, kSweepT12BCount};
         case MODE_T12BI: return {kSweepT12BI, kSweepT12BICount};
         case MODE_GENERAL: return {kSweepGeneral, kSweepGeneralCount};
+        case MODE_GN: return {kSweepGN, kSweepGNCount};
     }
     return {nullptr, 0};
 }
@@ -293,6 +294,24 @@ extern "C" int tsg_epg_forward_tangents(const tsg_program* program, const tsg_ti
     a.col_inv = columns[3];
     a.col_m0 = columns[4];
     return launch(mode, program, a, atom_count, int(state_count), launch_shape,
+                  static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tsg_gn_evaluate(const tsg_program* program, const tsg_tissue* tissue,
+                               int64_t atom_count, int64_t state_count, const void* measured,
+                               const int64_t* measured_rows, double* normal_equations,
+                               const tsg_launch* launch_shape, void* stream) {
+    int rc = check_common(program, tissue, atom_count, state_count);
+    if (rc) return rc;
+    if (atom_count == 0) return TSG_OK;
+    if (!measured || !normal_equations) return fail(TSG_ERR_ARGUMENT, "null measured or output buffer");
+    if (program->host.trains != 1) return fail(TSG_ERR_UNSUPPORTED, "Gauss-Newton runs one train");
+    SweepArgs a = base_args(program, tissue, atom_count, state_count);
+    a.layout = TSG_LAYOUT_COMPLEX_IJ;
+    a.measured = static_cast<const float2*>(measured);
+    a.measured_rows = measured_rows;
+    a.gn_out = normal_equations;
+    return launch(MODE_GN, program, a, atom_count, int(state_count), launch_shape,
                   static_cast<cudaStream_t>(stream));
 }
 

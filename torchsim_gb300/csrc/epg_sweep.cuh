@@ -75,7 +75,7 @@ __device__ __forceinline__ void put_sample(int layout, float* a, float* b, int64
     }
 }
 
-template <int R, int L, int TM, bool GEN>
+template <int R, int L, int TM, bool GEN, bool GN = false>
 __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
     using S = SystemLayout<TM, GEN>;
     constexpr int NT = S::N;
@@ -125,6 +125,22 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
 
     float last_dt = __int_as_float(0x7fffffff);  // NaN: first relax computes
     float e1 = 1.f, e2 = 1.f, k1 = 0.f, k2 = 0.f;
+
+    // Gauss-Newton sums: float over chunks of 32 samples, then into doubles.
+    static_assert(!GN || (S::T1 && S::T2), "GN sweeps carry the T1 and T2 tangents");
+    float cs[10];
+    double cd[10];
+    int in_chunk = 0;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        cs[k] = 0.f;
+        cd[k] = 0.0;
+    }
+    const float2* yrow = nullptr;
+    if constexpr (GN) {
+        const int64_t mrow = a.measured_rows ? a.measured_rows[ac] : (train * a.atoms + ac);
+        yrow = a.measured + mrow * a.outputs;
+    }
 
     const Op* ops = a.ops + train * a.n_ops;
     const float2* dirs = GEN ? a.op_dir + train * a.n_ops : nullptr;
@@ -313,7 +329,38 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
                     for (int j = 0; j < NT; ++j) dP[j][r] = dM[j][r] = 0.f;
                 }
             }
-            if ((code & OP_RECORD) && q == 0 && active) {
+            if constexpr (GN) {
+                if ((code & OP_RECORD) && q == 0 && active) {
+                    // API signal s = -v (v = m0 F+[0]); r = s - y. Columns of
+                    // dv: T1, T2 (tangents), M0 (F+[0]); J^T J and J^T r
+                    // carry the sign of s twice or not at all.
+                    const float2 y = yrow[op.record];
+                    const float v = m0 * P[0];
+                    const float res = v + y.x;  // -(r.real)
+                    const float j1 = m0 * dP[S::I_T1][0];
+                    const float j2 = m0 * dP[S::I_T2][0];
+                    const float j3 = P[0];
+                    cs[0] = fmaf(res, res, fmaf(y.y, y.y, cs[0]));
+                    cs[1] = fmaf(j1, j1, cs[1]);
+                    cs[2] = fmaf(j1, j2, cs[2]);
+                    cs[3] = fmaf(j1, j3, cs[3]);
+                    cs[4] = fmaf(j2, j2, cs[4]);
+                    cs[5] = fmaf(j2, j3, cs[5]);
+                    cs[6] = fmaf(j3, j3, cs[6]);
+                    cs[7] = fmaf(j1, res, cs[7]);
+                    cs[8] = fmaf(j2, res, cs[8]);
+                    cs[9] = fmaf(j3, res, cs[9]);
+                    if (++in_chunk == 32) {
+#pragma unroll
+                        for (int k = 0; k < 10; ++k) {
+                            cd[k] += double(cs[k]);
+                            cs[k] = 0.f;
+                        }
+                        in_chunk = 0;
+                    }
+                }
+            }
+            if ((code & OP_RECORD) && q == 0 && active && !GN) {
                 const int64_t idx = row * a.outputs + op.record;
                 if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
                     if (a.sig_a != nullptr || a.sig_b != nullptr)
@@ -359,14 +406,22 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
             }
         }
     }
+    if constexpr (GN) {
+        if (q == 0 && active) {
+            double* dst = a.gn_out + row * 10;
+#pragma unroll
+            for (int k = 0; k < 10; ++k) dst[k] = cd[k] + double(cs[k]);
+        }
+    }
 }
 
-template <int R, int L, int TM, bool GEN>
+template <int R, int L, int TM, bool GEN, bool GN = false>
 void launch_sweep(const SweepArgs& a, dim3 grid, dim3 block, size_t smem, cudaStream_t stream) {
-    epg_sweep_kernel<R, L, TM, GEN><<<grid, block, smem, stream>>>(a);
+    epg_sweep_kernel<R, L, TM, GEN, GN><<<grid, block, smem, stream>>>(a);
 }
 
 }  // namespace tsg
 
 #define TSG_SWEEP_ENTRY(MODE, R, L, TM, GEN) \
-    {MODE, R, L, &::tsg::launch_sweep<R, L, TM, GEN>}
+    {MODE, R, L, &::tsg::launch_sweep<R, L, TM, GEN, false>}
+#define TSG_GN_ENTRY(R, L) {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<R, L, 3, false, true>}

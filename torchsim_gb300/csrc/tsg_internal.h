@@ -120,6 +120,13 @@ struct SweepArgs {
     float* ckpt;
     int ckpt_every;
     int ckpt_count;
+    // Gauss-Newton accumulation (GN sweeps): the measured samples (complex64
+    // of the API signal) at row measured_rows[atom] (or atom when null), and
+    // per voxel: cost, J^T J (6, upper triangle by rows) and J^T r (3) of the
+    // natural parameters (T1, T2, M0), written as 10 doubles.
+    const float2* measured;
+    const int64_t* measured_rows;
+    double* gn_out;
 };
 
 using SweepLaunch = void (*)(const SweepArgs&, dim3 grid, dim3 block, size_t smem,
@@ -132,6 +139,7 @@ enum SweepMode : int {
     MODE_T12B = 7,      // T1, T2, B1
     MODE_T12BI = 15,    // T1, T2, B1, inversion
     MODE_GENERAL = 16,  // one general direction
+    MODE_GN = 35,       // T1, T2 (+ free M0) reduced to Gauss-Newton normal equations
 };
 
 struct SweepEntry {
@@ -152,6 +160,8 @@ extern const SweepEntry kSweepT12BI[];
 extern const int kSweepT12BICount;
 extern const SweepEntry kSweepGeneral[];
 extern const int kSweepGeneralCount;
+extern const SweepEntry kSweepGN[];
+extern const int kSweepGNCount;
 
 constexpr int kOpChunk = 1024;  // ops staged in shared memory at a time
 
