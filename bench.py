@@ -538,6 +538,31 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
     plain_done = serve_plain(program, 10, bounds, start, plain_reqs, loop)
     plain_span = time.perf_counter() - t0
     plain_lat = latency_summary(plain_done)
+
+    # Capacity: every request present at once (saturated), the server against
+    # the same solver one request at a time and against the plain form laid
+    # out as the reference lays it out (forward + one pass per Jacobian
+    # column, Jacobian in HBM), on the first `sat` requests.
+    from torchsim_gb300.recon import PlainGaussNewton
+
+    sat = min(requests, 12)
+    sat_vox = sum(m[0].shape[0] for m in made[:sat])
+    burst = [MapRequest(s, b, arrival=0.0, id=i) for i, (s, b, a, _) in enumerate(made[:sat])]
+    srv = GNServer(program, 10, bounds, start, loop, budget_bytes=120 * 2**30, device=device)
+    t0 = time.perf_counter()
+    srv.serve(burst, realtime=False)
+    torch.cuda.synchronize()
+    sat_server = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    serve_plain(program, 10, bounds, start,
+                [MapRequest(s, b, arrival=0.0, id=i) for i, (s, b, a, _) in enumerate(made[:sat])],
+                loop)
+    sat_fifo = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    serve_plain(program, 10, bounds, start,
+                [MapRequest(s, b, arrival=0.0, id=i) for i, (s, b, a, _) in enumerate(made[:sat])],
+                PlainGaussNewton(TrustRegion(), max_iterations=10))
+    sat_plain = time.perf_counter() - t0
     return {
         "workload": f"{requests} requests, Poisson {rate}/s, {total_voxels} voxels, 880-pulse "
                     "MRF, nstates 10, SNR 50, <=10 LM steps, 120 GB budget",
@@ -548,6 +573,10 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
                    "voxel_iterations": server.stats.voxel_iterations},
         "plain_one_request_at_a_time": {"maps_per_s": total_voxels / plain_span,
                                         "makespan_s": plain_span, **plain_lat},
+        "saturated": {"requests": sat, "voxels": sat_vox,
+                      "server_maps_per_s": sat_vox / sat_server,
+                      "fused_one_at_a_time_maps_per_s": sat_vox / sat_fifo,
+                      "reference_layout_plain_maps_per_s": sat_vox / sat_plain},
         "t1_median_relative_error": err,
     }
 

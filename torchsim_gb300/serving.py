@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 
 import torch
 
-from .recon import UNKNOWN, GaussNewton, VoxelPool, natural_of, to_free
+from .recon import UNKNOWN, GaussNewton, VoxelPool, fixed_shape, natural_of, to_free
 from .sequence import Program
 
 
@@ -107,7 +107,9 @@ class GNServer:
         self.loop = loop if loop is not None else GaussNewton(max_iterations=10)
         self.config = self.loop.config(self.bounds)
         self.device = device or torch.device("cuda", torch.cuda.current_device())
-        self.launch = launch
+        # One launch shape for every iteration, whatever the live voxel count:
+        # a voxel's arithmetic then never depends on the batch it is in.
+        self.launch = launch if launch is not None else fixed_shape(self.states)
         self.outputs = int(program.outputs)
         bytes_per_voxel = self.outputs * 8 + VoxelPool.BYTES_PER_VOXEL + 8 * 3 + 4
         self.capacity = max(1, int(budget_bytes // bytes_per_voxel))
