@@ -526,6 +526,7 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
     torch.cuda.synchronize()
     span = time.perf_counter() - t0
     lat = latency_summary(done)
+    server_stats = server.stats
     # Accuracy against the ground truth (median relative error over voxels).
     errs = []
     for r in done:
@@ -545,6 +546,8 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
     # column, Jacobian in HBM), on the first `sat` requests.
     from torchsim_gb300.recon import PlainGaussNewton
 
+    del server, warm
+    torch.cuda.empty_cache()
     sat = min(requests, 12)
     sat_vox = sum(m[0].shape[0] for m in made[:sat])
     burst = [MapRequest(s, b, arrival=0.0, id=i) for i, (s, b, a, _) in enumerate(made[:sat])]
@@ -567,10 +570,10 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
         "workload": f"{requests} requests, Poisson {rate}/s, {total_voxels} voxels, 880-pulse "
                     "MRF, nstates 10, SNR 50, <=10 LM steps, 120 GB budget",
         "server": {"maps_per_s": total_voxels / span, "makespan_s": span, **lat,
-                   "iterations": server.stats.iterations,
+                   "iterations": server_stats.iterations,
                    "launches_per_iteration": 3,
-                   "peak_live_voxels": server.stats.peak_live_voxels,
-                   "voxel_iterations": server.stats.voxel_iterations},
+                   "peak_live_voxels": server_stats.peak_live_voxels,
+                   "voxel_iterations": server_stats.voxel_iterations},
         "plain_one_request_at_a_time": {"maps_per_s": total_voxels / plain_span,
                                         "makespan_s": plain_span, **plain_lat},
         "saturated": {"requests": sat, "voxels": sat_vox,
