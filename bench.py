@@ -337,9 +337,9 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     if not args.skip_adjoint:
         line["adjoint"] = adjoint_section(torch, device)
     if not args.skip_batched:
-        line["batched"] = batched_section(torch, device)
+        line["batched"] = batched_section(torch, device, sequences=args.batch_sequences)
     if not args.skip_gn:
-        line["gn_server"] = gn_section(torch, device)
+        line["gn_server"] = gn_section(torch, device, requests=args.gn_requests)
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
     return line
@@ -470,7 +470,7 @@ def batched_section(torch, device, sequences: int = 512, repeats: int = 5) -> di
 # ---- Gauss-Newton mapping server ---------------------------------------------
 
 
-def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:
+def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:  # noqa: C901
     """Poisson arrivals (20 req/s, seeded); each request one slice of
     round(exp(U(ln 4096, ln 262144))) voxels of the 880-pulse MRF signal at
     ground-truth T1/T2/B1 (drawn as the 1,024-voxel workload) and M0 U(0.5,1.5)
@@ -705,6 +705,8 @@ def main() -> None:
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-gn", action="store_true")
+    ap.add_argument("--gn-requests", type=int, default=40)
+    ap.add_argument("--batch-sequences", type=int, default=512)
     ap.add_argument("--atoms", type=int, default=ATOMS,
                     help="first N grid atoms (a smaller case for profiling; default all)")
     ap.add_argument("--launch", type=int, nargs=3, metavar=("LANES", "ORDERS", "WARPS"))
