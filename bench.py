@@ -196,7 +196,15 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     sig = torch.empty((atoms, PULSES), dtype=torch.complex64, device=device)
     jac = torch.empty((atoms, 3, PULSES), dtype=torch.complex64, device=device)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
-    launch = tuple(args.launch) if args.launch else None
+    tune_info = None
+    if args.launch:
+        launch = tuple(args.launch)
+    else:
+        t_tune = time.perf_counter()
+        launch = engine.tuned_shape(program, tissue, STATES, names, use_cache=False)
+        tune_info = {"shape": {"lanes_per_voxel": launch[0], "orders_per_lane": launch[1],
+                               "warps_per_block": launch[2]},
+                     "tuning_s": time.perf_counter() - t_tune, "sample_atoms": min(32768, atoms)}
 
     def step():
         engine.forward_tangents(program, tissue, STATES, names, sig_out=sig, jac_out=jac,
@@ -331,6 +339,7 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         "e2e": e2e,
         "plain_form": plain,
         "gpu_launches": args.steps,
+        "launch_shape": tune_info if tune_info else {"given": list(launch)},
         "clocks": clk,
         "wall_s_timed_region": wall,
     }

@@ -166,6 +166,54 @@ def forward_tangents(program: Program, tissue: TissueMaps, states: int, names: S
     return sig, jac
 
 
+# (lanes per voxel, orders per lane) instantiated per kernel family, as in the
+# sweep tables of csrc/sweep_*.cu.
+FAMILY_SHAPES = {
+    0: [(1, 10), (1, 20), (2, 5), (2, 10), (4, 4), (4, 5), (4, 8), (8, 4), (8, 8), (16, 4),
+        (16, 8), (32, 4), (32, 8)],
+    3: [(1, 10), (2, 5), (2, 10), (4, 4), (4, 5), (4, 8), (8, 4), (8, 8), (16, 4), (16, 8),
+        (32, 4)],
+    7: [(2, 5), (4, 3), (4, 4), (4, 5), (8, 3), (8, 4), (16, 4), (32, 4)],
+    15: [(2, 5), (4, 4), (8, 4), (16, 4), (32, 4)],
+}
+
+
+def mode_of(names: Sequence[str]) -> int:
+    mask, _ = plan_tangents(names)
+    for family in (0, 3, 7, 15):
+        if mask & ~family == 0:
+            return family
+    raise ValueError("no kernel family carries these tangents")
+
+
+def tuned_shape(program: Program, tissue: TissueMaps, states: int, names: Sequence[str] = (),
+                sample: int = 32768, use_cache: bool = True) -> tuple[int, int, int]:
+    """The autotuner's (lanes, orders, warps) for this sweep, timed on the
+    first ``sample`` voxels and cached per (family, states, ops, outputs)."""
+    from . import autotune
+
+    family = mode_of(names) if names else 0
+    n = min(sample, tissue.voxels)
+    sub = TissueMaps(*[None if t is None else t[:n] for t in
+                       (tissue.t1, tissue.t2, tissue.m0, tissue.b1, tissue.inv)])
+    key = autotune.workload_key("sweep", family=family, states=states, ops=program.ops,
+                                outputs=program.outputs, sample=n)
+    sig = torch.empty((program.trains * n, program.outputs), dtype=torch.complex64,
+                      device=tissue.t1.device)
+    jac = torch.empty((program.trains * n, max(1, len(names)), program.outputs),
+                      dtype=torch.complex64, device=tissue.t1.device)
+
+    def run(shape):
+        if names:
+            forward_tangents(program, sub, states, names, sig_out=sig, jac_out=jac, launch=shape)
+        else:
+            forward(program, sub, states, out=sig, launch=shape)
+
+    cands = autotune.sweep_shapes(states, FAMILY_SHAPES[family])
+    best, _ = autotune.tune(key, cands, run, use_cache=use_cache)
+    return tuple(best)
+
+
 def tangent(program: Program, tissue: TissueMaps, states: int, *, t1=None, t2=None, m0=None,
             b1=None, inv=None, duration=None, flip=None, launch=None) -> torch.Tensor:
     """One general forward-mode direction; returns the tangent's imaginary

@@ -331,6 +331,23 @@ class NonlinearLeastSquares:
 
 
 
+def _solve3(M: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """Batched 3x3 SPD solve by Cholesky in torch ops (NaN where not SPD)."""
+    l00 = torch.sqrt(M[:, 0, 0])
+    l10 = M[:, 1, 0] / l00
+    l20 = M[:, 2, 0] / l00
+    l11 = torch.sqrt(M[:, 1, 1] - l10 * l10)
+    l21 = (M[:, 2, 1] - l20 * l10) / l11
+    l22 = torch.sqrt(M[:, 2, 2] - l20 * l20 - l21 * l21)
+    y0 = b[:, 0] / l00
+    y1 = (b[:, 1] - l10 * y0) / l11
+    y2 = (b[:, 2] - l20 * y0 - l21 * y1) / l22
+    x2 = y2 / l22
+    x1 = (y1 - l21 * x2) / l11
+    x0 = (y0 - l10 * x1 - l20 * x2) / l00
+    return torch.stack([x0, x1, x2], dim=-1)
+
+
 class PlainGaussNewton(GaussNewton):
     """The plain GPU form of the same Levenberg-Marquardt loop, laid out as
     the reference lays it out (``_at`` -> ``ModelOperator.jacobian`` ->
@@ -394,7 +411,7 @@ class PlainGaussNewton(GaussNewton):
                 damping, rising = damping[keep], rising[keep]
             if live.numel() == 0:
                 break
-            step = torch.linalg.solve(A + damping[:, None, None] * eye, -g)
+            step = _solve3(A + damping[:, None, None] * eye, -g)
             singular = ~torch.isfinite(step).all(-1)
             short = step.norm(dim=-1) < self.step_tolerance * (u.norm(dim=-1) + self.step_tolerance)
             cand = u + step
