@@ -138,8 +138,9 @@ class ClockSampler:
 # ---- the GPU arm ------------------------------------------------------------
 
 
-def fp32_peak(torch, lib, device) -> float:
-    """FP32 FLOP/s of the FMA probe kernel on this GPU (best of 5)."""
+def fp32_peak(torch, lib, device, paired: bool = False) -> float:
+    """FP32 FLOP/s of the FMA probe kernel on this GPU (best of 5); with
+    ``paired`` the probe issues paired FMAs (two per instruction)."""
     import ctypes
 
     sms = torch.cuda.get_device_properties(device).multi_processor_count
@@ -151,7 +152,8 @@ def fp32_peak(torch, lib, device) -> float:
     for _ in range(6):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record()
-        rc = lib.tsg_probe_fp32(blocks, threads, iters, out.data_ptr(), stream, ctypes.byref(flops))
+        probe = lib.tsg_probe_fp32x2 if paired else lib.tsg_probe_fp32
+        rc = probe(blocks, threads, iters, out.data_ptr(), stream, ctypes.byref(flops))
         e.record()
         e.synchronize()
         if rc != 0:
@@ -295,7 +297,9 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
 
     if rank != 0:
         return None
-    peak = fp32_peak(torch, lib, device)
+    peak_scalar = fp32_peak(torch, lib, device)
+    peak_paired = fp32_peak(torch, lib, device, paired=True)
+    peak = max(peak_scalar, peak_paired)
     flops = float(atoms) * PULSES * STATES * FLOPS_PER_UPDATE
     out_bytes = float(sig.numel() * 8 + jac.numel() * 8)
     in_bytes = 3.0 * atoms * 4
@@ -328,7 +332,10 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
             "unit": "TFLOP/s",
             "frac": achieved * 1e12 / peak,
             "traffic": traffic,
-            "peak_source": "measured: FP32 FMA probe kernel on this GPU in this run",
+            "peak_source": "measured: FP32 FMA probe kernels on this GPU in this run (max of "
+                           "scalar and paired FMA)",
+            "peak_scalar_fma": peak_scalar / 1e12,
+            "peak_paired_fma": peak_paired / 1e12,
             "flops_per_launch": flops,
             "hbm": {"achieved_gbs": (out_bytes + in_bytes) / kernel_s / 1e9,
                     "peak_gbs": hbm_peak,

@@ -122,6 +122,10 @@ int tsg_version(void);
  * counterpart: a measurement aid. */
 int tsg_probe_fp32(int64_t blocks, int threads, int iters, float* out, void* stream,
                    double* flops);
+/* The same probe written with paired FP32 FMAs (__ffma2_rn): four chains of
+ * float2 per thread, the same FLOPs per launch. */
+int tsg_probe_fp32x2(int64_t blocks, int threads, int iters, float* out, void* stream,
+                     double* flops);
 
 /* ---- pulse programs ---------------------------------------------------- */
 

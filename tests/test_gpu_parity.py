@@ -118,12 +118,14 @@ def _entries(mode_table):
 
 # Launch shapes instantiated per family (lanes_per_voxel, orders_per_lane).
 SHAPES = {
-    "forward": [(1, 10), (1, 20), (2, 5), (2, 10), (4, 4), (4, 5), (4, 8), (8, 4), (8, 8),
-                (16, 4), (16, 8), (32, 4), (32, 8)],
-    ("T1", "T2"): [(1, 10), (2, 5), (2, 10), (4, 4), (4, 5), (4, 8), (8, 4), (8, 8), (16, 4),
-                   (16, 8), (32, 4)],
-    ("T1", "T2", "B1"): [(2, 5), (4, 3), (4, 4), (4, 5), (8, 3), (8, 4), (16, 4), (32, 4)],
-    ("T1", "T2", "B1", "inv_efficiency"): [(2, 5), (4, 4), (8, 4), (16, 4), (32, 4)],
+    "forward": [(1, 10), (1, 20), (5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (4, 8), (8, 4),
+                (8, 8), (16, 4), (16, 8), (32, 4), (32, 8)],
+    ("T1", "T2"): [(1, 10), (5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (4, 8), (8, 4),
+                   (8, 8), (16, 4), (32, 4)],
+    ("T1", "T2", "B1"): [(5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (8, 4), (16, 4),
+                         (32, 4)],
+    ("T1", "T2", "B1", "inv_efficiency"): [(5, 2), (5, 4), (10, 2), (4, 4), (8, 4), (16, 4),
+                                           (32, 4)],
 }
 
 

@@ -88,6 +88,7 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_last_error": (ctypes.c_char_p, []),
     "tsg_version": (_int, []),
     "tsg_probe_fp32": (_int, [_i64, _int, _int, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),
+    "tsg_probe_fp32x2": (_int, [_i64, _int, _int, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),
     "tsg_program_create": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _int, _vp,
                                   ctypes.POINTER(_vp)]),
     "tsg_program_destroy": (_int, [_vp]),

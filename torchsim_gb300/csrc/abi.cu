@@ -62,7 +62,8 @@ const SweepEntry* choose(int mode, int states, int64_t work_items, const tsg_lau
         const int padded = e.lanes_per_voxel * e.orders_per_lane;
         if (padded < states) continue;
         if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
-        const double waste = double(padded) / states;
+        const int vpw = 32 / e.lanes_per_voxel;
+        const double waste = double(padded) / states * 32.0 / double(vpw * e.lanes_per_voxel);
         const double lanes = double(work_items) * e.lanes_per_voxel;
         const double fill = std::min(1.0, lanes / double(target_lanes));
         // Time ~ padded orders x lane redundancy / GPU fill.
@@ -627,8 +628,36 @@ __global__ void fp32_probe_kernel(float* out, int iters, float seed) {
     if (s == 123456.f) out[blockIdx.x] = s;  // keeps the chains live
 }
 
+// The same with paired FP32 FMAs (two lanes' worth of work per instruction).
+__global__ void fp32x2_probe_kernel(float* out, int iters, float seed) {
+    float2 a0 = make_float2(seed + threadIdx.x, seed - threadIdx.x);
+    float2 a1 = make_float2(a0.x + 1.f, a0.y + 1.f), a2 = make_float2(a0.x + 2.f, a0.y + 2.f);
+    float2 a3 = make_float2(a0.x + 3.f, a0.y + 3.f);
+    const float2 b = make_float2(0.999999f, 0.999999f), c = make_float2(1e-6f, 1e-6f);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            a0 = __ffma2_rn(a0, b, c); a1 = __ffma2_rn(a1, b, c);
+            a2 = __ffma2_rn(a2, b, c); a3 = __ffma2_rn(a3, b, c);
+        }
+    }
+    const float s = (a0.x + a0.y + a1.x + a1.y) + (a2.x + a2.y + a3.x + a3.y);
+    if (s == 123456.f) out[blockIdx.x] = s;
+}
+
 }  // namespace
 }  // namespace tsg
+
+extern "C" int tsg_probe_fp32x2(int64_t blocks, int threads, int iters, float* out, void* stream,
+                                double* flops) {
+    if (blocks < 1 || threads < 32 || threads > 1024 || iters < 1 || !out)
+        return fail(TSG_ERR_ARGUMENT, "invalid probe shape");
+    fp32x2_probe_kernel<<<unsigned(blocks), threads, 0, static_cast<cudaStream_t>(stream)>>>(
+        out, iters, 1.0f);
+    TSG_CUDA(cudaGetLastError());
+    if (flops) *flops = double(blocks) * threads * double(iters) * 4.0 * 8.0 * 2.0;
+    return TSG_OK;
+}
 
 extern "C" int tsg_probe_fp32(int64_t blocks, int threads, int iters, float* out, void* stream,
                               double* flops) {

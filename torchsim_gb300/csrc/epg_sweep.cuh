@@ -3,11 +3,15 @@
 // sequence, optionally with forward-mode tangents beside it.
 //
 // Thread mapping: a voxel's configuration orders are spread over L warp lanes
-// (lanes_per_voxel), R consecutive orders per lane (orders_per_lane), so a
-// warp holds 32/L voxels. The gradient shift moves F+ one order up and F- one
-// order down; within a lane that is a register move, across lanes a warp
-// shuffle. The program (ops) is staged in shared memory and read as a
-// broadcast, since every voxel of a block follows the same train.
+// (lanes_per_voxel), R = 2*RP consecutive orders per lane (orders_per_lane),
+// so a warp holds floor(32/L) voxels. Each lane keeps its orders as RP pairs
+// in float2 registers and does the relaxation and the RF rotation of two
+// orders with one paired FP32 instruction (__ffma2_rn / __fmul2_rn): the
+// recursion is issue-bound, and pairing halves the arithmetic instructions.
+// The gradient shift moves F+ one order up and F- one order down: within a
+// lane that is a register move, across lanes a warp shuffle. The program
+// (ops) is staged in shared memory and read as a broadcast, since every
+// voxel of a block follows the same train.
 //
 // Semantics follow the reference's real-subspace kernels: relaxation with
 // recovery, the real 3x3 RF rotation in alpha = flip*B1, inversion Z *= -eff,
@@ -35,32 +39,44 @@ struct SystemLayout {
     static constexpr int NA = N > 0 ? N : 1;
 };
 
-// One gradient shift of a (F+, F-) pair spread over L lanes of R orders.
-template <int R, int L>
-__device__ __forceinline__ void shift_pair(float (&p)[R], float (&m)[R], int q, bool kill,
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// One gradient shift of a (F+, F-) pair of order-pair arrays spread over L
+// lanes: F- moves one order down (the top order takes what the next lane
+// held, or nothing at the voxel's top), then F+ one order up with
+// F+[0] = -F-[0] at the voxel's first lane.
+template <int RP, int L>
+__device__ __forceinline__ void shift_pair(float2 (&p)[RP], float2 (&m)[RP], int q, bool kill,
                                            int kill_r) {
     float in_p = 0.f, in_m = 0.f;
     if constexpr (L > 1) {
-        in_p = __shfl_up_sync(0xffffffffu, p[R - 1], 1);
-        in_m = __shfl_down_sync(0xffffffffu, m[0], 1);
+        in_p = __shfl_up_sync(0xffffffffu, p[RP - 1].y, 1);
+        in_m = __shfl_down_sync(0xffffffffu, m[0].x, 1);
     }
+    float top = 0.f;
+    if constexpr (L > 1) top = (q == L - 1) ? 0.f : in_m;
 #pragma unroll
-    for (int r = 0; r < R - 1; ++r) m[r] = m[r + 1];
+    for (int k = 0; k < RP; ++k) {
+        m[k].x = m[k].y;
+        m[k].y = (k + 1 < RP) ? m[k + 1].x : top;
+    }
+    float bottom = -m[0].x;
+    if constexpr (L > 1) bottom = (q == 0) ? -m[0].x : in_p;
 #pragma unroll
-    for (int r = R - 1; r > 0; --r) p[r] = p[r - 1];
-    if constexpr (L > 1) {
-        m[R - 1] = (q == L - 1) ? 0.f : in_m;
-        p[0] = (q == 0) ? -m[0] : in_p;
-    } else {
-        m[R - 1] = 0.f;
-        p[0] = -m[0];
+    for (int k = RP - 1; k >= 0; --k) {
+        p[k].y = p[k].x;
+        p[k].x = (k > 0) ? p[k - 1].y : bottom;
     }
     // Orders at and above `states` stay empty: the only way in is F+ moving
     // up from the top kept order, so that one slot is cleared after a shift.
     if (kill) {
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-            if (r == kill_r) p[r] = 0.f;
+        for (int k = 0; k < RP; ++k) {
+            if (2 * k == kill_r) p[k].x = 0.f;
+            if (2 * k + 1 == kill_r) p[k].y = 0.f;
+        }
     }
 }
 
@@ -75,10 +91,11 @@ __device__ __forceinline__ void put_sample(int layout, float* a, float* b, int64
     }
 }
 
-template <int R, int L, int TM, bool GEN, bool GN = false>
+template <int RP, int L, int TM, bool GEN, bool GN = false>
 __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
     using S = SystemLayout<TM, GEN>;
     constexpr int NT = S::N;
+    constexpr int R = 2 * RP;
     constexpr int VPW = 32 / L;
     __shared__ Op s_ops[kOpChunk];
     __shared__ float2 s_dir[GEN ? kOpChunk : 1];
@@ -86,9 +103,11 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int q = lane % L;
-    const int64_t atom = (int64_t(blockIdx.x) * (blockDim.x >> 5) + warp) * VPW + lane / L;
+    const int slot = lane / L;
+    const int64_t atom = (int64_t(blockIdx.x) * (blockDim.x >> 5) + warp) * VPW + slot;
     const int64_t train = blockIdx.y;
-    const bool active = atom < a.atoms;
+    // Lanes past the last whole voxel of the warp (32 % L of them) idle.
+    const bool active = slot < VPW && atom < a.atoms;
     const int64_t ac = active ? atom : 0;
 
     const float t1 = a.t1[ac];
@@ -112,16 +131,17 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
 
     const bool kill = L * R > a.states;
     const int kill_r = a.states - q * R;
+    const float2 neg1 = dup(-1.f);
 
-    float P[R], M[R], Z[R];
-    float dP[S::NA][R], dM[S::NA][R], dZ[S::NA][R];
+    float2 P[RP], M[RP], Z[RP];
+    float2 dP[S::NA][RP], dM[S::NA][RP], dZ[S::NA][RP];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        P[r] = M[r] = Z[r] = 0.f;
+    for (int k = 0; k < RP; ++k) {
+        P[k] = M[k] = Z[k] = dup(0.f);
 #pragma unroll
-        for (int j = 0; j < S::NA; ++j) dP[j][r] = dM[j][r] = dZ[j][r] = 0.f;
+        for (int j = 0; j < S::NA; ++j) dP[j][k] = dM[j][k] = dZ[j][k] = dup(0.f);
     }
-    if (q == 0) Z[0] = 1.f;
+    if (q == 0) Z[0].x = 1.f;
 
     float last_dt = __int_as_float(0x7fffffff);  // NaN: first relax computes
     float e1 = 1.f, e2 = 1.f, k1 = 0.f, k2 = 0.f;
@@ -160,15 +180,20 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
             if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
                 // State entering this op, for the adjoint's segments.
                 const int k = (base + i) / a.ckpt_every;
-                const int S = a.states;
-                float* dst = a.ckpt + (row * a.ckpt_count + k) * (3 * int64_t(S));
+                const int Sn = a.states;
+                float* dst = a.ckpt + (row * a.ckpt_count + k) * (3 * int64_t(Sn));
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const int o = q * R + r;
-                    if (o < S) {
-                        dst[o] = P[r];
-                        dst[S + o] = M[r];
-                        dst[2 * S + o] = Z[r];
+                for (int kk = 0; kk < RP; ++kk) {
+                    const int o = q * R + 2 * kk;
+                    if (o < Sn) {
+                        dst[o] = P[kk].x;
+                        dst[Sn + o] = M[kk].x;
+                        dst[2 * Sn + o] = Z[kk].x;
+                    }
+                    if (o + 1 < Sn) {
+                        dst[o + 1] = P[kk].y;
+                        dst[Sn + o + 1] = M[kk].y;
+                        dst[2 * Sn + o + 1] = Z[kk].y;
                     }
                 }
             }
@@ -195,138 +220,143 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
                     float si, co;
                     sincosf(alpha, &si, &co);
                     const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
-                    const float cpp = ch * e2, cpm = sh * e2, cpz = si * e1;
-                    const float czp = hs * e2, czz = co * e1;
+                    const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
+                    const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
+                    const float2 czp = dup(hs * e2), czz = dup(co * e1);
 #pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const float p = P[r], m = M[r], z = Z[r];
-                        P[r] = fmaf(cpp, p, fmaf(cpm, m, -cpz * z));
-                        M[r] = fmaf(cpm, p, fmaf(cpp, m, cpz * z));
-                        Z[r] = fmaf(czp, p - m, czz * z);
+                    for (int k = 0; k < RP; ++k) {
+                        const float2 p = P[k], m = M[k], z = Z[k];
+                        const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
+                        P[k] = fma2(cpp, p, fma2(cpm, m, nt));
+                        M[k] = fma2(cpm, p, fma2(cpp, m, t));
+                        Z[k] = fma2(czp, fma2(neg1, m, p), mul2(czz, z));
                     }
                     if (q == 0) {
                         const float rec = 1.f - e1;
-                        P[0] = fmaf(-si, rec, P[0]);
-                        M[0] = fmaf(si, rec, M[0]);
-                        Z[0] = fmaf(co, rec, Z[0]);
+                        P[0].x = fmaf(-si, rec, P[0].x);
+                        M[0].x = fmaf(si, rec, M[0].x);
+                        Z[0].x = fmaf(co, rec, Z[0].x);
                     }
                     goto after_rf;
                 }
             }
             if (relax) {
+                const float2 E1 = dup(e1), E2 = dup(e2);
                 float e1g = 0.f, e2g = 0.f;
                 if constexpr (GEN) {
                     e1g = e1 * (op.dt * g_t1 * w1 - r1 * ddt);
                     e2g = e2 * (op.dt * g_t2 * w2 - r2 * ddt);
                 }
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
+                for (int k = 0; k < RP; ++k) {
                     if constexpr (S::T1) {
-                        dP[S::I_T1][r] *= e2;
-                        dM[S::I_T1][r] *= e2;
-                        dZ[S::I_T1][r] = fmaf(dZ[S::I_T1][r], e1, Z[r] * k1);
+                        dP[S::I_T1][k] = mul2(dP[S::I_T1][k], E2);
+                        dM[S::I_T1][k] = mul2(dM[S::I_T1][k], E2);
+                        dZ[S::I_T1][k] = fma2(dZ[S::I_T1][k], E1, mul2(Z[k], dup(k1)));
                     }
                     if constexpr (S::T2) {
-                        dP[S::I_T2][r] = fmaf(dP[S::I_T2][r], e2, P[r] * k2);
-                        dM[S::I_T2][r] = fmaf(dM[S::I_T2][r], e2, M[r] * k2);
-                        dZ[S::I_T2][r] *= e1;
+                        dP[S::I_T2][k] = fma2(dP[S::I_T2][k], E2, mul2(P[k], dup(k2)));
+                        dM[S::I_T2][k] = fma2(dM[S::I_T2][k], E2, mul2(M[k], dup(k2)));
+                        dZ[S::I_T2][k] = mul2(dZ[S::I_T2][k], E1);
                     }
                     if constexpr (S::B1) {
-                        dP[S::I_B1][r] *= e2;
-                        dM[S::I_B1][r] *= e2;
-                        dZ[S::I_B1][r] *= e1;
+                        dP[S::I_B1][k] = mul2(dP[S::I_B1][k], E2);
+                        dM[S::I_B1][k] = mul2(dM[S::I_B1][k], E2);
+                        dZ[S::I_B1][k] = mul2(dZ[S::I_B1][k], E1);
                     }
                     if constexpr (S::INV) {
-                        dP[S::I_INV][r] *= e2;
-                        dM[S::I_INV][r] *= e2;
-                        dZ[S::I_INV][r] *= e1;
+                        dP[S::I_INV][k] = mul2(dP[S::I_INV][k], E2);
+                        dM[S::I_INV][k] = mul2(dM[S::I_INV][k], E2);
+                        dZ[S::I_INV][k] = mul2(dZ[S::I_INV][k], E1);
                     }
                     if constexpr (GEN) {
-                        dP[S::I_GEN][r] = fmaf(dP[S::I_GEN][r], e2, P[r] * e2g);
-                        dM[S::I_GEN][r] = fmaf(dM[S::I_GEN][r], e2, M[r] * e2g);
-                        dZ[S::I_GEN][r] = fmaf(dZ[S::I_GEN][r], e1, Z[r] * e1g);
+                        dP[S::I_GEN][k] = fma2(dP[S::I_GEN][k], E2, mul2(P[k], dup(e2g)));
+                        dM[S::I_GEN][k] = fma2(dM[S::I_GEN][k], E2, mul2(M[k], dup(e2g)));
+                        dZ[S::I_GEN][k] = fma2(dZ[S::I_GEN][k], E1, mul2(Z[k], dup(e1g)));
                     }
-                    P[r] *= e2;
-                    M[r] *= e2;
-                    Z[r] *= e1;
+                    P[k] = mul2(P[k], E2);
+                    M[k] = mul2(M[k], E2);
+                    Z[k] = mul2(Z[k], E1);
                 }
                 if (q == 0) {
-                    Z[0] += 1.f - e1;
-                    if constexpr (S::T1) dZ[S::I_T1][0] -= k1;
-                    if constexpr (GEN) dZ[S::I_GEN][0] -= e1g;
+                    Z[0].x += 1.f - e1;
+                    if constexpr (S::T1) dZ[S::I_T1][0].x -= k1;
+                    if constexpr (GEN) dZ[S::I_GEN][0].x -= e1g;
                 }
             }
             for (int s = 0; s < n1; ++s) {
-                shift_pair<R, L>(P, M, q, kill, kill_r);
+                shift_pair<RP, L>(P, M, q, kill, kill_r);
 #pragma unroll
-                for (int j = 0; j < NT; ++j) shift_pair<R, L>(dP[j], dM[j], q, kill, kill_r);
+                for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
             }
             if (rf == RF_ROTATE) {
                 const float alpha = op.flip * b1;
                 float si, co;
                 sincosf(alpha, &si, &co);
-                const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co);
-                const float hs = 0.5f * si, hc = 0.5f * co;
+                const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
+                const float2 hs = dup(0.5f * si), hc = dup(0.5f * co);
+                const float2 si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
                 float at_b1 = 0.f, at_gen = 0.f;
                 if constexpr (S::B1) at_b1 = op.flip;
                 if constexpr (GEN) at_gen = dfl * b1 + op.flip * g_b1;
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const float p = P[r], m = M[r], z = Z[r];
-                    const float w = p - m;
-                    float U = 0.f, V = 0.f;
-                    if constexpr (S::B1 || GEN) {
-                        U = fmaf(-hs, w, -co * z);
-                        V = fmaf(hc, w, -si * z);
-                    }
+                for (int k = 0; k < RP; ++k) {
+                    const float2 p = P[k], m = M[k], z = Z[k];
+                    const float2 t = mul2(si2, z), nt = mul2(nsi2, z);
+                    const float2 w = fma2(neg1, m, p);
+                    const float2 Pn = fma2(ch, p, fma2(sh, m, nt));
+                    const float2 Mn = fma2(sh, p, fma2(ch, m, t));
+                    const float2 Zn = fma2(hs, w, mul2(co2, z));
+                    // d/dalpha of the rotation: dP = -Zn, dM = Zn, dZ = V.
+                    float2 V = dup(0.f);
+                    if constexpr (S::B1 || GEN) V = fma2(hc, w, nt);
 #pragma unroll
                     for (int j = 0; j < NT; ++j) {
-                        const float dp = dP[j][r], dm = dM[j][r], dz = dZ[j][r];
-                        float np = fmaf(ch, dp, fmaf(sh, dm, -si * dz));
-                        float nm = fmaf(sh, dp, fmaf(ch, dm, si * dz));
-                        float nz = fmaf(hs, dp - dm, co * dz);
-                        float at = 0.f;
-                        if (S::B1 && j == S::I_B1) at = at_b1;
-                        if (GEN && j == S::I_GEN) at = at_gen;
+                        const float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
+                        const float2 dt = mul2(si2, dz), ndt = mul2(nsi2, dz);
+                        float2 np = fma2(ch, dp, fma2(sh, dm, ndt));
+                        float2 nm = fma2(sh, dp, fma2(ch, dm, dt));
+                        float2 nz = fma2(hs, fma2(neg1, dm, dp), mul2(co2, dz));
                         if ((S::B1 && j == S::I_B1) || (GEN && j == S::I_GEN)) {
-                            np = fmaf(at, U, np);
-                            nm = fmaf(-at, U, nm);
-                            nz = fmaf(at, V, nz);
+                            const float at = (S::B1 && j == S::I_B1) ? at_b1 : at_gen;
+                            np = fma2(dup(-at), Zn, np);
+                            nm = fma2(dup(at), Zn, nm);
+                            nz = fma2(dup(at), V, nz);
                         }
-                        dP[j][r] = np;
-                        dM[j][r] = nm;
-                        dZ[j][r] = nz;
+                        dP[j][k] = np;
+                        dM[j][k] = nm;
+                        dZ[j][k] = nz;
                     }
-                    P[r] = fmaf(ch, p, fmaf(sh, m, -si * z));
-                    M[r] = fmaf(sh, p, fmaf(ch, m, si * z));
-                    Z[r] = fmaf(hs, w, co * z);
+                    P[k] = Pn;
+                    M[k] = Mn;
+                    Z[k] = Zn;
                 }
             } else if (rf == RF_INVERT) {
-                const float f = -eff;
+                const float2 f = dup(-eff);
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
+                for (int k = 0; k < RP; ++k) {
 #pragma unroll
                     for (int j = 0; j < NT; ++j) {
-                        float nz = dZ[j][r] * f;
-                        if (S::INV && j == S::I_INV) nz = nz - Z[r];
-                        if (GEN && j == S::I_GEN) nz = fmaf(Z[r], -g_inv, nz);
-                        dZ[j][r] = nz;
+                        float2 nz = mul2(dZ[j][k], f);
+                        if (S::INV && j == S::I_INV) nz = fma2(neg1, Z[k], nz);
+                        if (GEN && j == S::I_GEN) nz = fma2(Z[k], dup(-g_inv), nz);
+                        dZ[j][k] = nz;
                     }
-                    Z[r] *= f;
+                    Z[k] = mul2(Z[k], f);
                 }
             }
         after_rf:
             for (int s = 0; s < op_shift2(code); ++s) {
-                shift_pair<R, L>(P, M, q, kill, kill_r);
+                shift_pair<RP, L>(P, M, q, kill, kill_r);
 #pragma unroll
-                for (int j = 0; j < NT; ++j) shift_pair<R, L>(dP[j], dM[j], q, kill, kill_r);
+                for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
             }
             if (code & OP_SPOIL1) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    P[r] = M[r] = 0.f;
+                for (int k = 0; k < RP; ++k) {
+                    P[k] = M[k] = dup(0.f);
 #pragma unroll
-                    for (int j = 0; j < NT; ++j) dP[j][r] = dM[j][r] = 0.f;
+                    for (int j = 0; j < NT; ++j) dP[j][k] = dM[j][k] = dup(0.f);
                 }
             }
             if constexpr (GN) {
@@ -335,11 +365,12 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
                     // dv: T1, T2 (tangents), M0 (F+[0]); J^T J and J^T r
                     // carry the sign of s twice or not at all.
                     const float2 y = yrow[op.record];
-                    const float v = m0 * P[0];
+                    const float p0 = P[0].x;
+                    const float v = m0 * p0;
                     const float res = v + y.x;  // -(r.real)
-                    const float j1 = m0 * dP[S::I_T1][0];
-                    const float j2 = m0 * dP[S::I_T2][0];
-                    const float j3 = P[0];
+                    const float j1 = m0 * dP[S::I_T1][0].x;
+                    const float j2 = m0 * dP[S::I_T2][0].x;
+                    const float j3 = p0;
                     cs[0] = fmaf(res, res, fmaf(y.y, y.y, cs[0]));
                     cs[1] = fmaf(j1, j1, cs[1]);
                     cs[2] = fmaf(j1, j2, cs[2]);
@@ -362,46 +393,47 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
             }
             if ((code & OP_RECORD) && q == 0 && active && !GN) {
                 const int64_t idx = row * a.outputs + op.record;
+                const float p0 = P[0].x;
                 if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
                     if (a.sig_a != nullptr || a.sig_b != nullptr)
-                        put_sample(a.layout, a.sig_a, a.sig_b, idx, m0 * P[0]);
+                        put_sample(a.layout, a.sig_a, a.sig_b, idx, m0 * p0);
                 }
                 const int64_t jrow = row * a.jac_cols;
                 if constexpr (S::T1)
                     if (a.col_t1 >= 0)
                         put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_t1) * a.outputs + op.record,
-                                   m0 * dP[S::I_T1][0]);
+                                   m0 * dP[S::I_T1][0].x);
                 if constexpr (S::T2)
                     if (a.col_t2 >= 0)
                         put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_t2) * a.outputs + op.record,
-                                   m0 * dP[S::I_T2][0]);
+                                   m0 * dP[S::I_T2][0].x);
                 if constexpr (S::B1)
                     if (a.col_b1 >= 0)
                         put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_b1) * a.outputs + op.record,
-                                   m0 * dP[S::I_B1][0]);
+                                   m0 * dP[S::I_B1][0].x);
                 if constexpr (S::INV)
                     if (a.col_inv >= 0)
                         put_sample(a.layout, a.jac_a, a.jac_b,
-                                   (jrow + a.col_inv) * a.outputs + op.record, m0 * dP[S::I_INV][0]);
+                                   (jrow + a.col_inv) * a.outputs + op.record, m0 * dP[S::I_INV][0].x);
                 if constexpr (GEN)
                     if (a.col_gen >= 0)
                         put_sample(a.layout, a.jac_a, a.jac_b,
                                    (jrow + a.col_gen) * a.outputs + op.record,
-                                   fmaf(g_m0, P[0], m0 * dP[S::I_GEN][0]));
+                                   fmaf(g_m0, p0, m0 * dP[S::I_GEN][0].x));
                 if (a.col_m0 >= 0)
-                    put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_m0) * a.outputs + op.record, P[0]);
+                    put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_m0) * a.outputs + op.record, p0);
             }
             for (int s = 0; s < op_shift3(code); ++s) {
-                shift_pair<R, L>(P, M, q, kill, kill_r);
+                shift_pair<RP, L>(P, M, q, kill, kill_r);
 #pragma unroll
-                for (int j = 0; j < NT; ++j) shift_pair<R, L>(dP[j], dM[j], q, kill, kill_r);
+                for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
             }
             if (code & OP_SPOIL2) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    P[r] = M[r] = 0.f;
+                for (int k = 0; k < RP; ++k) {
+                    P[k] = M[k] = dup(0.f);
 #pragma unroll
-                    for (int j = 0; j < NT; ++j) dP[j][r] = dM[j][r] = 0.f;
+                    for (int j = 0; j < NT; ++j) dP[j][k] = dM[j][k] = dup(0.f);
                 }
             }
         }
@@ -415,13 +447,14 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
     }
 }
 
-template <int R, int L, int TM, bool GEN, bool GN = false>
+template <int RP, int L, int TM, bool GEN, bool GN = false>
 void launch_sweep(const SweepArgs& a, dim3 grid, dim3 block, size_t smem, cudaStream_t stream) {
-    epg_sweep_kernel<R, L, TM, GEN, GN><<<grid, block, smem, stream>>>(a);
+    epg_sweep_kernel<RP, L, TM, GEN, GN><<<grid, block, smem, stream>>>(a);
 }
 
 }  // namespace tsg
 
+// Table entries take orders per lane R (even): the kernel keeps R/2 pairs.
 #define TSG_SWEEP_ENTRY(MODE, R, L, TM, GEN) \
-    {MODE, R, L, &::tsg::launch_sweep<R, L, TM, GEN, false>}
-#define TSG_GN_ENTRY(R, L) {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<R, L, 3, false, true>}
+    {MODE, R, L, &::tsg::launch_sweep<(R) / 2, L, TM, GEN, false>}
+#define TSG_GN_ENTRY(R, L) {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<(R) / 2, L, 3, false, true>}

@@ -6,10 +6,12 @@ namespace tsg {
 const SweepEntry kSweepForward[] = {
     TSG_SWEEP_ENTRY(MODE_FORWARD, 10, 1, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 20, 1, 0, false),
-    TSG_SWEEP_ENTRY(MODE_FORWARD, 5, 2, 0, false),
-    TSG_SWEEP_ENTRY(MODE_FORWARD, 10, 2, 0, false),
+    TSG_SWEEP_ENTRY(MODE_FORWARD, 2, 5, 0, false),
+    TSG_SWEEP_ENTRY(MODE_FORWARD, 6, 2, 0, false),
+    TSG_SWEEP_ENTRY(MODE_FORWARD, 4, 5, 0, false),
+    TSG_SWEEP_ENTRY(MODE_FORWARD, 2, 10, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 4, 4, 0, false),
-    TSG_SWEEP_ENTRY(MODE_FORWARD, 5, 4, 0, false),
+    TSG_SWEEP_ENTRY(MODE_FORWARD, 6, 4, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 8, 4, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 4, 8, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 8, 8, 0, false),

@@ -5,13 +5,15 @@
 namespace tsg {
 const SweepEntry kSweepGeneral[] = {
     TSG_SWEEP_ENTRY(MODE_GENERAL, 10, 1, 0, true),
-    TSG_SWEEP_ENTRY(MODE_GENERAL, 5, 2, 0, true),
+    TSG_SWEEP_ENTRY(MODE_GENERAL, 2, 5, 0, true),
+    TSG_SWEEP_ENTRY(MODE_GENERAL, 6, 2, 0, true),
+    TSG_SWEEP_ENTRY(MODE_GENERAL, 4, 5, 0, true),
+    TSG_SWEEP_ENTRY(MODE_GENERAL, 2, 10, 0, true),
     TSG_SWEEP_ENTRY(MODE_GENERAL, 4, 4, 0, true),
-    TSG_SWEEP_ENTRY(MODE_GENERAL, 5, 4, 0, true),
+    TSG_SWEEP_ENTRY(MODE_GENERAL, 6, 4, 0, true),
     TSG_SWEEP_ENTRY(MODE_GENERAL, 8, 4, 0, true),
     TSG_SWEEP_ENTRY(MODE_GENERAL, 4, 8, 0, true),
     TSG_SWEEP_ENTRY(MODE_GENERAL, 4, 16, 0, true),
-    TSG_SWEEP_ENTRY(MODE_GENERAL, 8, 16, 0, true),
     TSG_SWEEP_ENTRY(MODE_GENERAL, 4, 32, 0, true),
 };
 const int kSweepGeneralCount = sizeof(kSweepGeneral) / sizeof(kSweepGeneral[0]);

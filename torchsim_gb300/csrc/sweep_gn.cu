@@ -9,9 +9,7 @@
 
 namespace tsg {
 const SweepEntry kSweepGN[] = {
-    TSG_GN_ENTRY(10, 1), TSG_GN_ENTRY(5, 2), TSG_GN_ENTRY(10, 2), TSG_GN_ENTRY(4, 4),
-    TSG_GN_ENTRY(5, 4), TSG_GN_ENTRY(8, 4), TSG_GN_ENTRY(4, 8), TSG_GN_ENTRY(8, 8),
-    TSG_GN_ENTRY(4, 16), TSG_GN_ENTRY(4, 32),
+    TSG_GN_ENTRY(10, 1), TSG_GN_ENTRY(2, 5), TSG_GN_ENTRY(6, 2), TSG_GN_ENTRY(4, 5), TSG_GN_ENTRY(2, 10), TSG_GN_ENTRY(4, 4), TSG_GN_ENTRY(8, 4), TSG_GN_ENTRY(4, 8), TSG_GN_ENTRY(8, 8), TSG_GN_ENTRY(4, 16), TSG_GN_ENTRY(4, 32),
 };
 const int kSweepGNCount = sizeof(kSweepGN) / sizeof(kSweepGN[0]);
 }  // namespace tsg

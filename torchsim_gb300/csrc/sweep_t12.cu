@@ -4,15 +4,16 @@
 namespace tsg {
 const SweepEntry kSweepT12[] = {
     TSG_SWEEP_ENTRY(MODE_T12, 10, 1, 3, false),
-    TSG_SWEEP_ENTRY(MODE_T12, 5, 2, 3, false),
-    TSG_SWEEP_ENTRY(MODE_T12, 10, 2, 3, false),
+    TSG_SWEEP_ENTRY(MODE_T12, 2, 5, 3, false),
+    TSG_SWEEP_ENTRY(MODE_T12, 6, 2, 3, false),
+    TSG_SWEEP_ENTRY(MODE_T12, 4, 5, 3, false),
+    TSG_SWEEP_ENTRY(MODE_T12, 2, 10, 3, false),
     TSG_SWEEP_ENTRY(MODE_T12, 4, 4, 3, false),
-    TSG_SWEEP_ENTRY(MODE_T12, 5, 4, 3, false),
+    TSG_SWEEP_ENTRY(MODE_T12, 6, 4, 3, false),
     TSG_SWEEP_ENTRY(MODE_T12, 8, 4, 3, false),
     TSG_SWEEP_ENTRY(MODE_T12, 4, 8, 3, false),
     TSG_SWEEP_ENTRY(MODE_T12, 8, 8, 3, false),
     TSG_SWEEP_ENTRY(MODE_T12, 4, 16, 3, false),
-    TSG_SWEEP_ENTRY(MODE_T12, 8, 16, 3, false),
     TSG_SWEEP_ENTRY(MODE_T12, 4, 32, 3, false),
 };
 const int kSweepT12Count = sizeof(kSweepT12) / sizeof(kSweepT12[0]);

@@ -3,11 +3,12 @@
 
 namespace tsg {
 const SweepEntry kSweepT12B[] = {
-    TSG_SWEEP_ENTRY(MODE_T12B, 5, 2, 7, false),
-    TSG_SWEEP_ENTRY(MODE_T12B, 3, 4, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 2, 5, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 6, 2, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 4, 5, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 2, 10, 7, false),
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 4, 7, false),
-    TSG_SWEEP_ENTRY(MODE_T12B, 5, 4, 7, false),
-    TSG_SWEEP_ENTRY(MODE_T12B, 3, 8, 7, false),
+    TSG_SWEEP_ENTRY(MODE_T12B, 6, 4, 7, false),
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 8, 7, false),
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 16, 7, false),
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 32, 7, false),

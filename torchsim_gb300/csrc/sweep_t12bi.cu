@@ -3,7 +3,9 @@
 
 namespace tsg {
 const SweepEntry kSweepT12BI[] = {
-    TSG_SWEEP_ENTRY(MODE_T12BI, 5, 2, 15, false),
+    TSG_SWEEP_ENTRY(MODE_T12BI, 2, 5, 15, false),
+    TSG_SWEEP_ENTRY(MODE_T12BI, 4, 5, 15, false),
+    TSG_SWEEP_ENTRY(MODE_T12BI, 2, 10, 15, false),
     TSG_SWEEP_ENTRY(MODE_T12BI, 4, 4, 15, false),
     TSG_SWEEP_ENTRY(MODE_T12BI, 4, 8, 15, false),
     TSG_SWEEP_ENTRY(MODE_T12BI, 4, 16, 15, false),

@@ -169,12 +169,12 @@ def forward_tangents(program: Program, tissue: TissueMaps, states: int, names: S
 # (lanes per voxel, orders per lane) instantiated per kernel family, as in the
 # sweep tables of csrc/sweep_*.cu.
 FAMILY_SHAPES = {
-    0: [(1, 10), (1, 20), (2, 5), (2, 10), (4, 4), (4, 5), (4, 8), (8, 4), (8, 8), (16, 4),
-        (16, 8), (32, 4), (32, 8)],
-    3: [(1, 10), (2, 5), (2, 10), (4, 4), (4, 5), (4, 8), (8, 4), (8, 8), (16, 4), (16, 8),
+    0: [(1, 10), (1, 20), (5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (4, 8), (8, 4), (8, 8),
+        (16, 4), (16, 8), (32, 4), (32, 8)],
+    3: [(1, 10), (5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (4, 8), (8, 4), (8, 8), (16, 4),
         (32, 4)],
-    7: [(2, 5), (4, 3), (4, 4), (4, 5), (8, 3), (8, 4), (16, 4), (32, 4)],
-    15: [(2, 5), (4, 4), (8, 4), (16, 4), (32, 4)],
+    7: [(5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (8, 4), (16, 4), (32, 4)],
+    15: [(5, 2), (5, 4), (10, 2), (4, 4), (8, 4), (16, 4), (32, 4)],
 }
 
 
