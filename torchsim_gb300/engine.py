@@ -196,7 +196,7 @@ def tuned_shape(program: Program, tissue: TissueMaps, states: int, names: Sequen
     n = min(sample, tissue.voxels)
     sub = TissueMaps(*[None if t is None else t[:n] for t in
                        (tissue.t1, tissue.t2, tissue.m0, tissue.b1, tissue.inv)])
-    key = autotune.workload_key("sweep", family=family, states=states, ops=program.ops,
+    key = autotune.workload_key("sweep", kernel_family=family, states=states, ops=program.ops,
                                 outputs=program.outputs, sample=n)
     sig = torch.empty((program.trains * n, program.outputs), dtype=torch.complex64,
                       device=tissue.t1.device)
