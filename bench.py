@@ -205,7 +205,8 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         t_tune = time.perf_counter()
         launch = engine.tuned_shape(program, tissue, STATES, names, use_cache=False)
         tune_info = {"shape": {"lanes_per_voxel": launch[0], "orders_per_lane": launch[1],
-                               "warps_per_block": launch[2]},
+                               "warps_per_block": launch[2],
+                               "min_blocks_per_sm": launch[3] if len(launch) > 3 else 0},
                      "tuning_s": time.perf_counter() - t_tune, "sample_atoms": min(32768, atoms)}
 
     def step():
@@ -725,7 +726,8 @@ def main() -> None:
     ap.add_argument("--batch-sequences", type=int, default=512)
     ap.add_argument("--atoms", type=int, default=ATOMS,
                     help="first N grid atoms (a smaller case for profiling; default all)")
-    ap.add_argument("--launch", type=int, nargs=3, metavar=("LANES", "ORDERS", "WARPS"))
+    ap.add_argument("--launch", type=int, nargs="+", metavar="N",
+                    help="lanes per voxel, orders per lane, warps per block[, min blocks per SM]")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

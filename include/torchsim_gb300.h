@@ -96,15 +96,17 @@ typedef struct {
     float* duration_s;
 } tsg_gradients;
 
-/* Launch shape. Zero fields are chosen by the built-in heuristic (or the
- * tuned table installed with tsg_tune_set). lanes_per_voxel spreads the
- * F+/F-/Z orders of one voxel over that many warp lanes; orders_per_lane is
- * how many orders each lane keeps in registers; warps_per_block sets the
- * voxels per CTA. */
+/* Launch shape. Zero fields are chosen by the built-in heuristic.
+ * lanes_per_voxel spreads the F+/F-/Z orders of one voxel over that many warp
+ * lanes; orders_per_lane is how many orders each lane keeps in registers
+ * (even for the sweeps); warps_per_block sets the voxels per CTA;
+ * min_blocks_per_sm selects a register-budget variant compiled to keep that
+ * many 128-thread blocks resident per SM (0: the default budget). */
 typedef struct {
     int lanes_per_voxel;
     int orders_per_lane;
     int warps_per_block;
+    int min_blocks_per_sm;
 } tsg_launch;
 
 typedef struct tsg_program tsg_program;

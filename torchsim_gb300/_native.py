@@ -76,7 +76,7 @@ class GNConfig(ctypes.Structure):
 
 class Launch(ctypes.Structure):
     _fields_ = [("lanes_per_voxel", ctypes.c_int), ("orders_per_lane", ctypes.c_int),
-                ("warps_per_block", ctypes.c_int)]
+                ("warps_per_block", ctypes.c_int), ("min_blocks_per_sm", ctypes.c_int)]
 
 
 _i64 = ctypes.c_int64
@@ -168,8 +168,10 @@ def call(name: str, *args) -> None:
 
 
 def launch_shape(shape) -> ctypes.POINTER(Launch) | None:
-    """A Launch struct from a (lanes, orders, warps) tuple, or None for auto."""
+    """A Launch struct from a (lanes, orders, warps[, min_blocks]) tuple, or
+    None for the built-in choice."""
     if shape is None:
         return None
-    lanes, orders, warps = shape
-    return ctypes.pointer(Launch(int(lanes), int(orders), int(warps)))
+    lanes, orders, warps = shape[:3]
+    min_blocks = shape[3] if len(shape) > 3 else 0
+    return ctypes.pointer(Launch(int(lanes), int(orders), int(warps), int(min_blocks)))

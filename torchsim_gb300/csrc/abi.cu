@@ -50,8 +50,11 @@ const SweepEntry* choose(int mode, int states, int64_t work_items, const tsg_lau
         for (int i = 0; i < t.count; ++i)
             if (t.entries[i].lanes_per_voxel == want->lanes_per_voxel &&
                 t.entries[i].orders_per_lane == want->orders_per_lane &&
-                want->lanes_per_voxel * want->orders_per_lane >= states)
+                t.entries[i].min_blocks == want->min_blocks_per_sm &&
+                want->lanes_per_voxel * want->orders_per_lane >= states) {
+                if (t.entries[i].min_blocks > 0 && *warps > 4) return nullptr;
                 return &t.entries[i];
+            }
         return nullptr;
     }
     const int64_t target_lanes = int64_t(sm_count()) * 1024;
@@ -61,6 +64,7 @@ const SweepEntry* choose(int mode, int states, int64_t work_items, const tsg_lau
         const SweepEntry& e = t.entries[i];
         const int padded = e.lanes_per_voxel * e.orders_per_lane;
         if (padded < states) continue;
+        if (e.min_blocks > 0) continue;  // register-budget variants: by request only
         if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
         const int vpw = 32 / e.lanes_per_voxel;
         const double waste = double(padded) / states * 32.0 / double(vpw * e.lanes_per_voxel);

@@ -91,8 +91,8 @@ __device__ __forceinline__ void put_sample(int layout, float* a, float* b, int64
     }
 }
 
-template <int RP, int L, int TM, bool GEN, bool GN = false>
-__global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
+template <int RP, int L, int TM, bool GEN, bool GN = false, int MINB = 1>
+__global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(const SweepArgs a) {
     using S = SystemLayout<TM, GEN>;
     constexpr int NT = S::N;
     constexpr int R = 2 * RP;
@@ -447,14 +447,18 @@ __global__ void __launch_bounds__(256) epg_sweep_kernel(const SweepArgs a) {
     }
 }
 
-template <int RP, int L, int TM, bool GEN, bool GN = false>
+template <int RP, int L, int TM, bool GEN, bool GN = false, int MINB = 1>
 void launch_sweep(const SweepArgs& a, dim3 grid, dim3 block, size_t smem, cudaStream_t stream) {
-    epg_sweep_kernel<RP, L, TM, GEN, GN><<<grid, block, smem, stream>>>(a);
+    epg_sweep_kernel<RP, L, TM, GEN, GN, MINB><<<grid, block, smem, stream>>>(a);
 }
 
 }  // namespace tsg
 
 // Table entries take orders per lane R (even): the kernel keeps R/2 pairs.
 #define TSG_SWEEP_ENTRY(MODE, R, L, TM, GEN) \
-    {MODE, R, L, &::tsg::launch_sweep<(R) / 2, L, TM, GEN, false>}
-#define TSG_GN_ENTRY(R, L) {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<(R) / 2, L, 3, false, true>}
+    {MODE, R, L, &::tsg::launch_sweep<(R) / 2, L, TM, GEN, false>, 0}
+// A register-budget variant: at most 128 threads per block and at least
+// MINB blocks resident per SM, i.e. 65536 / (128 * MINB) registers a thread.
+#define TSG_SWEEP_ENTRY_MINB(MODE, R, L, TM, GEN, MINB) \
+    {MODE, R, L, &::tsg::launch_sweep<(R) / 2, L, TM, GEN, false, MINB>, MINB}
+#define TSG_GN_ENTRY(R, L) {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<(R) / 2, L, 3, false, true>, 0}

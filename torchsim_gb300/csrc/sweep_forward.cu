@@ -19,6 +19,7 @@ const SweepEntry kSweepForward[] = {
     TSG_SWEEP_ENTRY(MODE_FORWARD, 8, 16, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 4, 32, 0, false),
     TSG_SWEEP_ENTRY(MODE_FORWARD, 8, 32, 0, false),
+    TSG_SWEEP_ENTRY(MODE_FORWARD, 10, 2, 0, false),
 };
 const int kSweepForwardCount = sizeof(kSweepForward) / sizeof(kSweepForward[0]);
 }  // namespace tsg

@@ -12,6 +12,10 @@ const SweepEntry kSweepT12B[] = {
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 8, 7, false),
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 16, 7, false),
     TSG_SWEEP_ENTRY(MODE_T12B, 4, 32, 7, false),
+    TSG_SWEEP_ENTRY_MINB(MODE_T12B, 4, 5, 7, false, 5),
+    TSG_SWEEP_ENTRY_MINB(MODE_T12B, 4, 5, 7, false, 6),
+    TSG_SWEEP_ENTRY_MINB(MODE_T12B, 2, 10, 7, false, 8),
+    TSG_SWEEP_ENTRY_MINB(MODE_T12B, 4, 4, 7, false, 6),
 };
 const int kSweepT12BCount = sizeof(kSweepT12B) / sizeof(kSweepT12B[0]);
 }  // namespace tsg

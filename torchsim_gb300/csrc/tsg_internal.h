@@ -147,6 +147,7 @@ struct SweepEntry {
     int orders_per_lane;  // R
     int lanes_per_voxel;  // L
     SweepLaunch launch;
+    int min_blocks;       // register-budget variant (0: default budget)
 };
 
 // Tables defined by the per-mode translation units.

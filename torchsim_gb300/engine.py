@@ -170,12 +170,16 @@ def forward_tangents(program: Program, tissue: TissueMaps, states: int, names: S
 # sweep tables of csrc/sweep_*.cu.
 FAMILY_SHAPES = {
     0: [(1, 10), (1, 20), (5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (4, 8), (8, 4), (8, 8),
-        (16, 4), (16, 8), (32, 4), (32, 8)],
+        (16, 4), (16, 8), (32, 4), (32, 8), (2, 10)],
     3: [(1, 10), (5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (4, 8), (8, 4), (8, 8), (16, 4),
         (32, 4)],
     7: [(5, 2), (2, 6), (5, 4), (10, 2), (4, 4), (4, 6), (8, 4), (16, 4), (32, 4)],
     15: [(5, 2), (5, 4), (10, 2), (4, 4), (8, 4), (16, 4), (32, 4)],
 }
+
+
+# (lanes, orders, min blocks per SM) register-budget variants per family.
+REGISTER_VARIANTS = {7: [(5, 4, 5), (5, 4, 6), (10, 2, 8), (4, 4, 6)]}
 
 
 def mode_of(names: Sequence[str]) -> int:
@@ -210,6 +214,8 @@ def tuned_shape(program: Program, tissue: TissueMaps, states: int, names: Sequen
             forward(program, sub, states, out=sig, launch=shape)
 
     cands = autotune.sweep_shapes(states, FAMILY_SHAPES[family])
+    cands += [(lanes, orders, 4, mb) for lanes, orders, mb in REGISTER_VARIANTS.get(family, [])
+              if lanes * orders >= states]
     best, _ = autotune.tune(key, cands, run, use_cache=use_cache)
     return tuple(best)
 
