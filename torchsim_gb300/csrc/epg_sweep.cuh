@@ -165,6 +165,15 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     const Op* ops = a.ops + train * a.n_ops;
     const float2* dirs = GEN ? a.op_dir + train * a.n_ops : nullptr;
     const int64_t row = train * a.atoms + atom;
+    // Output row bases, once: a record then only adds its sample index.
+    // Column offsets (col * outputs) are the same for every thread.
+    const int64_t sig_base = row * a.outputs;
+    const int64_t jbase = row * a.jac_cols * a.outputs;
+    // Each pulse's sin/cos is the same for all L lanes of a voxel: lane q
+    // computes it for one of the next L ops and the voxel's lanes exchange
+    // them with a shuffle, so each lane evaluates one sincosf per L pulses.
+    float my_si = 0.f, my_co = 1.f;
+    const int first_lane = lane - q;
 
     for (int base = 0; base < a.n_ops; base += kOpChunk) {
         const int count = min(kOpChunk, a.n_ops - base);
@@ -177,6 +186,19 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
         for (int i = 0; i < count; ++i) {
             const Op op = s_ops[i];
             const uint32_t code = op.code;
+            const int g = i % L;
+            if constexpr (L > 1) {
+                if (g == 0) {
+                    const int j = i + q;
+                    float sj = 0.f, cj = 1.f;
+                    if (j < count) {
+                        const Op oj = s_ops[j];
+                        if (op_rf(oj.code) == RF_ROTATE) sincosf(oj.flip * b1, &sj, &cj);
+                    }
+                    my_si = sj;
+                    my_co = cj;
+                }
+            }
             if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
                 // State entering this op, for the adjoint's segments.
                 const int k = (base + i) / a.ckpt_every;
@@ -216,9 +238,13 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 if (relax && rf == RF_ROTATE && n1 == 0) {
                     // Relaxation folded into the rotation: one 3x3 per order
                     // with the recovery of order 0 added after.
-                    const float alpha = op.flip * b1;
                     float si, co;
-                    sincosf(alpha, &si, &co);
+                    if constexpr (L > 1) {
+                        si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
+                        co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
+                    } else {
+                        sincosf(op.flip * b1, &si, &co);
+                    }
                     const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
                     const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
                     const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
@@ -290,9 +316,13 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
             }
             if (rf == RF_ROTATE) {
-                const float alpha = op.flip * b1;
                 float si, co;
-                sincosf(alpha, &si, &co);
+                if constexpr (L > 1) {
+                    si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
+                    co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
+                } else {
+                    sincosf(op.flip * b1, &si, &co);
+                }
                 const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
                 const float2 hs = dup(0.5f * si), hc = dup(0.5f * co);
                 const float2 si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
@@ -392,36 +422,30 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 }
             }
             if ((code & OP_RECORD) && q == 0 && active && !GN) {
-                const int64_t idx = row * a.outputs + op.record;
+                const int rec = op.record;
                 const float p0 = P[0].x;
                 if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
                     if (a.sig_a != nullptr || a.sig_b != nullptr)
-                        put_sample(a.layout, a.sig_a, a.sig_b, idx, m0 * p0);
+                        put_sample(a.layout, a.sig_a, a.sig_b, sig_base + rec, m0 * p0);
                 }
-                const int64_t jrow = row * a.jac_cols;
                 if constexpr (S::T1)
                     if (a.col_t1 >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_t1) * a.outputs + op.record,
-                                   m0 * dP[S::I_T1][0].x);
+                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_t1 * a.outputs + rec, m0 * dP[S::I_T1][0].x);
                 if constexpr (S::T2)
                     if (a.col_t2 >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_t2) * a.outputs + op.record,
-                                   m0 * dP[S::I_T2][0].x);
+                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_t2 * a.outputs + rec, m0 * dP[S::I_T2][0].x);
                 if constexpr (S::B1)
                     if (a.col_b1 >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_b1) * a.outputs + op.record,
-                                   m0 * dP[S::I_B1][0].x);
+                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_b1 * a.outputs + rec, m0 * dP[S::I_B1][0].x);
                 if constexpr (S::INV)
                     if (a.col_inv >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b,
-                                   (jrow + a.col_inv) * a.outputs + op.record, m0 * dP[S::I_INV][0].x);
+                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_inv * a.outputs + rec,
+                                   m0 * dP[S::I_INV][0].x);
                 if constexpr (GEN)
                     if (a.col_gen >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b,
-                                   (jrow + a.col_gen) * a.outputs + op.record,
+                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_gen * a.outputs + rec,
                                    fmaf(g_m0, p0, m0 * dP[S::I_GEN][0].x));
-                if (a.col_m0 >= 0)
-                    put_sample(a.layout, a.jac_a, a.jac_b, (jrow + a.col_m0) * a.outputs + op.record, p0);
+                if (a.col_m0 >= 0) put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_m0 * a.outputs + rec, p0);
             }
             for (int s = 0; s < op_shift3(code); ++s) {
                 shift_pair<RP, L>(P, M, q, kill, kill_r);
