@@ -112,7 +112,8 @@ def test_segment_length_does_not_change_gradients(cuda, ops_per_checkpoint):
     assert max_rel(dur[nz], ref["duration_s"][nz]) <= GRAD_TOL
 
 
-@pytest.mark.parametrize("shape", [(1, 20, 4), (2, 10, 4), (4, 5, 2), (4, 8, 4), (8, 4, 8),
+@pytest.mark.parametrize("shape", [(1, 20, 4), (1, 10, 2), (5, 2, 4), (2, 6, 4), (5, 4, 2),
+                                   (10, 2, 4), (4, 4, 8), (4, 6, 4), (8, 4, 4), (8, 8, 2),
                                    (16, 4, 4), (32, 4, 4)])
 def test_adjoint_launch_shapes(cuda, shape):
     from torchsim_gb300 import engine

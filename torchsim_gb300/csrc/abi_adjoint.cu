@@ -67,7 +67,9 @@ int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_
         if (padded < states) continue;
         if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
         if (want && want->orders_per_lane > 0 && e.orders_per_lane != want->orders_per_lane) continue;
-        const double waste = double(padded) / double(states);
+        const int vpw = 32 / e.lanes_per_voxel;
+        const double waste = double(padded) / double(states) * 32.0 /
+                             double(vpw * e.lanes_per_voxel);
         const double lanes = double(atoms * prog->host.trains) * e.lanes_per_voxel;
         const double fill = std::min(1.0, lanes / target);
         const double score = waste / std::max(fill, 1e-3) *
@@ -80,14 +82,17 @@ int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_
     if (!best) return fail(TSG_ERR_UNSUPPORTED, "no adjoint kernel for this state count / launch shape");
     plan->entry = best;
     const int threads = 32 * plan->warps;
-    const size_t per_op = size_t(3) * best->orders_per_lane * threads * sizeof(float);
+    const int vpb = plan->warps * (32 / best->lanes_per_voxel);
+    // Per op of a segment: the op, its transcendentals per voxel, and the
+    // pre-RF state (3 planes x orders x threads).
+    const size_t per_op = sizeof(Op) + sizeof(float4) * size_t(vpb) +
+                          size_t(3) * best->orders_per_lane * threads * sizeof(float);
     int c = ops_per_checkpoint;
     if (c <= 0) c = int(std::max<size_t>(1, std::min<size_t>(64, kStageBudget / per_op)));
     if (size_t(c) * per_op > 200 * 1024) return fail(TSG_ERR_CAPACITY, "segment does not fit in shared memory");
     plan->ops_per_checkpoint = c;
     const int64_t ops = prog->host.ops;
     plan->checkpoint_count = int((ops + c - 1) / c);
-    const int64_t vpb = int64_t(plan->warps) * (32 / best->lanes_per_voxel);
     plan->blocks = (atoms + vpb - 1) / vpb;
     plan->warps_per_train = plan->blocks * plan->warps;
     plan->checkpoint_bytes = prog->host.trains * atoms * int64_t(plan->checkpoint_count) * 3 * states *
