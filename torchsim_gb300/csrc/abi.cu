@@ -57,6 +57,31 @@ const SweepEntry* choose(int mode, int states, int64_t work_items, const tsg_lau
             }
         return nullptr;
     }
+    // Measured preferences on GB300 (launch-shape sweeps of each family):
+    // one voxel per lane wherever its orders fit the registers, five lanes of
+    // four orders for the four-system dictionary sweep at 20 states (with the
+    // register-budget variant once the grid is large).
+    struct Preferred {
+        int mode, max_states, lanes, orders, min_blocks;
+        int64_t min_items;
+    };
+    static const Preferred kPreferred[] = {
+        {MODE_FORWARD, 10, 1, 10, 0, 0}, {MODE_FORWARD, 20, 1, 20, 0, 0},
+        {MODE_T12, 10, 1, 10, 0, 0},     {MODE_GENERAL, 10, 1, 10, 0, 0},
+        {MODE_GN, 10, 1, 10, 0, 0},      {MODE_T12B, 20, 5, 4, 5, 65536},
+        {MODE_T12B, 20, 5, 4, 0, 0},     {MODE_T12BI, 10, 5, 2, 0, 0},
+        {MODE_T12BI, 20, 5, 4, 0, 0},
+    };
+    if (!(want && (want->lanes_per_voxel > 0 || want->orders_per_lane > 0))) {
+        for (const Preferred& p : kPreferred) {
+            if (p.mode != mode || states > p.max_states || work_items < p.min_items) continue;
+            if (p.min_blocks > 0 && *warps > 4) continue;
+            for (int i = 0; i < t.count; ++i)
+                if (t.entries[i].lanes_per_voxel == p.lanes && t.entries[i].orders_per_lane == p.orders &&
+                    t.entries[i].min_blocks == p.min_blocks)
+                    return &t.entries[i];
+        }
+    }
     const int64_t target_lanes = int64_t(sm_count()) * 1024;
     const SweepEntry* best = nullptr;
     double best_score = 1e300;

@@ -27,7 +27,7 @@ __global__ void reduce_tissue_gradients(const float* partial, int64_t atoms, int
 namespace {
 
 // Shared memory a block may give the segment's pre-RF states.
-constexpr size_t kStageBudget = 64 * 1024;
+constexpr size_t kStageBudget = 100 * 1024;
 
 struct AdjointPlan {
     const AdjointEntry* entry = nullptr;
@@ -56,7 +56,10 @@ int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_
     if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
     if (atoms < 0 || states < 1) return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
     if (states > 256) return fail(TSG_ERR_CAPACITY, "more than 256 states");
-    plan->warps = (want && want->warps_per_block > 0) ? want->warps_per_block : 4;
+    const bool shaped = want && (want->lanes_per_voxel > 0 || want->orders_per_lane > 0);
+    // One voxel per lane up to 20 states (measured best), two warps a block.
+    const bool one_lane = !shaped && states <= 20;
+    plan->warps = (want && want->warps_per_block > 0) ? want->warps_per_block : (one_lane ? 2 : 4);
     if (plan->warps < 1 || plan->warps > 8) return fail(TSG_ERR_ARGUMENT, "warps_per_block must be 1..8");
     const AdjointEntry* best = nullptr;
     double best_score = 1e300;
@@ -67,6 +70,7 @@ int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_
         if (padded < states) continue;
         if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
         if (want && want->orders_per_lane > 0 && e.orders_per_lane != want->orders_per_lane) continue;
+        if (one_lane && e.lanes_per_voxel != 1) continue;
         const int vpw = 32 / e.lanes_per_voxel;
         const double waste = double(padded) / double(states) * 32.0 /
                              double(vpw * e.lanes_per_voxel);

@@ -78,7 +78,7 @@ def config_of(bounds: Mapping[str, Any], tau: float, gradient_tolerance: float,
 def fixed_shape(states: int) -> tuple[int, int, int]:
     """A (lanes per voxel, orders per lane, warps per CTA) of the GN sweep
     table that covers ``states``, chosen from the state count alone."""
-    for lanes, orders in ((5, 2), (4, 4), (5, 4), (8, 4), (8, 8), (16, 4), (32, 4)):
+    for lanes, orders in ((1, 10), (5, 4), (8, 4), (8, 8), (16, 4), (32, 4)):
         if lanes * orders >= states:
             return (lanes, orders, 4)
     raise ValueError("more than 128 states")
