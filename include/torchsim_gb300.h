@@ -190,8 +190,8 @@ int tsg_epg_tangent(const tsg_program* program, const tsg_tissue* tissue, int64_
 
 /* Forward (as tsg_epg_forward; outputs nullable) that also stores the state
  * entering every ops_per_checkpoint-th op into `checkpoints` (DEVICE,
- * train x atom x ceil(ops/ops_per_checkpoint) x 3 x state_count floats), the
- * input of tsg_epg_adjoint. */
+ * train x ceil(ops/ops_per_checkpoint) x 3 x state_count x atom floats, atoms
+ * innermost), the input of tsg_epg_adjoint. */
 int tsg_epg_forward_checkpointed(const tsg_program* program, const tsg_tissue* tissue,
                                  int64_t atom_count, int64_t state_count, int layout, float* out_a,
                                  float* out_b, float* checkpoints, int ops_per_checkpoint,

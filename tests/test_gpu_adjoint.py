@@ -113,9 +113,10 @@ def test_segment_length_does_not_change_gradients(cuda, ops_per_checkpoint):
 
 
 @pytest.mark.parametrize("shape", [(1, 20, 4), (1, 10, 2), (5, 2, 4), (2, 6, 4), (5, 4, 2),
-                                   (10, 2, 4), (4, 4, 8), (4, 6, 4), (8, 4, 4), (8, 8, 2),
+                                   (10, 2, 4), (4, 4, 2), (4, 6, 4), (8, 4, 4), (8, 8, 2),
                                    (16, 4, 4), (32, 4, 4)])
-def test_adjoint_launch_shapes(cuda, shape):
+@pytest.mark.parametrize("mode", ["checkpointed", "trajectory"])
+def test_adjoint_launch_shapes(cuda, shape, mode):
     from torchsim_gb300 import engine
     from torchsim_gb300.sequence import mrf_events, program_for
 
@@ -130,7 +131,8 @@ def test_adjoint_launch_shapes(cuda, shape):
     prog = program_for(ev, cuda)
     tissue = engine.tissue_maps(cuda, V, t1, t2, None, b1, inv)
     seed = torch.from_numpy(rng.standard_normal((V, ev.outputs)).astype(np.complex64)).to(cuda)
-    c, ck, _ = engine.adjoint_plan(prog, V, S, shape, 0)
+    c, ck, _ = engine.adjoint_plan(prog, V, S, shape, 1 if mode == "trajectory" else 0)
+    assert (c == 1) == (mode == "trajectory")
     ckpt = torch.empty(ck // 4, dtype=torch.float32, device=cuda)
     # The checkpoint layout does not depend on the forward's launch shape.
     engine.forward_checkpointed(prog, tissue, S, c, ckpt)
@@ -141,7 +143,7 @@ def test_adjoint_launch_shapes(cuda, shape):
                     "f64")
     for name in ("t1_ms", "t2_ms", "b1", "inversion", "flip_rad"):
         got = grads[name].cpu().numpy().reshape(ref[name].shape)
-        assert max_rel(got, ref[name]) <= GRAD_TOL, (shape, name)
+        assert max_rel(got, ref[name]) <= GRAD_TOL, (shape, mode, name)
 
 
 def test_adjoint_against_central_differences(cuda):
@@ -201,3 +203,12 @@ def test_adjoint_deterministic(cuda, golden):
     b = _loss_grads(d["flip_deg"], d["tr_ms"], d["t1"], d["t2"], d["b1"], d["target"], 8, cuda)
     for k in ("flip", "tr", "t1", "t2", "b1"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_adjoint_block_size_is_checked(cuda):
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    prog = program_for(mrf_events(np.full(8, 20.0, np.float32), 9.0), cuda)
+    with pytest.raises(ValueError):
+        engine.adjoint_plan(prog, 16, 10, (5, 2, 8), 0)

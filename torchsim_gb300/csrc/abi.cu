@@ -281,9 +281,19 @@ extern "C" int tsg_epg_forward_checkpointed(const tsg_program* program, const ts
     a.sig_a = out_a;
     a.sig_b = out_b;
     if (layout == TSG_LAYOUT_PLANES ? !out_b : !out_a) a.sig_a = a.sig_b = nullptr;
-    a.ckpt = checkpoints;
-    a.ckpt_every = ops_per_checkpoint;
-    a.ckpt_count = int((program->host.ops + ops_per_checkpoint - 1) / ops_per_checkpoint);
+    if (ops_per_checkpoint == 1) {
+        // Trajectory mode: every op's entry state as order pairs, then the
+        // recorded F+[0] values.
+        const int64_t state_bytes = trajectory_state_bytes(program->host.trains, program->host.ops,
+                                                           atom_count, state_count);
+        a.traj = reinterpret_cast<float2*>(checkpoints);
+        a.traj_rec = reinterpret_cast<float*>(reinterpret_cast<char*>(checkpoints) +
+                                              align256(state_bytes));
+    } else {
+        a.ckpt = checkpoints;
+        a.ckpt_every = ops_per_checkpoint;
+        a.ckpt_count = int((program->host.ops + ops_per_checkpoint - 1) / ops_per_checkpoint);
+    }
     return launch(MODE_FORWARD, program, a, atom_count, int(state_count), launch_shape,
                   static_cast<cudaStream_t>(stream));
 }

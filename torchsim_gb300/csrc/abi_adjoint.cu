@@ -31,6 +31,7 @@ constexpr size_t kStageBudget = 100 * 1024;
 
 struct AdjointPlan {
     const AdjointEntry* entry = nullptr;
+    bool trajectory = false;
     int warps = 4;
     int ops_per_checkpoint = 1;
     int checkpoint_count = 0;
@@ -51,21 +52,21 @@ int sm_count_adj() {
     return count;
 }
 
-int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_launch* want,
-              int ops_per_checkpoint, AdjointPlan* plan) {
-    if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
-    if (atoms < 0 || states < 1) return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
-    if (states > 256) return fail(TSG_ERR_CAPACITY, "more than 256 states");
-    const bool shaped = want && (want->lanes_per_voxel > 0 || want->orders_per_lane > 0);
-    // One voxel per lane up to 20 states (measured best), two warps a block.
-    const bool one_lane = !shaped && states <= 20;
+int make_plan_with(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_launch* want,
+                   int ops_per_checkpoint, bool one_lane, AdjointPlan* plan) {
     plan->warps = (want && want->warps_per_block > 0) ? want->warps_per_block : (one_lane ? 2 : 4);
-    if (plan->warps < 1 || plan->warps > 8) return fail(TSG_ERR_ARGUMENT, "warps_per_block must be 1..8");
+    // ops_per_checkpoint == 1 is trajectory mode: the forward stores every
+    // op's entry state and the reverse sweep re-runs nothing.
+    const bool trajectory = ops_per_checkpoint == 1;
+    plan->trajectory = trajectory;
+    int table_count = 0;
+    const AdjointEntry* table = adjoint_table(plan->warps, trajectory, &table_count);
+    if (!table) return fail(TSG_ERR_ARGUMENT, "the adjoint takes 2 or 4 warps per block");
     const AdjointEntry* best = nullptr;
     double best_score = 1e300;
     const double target = double(sm_count_adj()) * 512.0;
-    for (int i = 0; i < kAdjointCount; ++i) {
-        const AdjointEntry& e = kAdjoint[i];
+    for (int i = 0; i < table_count; ++i) {
+        const AdjointEntry& e = table[i];
         const int padded = e.lanes_per_voxel * e.orders_per_lane;
         if (padded < states) continue;
         if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
@@ -87,25 +88,69 @@ int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_
     plan->entry = best;
     const int threads = 32 * plan->warps;
     const int vpb = plan->warps * (32 / best->lanes_per_voxel);
-    // Per op of a segment: the op, its transcendentals per voxel, and the
-    // pre-RF state (3 planes x orders x threads).
-    const size_t per_op = sizeof(Op) + sizeof(float4) * size_t(vpb) +
-                          size_t(3) * best->orders_per_lane * threads * sizeof(float);
-    int c = ops_per_checkpoint;
-    if (c <= 0) c = int(std::max<size_t>(1, std::min<size_t>(64, kStageBudget / per_op)));
-    if (size_t(c) * per_op > 200 * 1024) return fail(TSG_ERR_CAPACITY, "segment does not fit in shared memory");
-    plan->ops_per_checkpoint = c;
     const int64_t ops = prog->host.ops;
-    plan->checkpoint_count = int((ops + c - 1) / c);
+    const int64_t event_bytes = prog->host.trains * ((atoms + vpb - 1) / vpb) * plan->warps * ops *
+                                int64_t(sizeof(float2));
+    const int64_t tissue_bytes = prog->host.trains * atoms * 5 * int64_t(sizeof(float));
     plan->blocks = (atoms + vpb - 1) / vpb;
     plan->warps_per_train = plan->blocks * plan->warps;
+    plan->workspace_bytes = align256(event_bytes) + tissue_bytes;
+    if (trajectory) {
+        // Shared memory: a chunk of ops, their transcendentals, the lanes'
+        // event partials (rows of chunk + 1) and the entry-state ring.
+        plan->ops_per_checkpoint = 1;
+        plan->checkpoint_count = int(ops);
+        plan->checkpoint_bytes =
+            align256(trajectory_state_bytes(prog->host.trains, ops, atoms, states)) +
+            trajectory_record_bytes(prog->host.trains, prog->host.outputs, atoms);
+        if (ops > kTrajMaxOps)
+            return fail(TSG_ERR_CAPACITY, "trajectory mode takes at most 2048 ops; use checkpoints");
+        plan->smem = size_t(kTrajRing) * threads *
+                         (sizeof(float4) + sizeof(float2) +
+                          sizeof(float2) * 3 * size_t(best->orders_per_lane / 2)) +
+                     sizeof(float2) * size_t(threads) * (kTrajChunk + 1) + sizeof(Op) * size_t(ops);
+        if (plan->smem > 200 * 1024)
+            return fail(TSG_ERR_CAPACITY, "trajectory ring does not fit in shared memory");
+        return TSG_OK;
+    }
+    // Per op of a segment: the op, its transcendentals per voxel, the
+    // pre-RF state (3 planes x orders x threads) and each lane's event
+    // partials (float2; one more column pads the rows to an odd length).
+    const size_t per_op = sizeof(Op) + sizeof(float4) * size_t(vpb) +
+                          size_t(3) * best->orders_per_lane * threads * sizeof(float) +
+                          sizeof(float2) * size_t(threads) + sizeof(float) * size_t(threads);
+    // Fixed: the event rows' pad column and the prefetched checkpoint.
+    const size_t pad = sizeof(float2) * size_t(threads) +
+                       size_t(3) * best->orders_per_lane * threads * sizeof(float);
+    int c = ops_per_checkpoint;
+    if (c <= 0) c = int(std::max<size_t>(1, std::min<size_t>(64, (kStageBudget - pad) / per_op)));
+    if (size_t(c) * per_op + pad > 200 * 1024)
+        return fail(TSG_ERR_CAPACITY, "segment does not fit in shared memory");
+    plan->ops_per_checkpoint = c;
+    plan->checkpoint_count = int((ops + c - 1) / c);
     plan->checkpoint_bytes = prog->host.trains * atoms * int64_t(plan->checkpoint_count) * 3 * states *
                              int64_t(sizeof(float));
-    const int64_t event_bytes = prog->host.trains * plan->warps_per_train * ops * int64_t(sizeof(float2));
-    const int64_t tissue_bytes = prog->host.trains * atoms * 5 * int64_t(sizeof(float));
-    plan->workspace_bytes = ((event_bytes + 255) / 256) * 256 + tissue_bytes;
-    plan->smem = size_t(c) * per_op;
+    plan->smem = size_t(c) * per_op + pad;
     return TSG_OK;
+}
+
+int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_launch* want,
+              int ops_per_checkpoint, AdjointPlan* plan) {
+    if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
+    if (atoms < 0 || states < 1) return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
+    if (states > 256) return fail(TSG_ERR_CAPACITY, "more than 256 states");
+    const bool shaped = want && (want->lanes_per_voxel > 0 || want->orders_per_lane > 0);
+    // One voxel per lane up to 20 states (measured best), two warps a block;
+    // a requested segment too long for its shared memory takes the
+    // multi-lane shapes instead.
+    if (!shaped && states <= 20) {
+        AdjointPlan trial;
+        if (make_plan_with(prog, atoms, states, want, ops_per_checkpoint, true, &trial) == TSG_OK) {
+            *plan = trial;
+            return TSG_OK;
+        }
+    }
+    return make_plan_with(prog, atoms, states, want, ops_per_checkpoint, false, plan);
 }
 
 }  // namespace
@@ -131,7 +176,15 @@ int run_adjoint(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms
     a.inv = tissue->inversion;
     a.seed = seed;
     a.seed_layout = seed_layout;
-    a.ckpt = ckpt;
+    if (plan.trajectory) {
+        const int64_t state_bytes =
+            trajectory_state_bytes(prog->host.trains, ops, atoms, states);
+        a.traj = reinterpret_cast<const float2*>(ckpt);
+        a.traj_rec = reinterpret_cast<const float*>(reinterpret_cast<const char*>(ckpt) +
+                                                    align256(state_bytes));
+    } else {
+        a.ckpt = ckpt;
+    }
     a.ckpt_every = plan.ops_per_checkpoint;
     a.ckpt_count = plan.checkpoint_count;
     a.event_partial = static_cast<float2*>(workspace);

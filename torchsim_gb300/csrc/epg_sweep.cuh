@@ -200,22 +200,45 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 }
             }
             if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
-                // State entering this op, for the adjoint's segments.
+                // State entering this op, for the adjoint's segments; atoms
+                // innermost, so a warp's stores of one order are contiguous.
                 const int k = (base + i) / a.ckpt_every;
                 const int Sn = a.states;
-                float* dst = a.ckpt + (row * a.ckpt_count + k) * (3 * int64_t(Sn));
+                const int64_t n = a.atoms;
+                float* dst = a.ckpt + (train * a.ckpt_count + k) * (3 * int64_t(Sn)) * n + atom;
 #pragma unroll
                 for (int kk = 0; kk < RP; ++kk) {
                     const int o = q * R + 2 * kk;
                     if (o < Sn) {
-                        dst[o] = P[kk].x;
-                        dst[Sn + o] = M[kk].x;
-                        dst[2 * Sn + o] = Z[kk].x;
+                        dst[o * n] = P[kk].x;
+                        dst[(Sn + o) * n] = M[kk].x;
+                        dst[(2 * Sn + o) * n] = Z[kk].x;
                     }
                     if (o + 1 < Sn) {
-                        dst[o + 1] = P[kk].y;
-                        dst[Sn + o + 1] = M[kk].y;
-                        dst[2 * Sn + o + 1] = Z[kk].y;
+                        dst[(o + 1) * n] = P[kk].y;
+                        dst[(Sn + o + 1) * n] = M[kk].y;
+                        dst[(2 * Sn + o + 1) * n] = Z[kk].y;
+                    }
+                }
+            }
+            if constexpr (NT == 0 && !GEN && !GN) {
+                if (a.traj != nullptr && active) {
+                    // Every op's entry state as this lane's order pairs, in
+                    // tiles of 32 atoms: [train][tile][op][plane][pair][32].
+                    const int np = (a.states + 1) >> 1;
+                    const int64_t tiles = (a.atoms + 31) >> 5;
+                    float2* dst = a.traj +
+                                  ((train * tiles + (atom >> 5)) * a.n_ops + base + i) *
+                                      (3 * int64_t(np) * 32) +
+                                  (atom & 31);
+#pragma unroll
+                    for (int kk = 0; kk < RP; ++kk) {
+                        const int pj = q * RP + kk;
+                        if (pj < np) {
+                            dst[pj * 32] = P[kk];
+                            dst[(np + pj) * 32] = M[kk];
+                            dst[(2 * np + pj) * 32] = Z[kk];
+                        }
                     }
                 }
             }
@@ -424,6 +447,9 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
             if ((code & OP_RECORD) && q == 0 && active && !GN) {
                 const int rec = op.record;
                 const float p0 = P[0].x;
+                if constexpr (NT == 0 && !GEN)
+                    if (a.traj_rec != nullptr)
+                        a.traj_rec[(train * a.outputs + rec) * a.atoms + atom] = p0;
                 if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
                     if (a.sig_a != nullptr || a.sig_b != nullptr)
                         put_sample(a.layout, a.sig_a, a.sig_b, sig_base + rec, m0 * p0);

@@ -115,11 +115,17 @@ struct SweepArgs {
     int jac_cols;
     int col_t1, col_t2, col_b1, col_inv, col_m0, col_gen;
     // Optional state checkpoints for the adjoint: every ckpt_every ops the
-    // state entering that op is stored, [train][atom][k][plane][order] with
-    // plane F+, F-, Z and `states` orders.
+    // state entering that op is stored, [train][k][plane][order][atom] with
+    // plane F+, F-, Z and `states` orders (atoms innermost: coalesced).
     float* ckpt;
     int ckpt_every;
     int ckpt_count;
+    // Optional trajectory for the adjoint (forward sweeps only): every op's
+    // entry state as order pairs, tiled by 32 atoms,
+    // [train][atom / 32][op][plane][pair][atom % 32] float2 with
+    // (states + 1) / 2 pairs, and every recorded F+[0], [train][output][atom].
+    float2* traj;
+    float* traj_rec;
     // Gauss-Newton accumulation (GN sweeps): the measured samples (complex64
     // of the API signal) at row measured_rows[atom] (or atom when null), and
     // per voxel: cost, J^T J (6, upper triangle by rows) and J^T r (3) of the
@@ -182,7 +188,9 @@ struct AdjointArgs {
     // or the complex64 gradient of 1j*signal (layout COMPLEX_IJ).
     const float* seed;
     int seed_layout;
-    const float* ckpt;   // [train][atom][k][3][states], written by a forward sweep
+    const float* ckpt;   // [train][k][3][states][atom], written by a forward sweep
+    const float2* traj;  // trajectory mode: [train][atom/32][op][3][(states+1)/2][atom%32] float2
+    const float* traj_rec;  // trajectory mode: recorded F+[0], [train][output][atom]
     int ckpt_every;      // ops per segment (C)
     int ckpt_count;      // segments per row
     float2* event_partial;   // [train][warp][op]: (flip, duration) gradient partials
@@ -196,11 +204,30 @@ using AdjointLaunch = void (*)(const AdjointArgs&, dim3 grid, dim3 block, size_t
 struct AdjointEntry {
     int orders_per_lane;
     int lanes_per_voxel;
+    int warps;  // warps per block (compile-time in the kernel)
     AdjointLaunch launch;
     const void* kernel;  // for the shared-memory attribute
 };
 
-extern const AdjointEntry kAdjoint[];
-extern const int kAdjointCount;
+// The reverse-sweep kernels built for `warps` warps per block (2 or 4),
+// checkpointed or trajectory; null with *count = 0 for any other block size.
+const AdjointEntry* adjoint_table(int warps, bool trajectory, int* count);
+
+// Trajectory-mode reverse sweep: ops per event-gradient reduction, ops in
+// flight per lane (ring slots in shared memory), and the longest program it
+// keeps in shared memory.
+constexpr int kTrajChunk = 32;
+constexpr int kTrajRing = 4;
+constexpr int kTrajMaxOps = 2048;
+
+// Bytes of the adjoint's trajectory mode: entry states (whole tiles of 32
+// atoms) and recorded F+[0].
+inline int64_t trajectory_state_bytes(int64_t trains, int64_t ops, int64_t atoms, int64_t states) {
+    return trains * ((atoms + 31) / 32) * ops * 3 * ((states + 1) / 2) * 32 * int64_t(sizeof(float2));
+}
+inline int64_t trajectory_record_bytes(int64_t trains, int64_t outputs, int64_t atoms) {
+    return trains * outputs * atoms * int64_t(sizeof(float));
+}
+inline int64_t align256(int64_t bytes) { return (bytes + 255) / 256 * 256; }
 
 }  // namespace tsg

@@ -279,6 +279,21 @@ def forward_checkpointed(program: Program, tissue: TissueMaps, states: int, ops_
     return out
 
 
+# Trajectory mode (every op's entry state kept, nothing re-run in the reverse
+# sweep) is used while its buffer takes at most this share of the free device
+# memory; longer problems fall back to checkpoints every few ops.
+TRAJECTORY_MEMORY_SHARE = 0.25
+
+
+def segment_for(program: Program, voxels: int, states: int, launch=None) -> int:
+    """Ops per checkpoint for an autograd forward: 1 (trajectory mode) when
+    the trajectory fits ``TRAJECTORY_MEMORY_SHARE`` of free memory, else 0
+    (the library's checkpoint spacing)."""
+    _, traj_bytes, _ = adjoint_plan(program, voxels, states, launch, 1)
+    free, _ = torch.cuda.mem_get_info()
+    return 1 if traj_bytes <= TRAJECTORY_MEMORY_SHARE * free else 0
+
+
 GRAD_NAMES = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")
 
 
@@ -306,7 +321,8 @@ def adjoint(program: Program, tissue: TissueMaps, states: int, seed: torch.Tenso
 
 
 class EpgFunction(torch.autograd.Function):
-    """Forward sweep whose backward is the checkpointed adjoint kernel.
+    """Forward sweep whose backward is the adjoint kernel (trajectory mode
+    when it fits in memory, else checkpointed).
 
     The role of the reference's ``_NativeEpg`` (sequence/_accelerators.py:
     1402-1594): inputs are the flat tissue maps and the event-level flip and
@@ -320,7 +336,8 @@ class EpgFunction(torch.autograd.Function):
         tissue = TissueMaps(t1.detach(), t2.detach(), None if m0 is None else m0.detach(),
                             None if b1 is None else b1.detach(),
                             None if inv is None else inv.detach())
-        c, ck_bytes, _ = adjoint_plan(program, tissue.voxels, states, launch)
+        c, ck_bytes, _ = adjoint_plan(program, tissue.voxels, states, launch,
+                                      segment_for(program, tissue.voxels, states, launch))
         ckpt = torch.empty(max(ck_bytes // 4, 1), dtype=torch.float32, device=t1.device)
         out = torch.empty((program.trains * tissue.voxels, program.outputs), dtype=torch.complex64,
                           device=t1.device)

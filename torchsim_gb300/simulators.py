@@ -204,6 +204,12 @@ class _EpgSimulator:
         """Return ``(signal, jacobian)``; the Jacobian is ``(*voxels, k, samples)``
         (``(*voxels, samples)`` for a single name given as a string)."""
         names = (diff,) if isinstance(diff, str) else tuple(diff)
+        if torch.is_grad_enabled() and any(
+                isinstance(v, torch.Tensor) and v.requires_grad
+                for v in {**self.protocol, **values}.values()):
+            raise NotImplementedError(
+                "the Jacobian is not differentiable here: second-order (forward-over-reverse) "
+                "derivatives are not built")
         signal, jac = self._run(values, names)
         if isinstance(diff, str):
             jac = jac[..., 0, :]
