@@ -367,8 +367,9 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
 
 def adjoint_section(torch, device, repeats: int = 5) -> dict:
     """Gradient of sum |s - target|^2 over 16,384 voxels w.r.t. 600 flips and
-    600 TRs (and the tissue), nstates 20: the checkpointed adjoint against one
-    plain forward of the same sequence."""
+    600 TRs (and the tissue), nstates 20: the adjoint (trajectory or
+    checkpointed, whichever the tuner finds faster) against one plain forward
+    of the same sequence."""
     from torchsim_gb300 import engine
     from torchsim_gb300.sequence import mrf_events, program_for
 
@@ -410,8 +411,10 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
         ckpt, work = buffers[(shape, c)]
         engine.adjoint(prog, tissue, S, seed, ckpt, c, grads, workspace=work, launch=shape)
 
+    # Segment length 1 is trajectory mode (every op's entry state kept);
+    # longer segments are checkpoints with a re-run.
     adj_cands = [(*shape, c) for shape in ((1, 20, 2), (1, 20, 4), (5, 4, 2), (5, 4, 4), (4, 6, 2),
-                                           (10, 2, 4), (2, 10, 2)) for c in (4, 6, 8)]
+                                           (10, 2, 4), (2, 10, 2)) for c in (1, 4, 5, 6)]
     adj_best, _ = autotune.tune(autotune.workload_key("adjoint", states=S, ops=prog.ops, voxels=V),
                                 adj_cands, run_adjoint, use_cache=False)
     shape, c_req = tuple(adj_best[:3]), adj_best[3]
@@ -441,6 +444,7 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
     return {
         "workload": "MRF adjoint: 16384 voxels, 600 pulses (flip U(5,70) deg, TR U(8,15) ms), "
                     "nstates 20, loss sum |s - target|^2",
+        "mode": "trajectory" if c == 1 else "checkpointed",
         "ops_per_checkpoint": c,
         "checkpoint_bytes": ck,
         "forward_shape": list(fwd_shape),

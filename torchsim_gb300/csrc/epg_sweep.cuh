@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                     my_co = cj;
                 }
             }
+            if constexpr (NT == 0 && !GEN && !GN) {
             if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
                 // State entering this op, for the adjoint's segments; atoms
                 // innermost, so a warp's stores of one order are contiguous.
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                         dst[(2 * Sn + o + 1) * n] = Z[kk].y;
                     }
                 }
+            }
             }
             if constexpr (NT == 0 && !GEN && !GN) {
                 if (a.traj != nullptr && active) {
