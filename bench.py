@@ -354,7 +354,8 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     if not args.skip_adjoint:
         line["adjoint"] = adjoint_section(torch, device)
     if not args.skip_batched:
-        line["batched"] = batched_section(torch, device, sequences=args.batch_sequences)
+        line["batched"] = batched_section(torch, device, sequences=args.batch_sequences,
+                                          shape=args.batch_shape)
     if not args.skip_gn:
         line["gn_server"] = gn_section(torch, device, requests=args.gn_requests)
     if not args.skip_cpu:
@@ -464,7 +465,8 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
 # ---- uneven CPMG batch in one persistent launch ------------------------------
 
 
-def batched_section(torch, device, sequences: int = 512, repeats: int = 5) -> dict:
+def batched_section(torch, device, sequences: int = 512, repeats: int = 5,
+                    shape: tuple[int, int, int] | None = None) -> dict:
     """512 CPMG sequences: ETL U{8..64}, refocusing U(100,180) deg per echo,
     ESP U(5,15) ms, excitation 90 deg at 90 deg phase, refocusing phase 90 deg,
     voxels per sequence round(exp(U(ln 1e3, ln 6.4e4))), T1 U(300,3000),
@@ -485,7 +487,10 @@ def batched_section(torch, device, sequences: int = 512, repeats: int = 5) -> di
                                   rng.uniform(0.7, 1.3, v).astype(np.float32)))
     batch = SequenceBatch(entries, device)
     t0 = time.perf_counter()
-    shape, timings = batch.tune(use_cache=False)
+    if shape is None:
+        shape, timings = batch.tune(use_cache=False)
+    else:
+        batch.shape, timings = tuple(shape), {}
     tune_s = time.perf_counter() - t0
     batch.capture()
 
@@ -761,6 +766,9 @@ def main() -> None:
     ap.add_argument("--skip-gn", action="store_true")
     ap.add_argument("--gn-requests", type=int, default=40)
     ap.add_argument("--batch-sequences", type=int, default=512)
+    ap.add_argument("--batch-shape", type=int, nargs=3, default=None,
+                    metavar=("ORDERS", "WARPS", "CTAS_PER_SM"),
+                    help="persistent launch shape of the batched section (default: autotuned)")
     ap.add_argument("--atoms", type=int, default=ATOMS,
                     help="first N grid atoms (a smaller case for profiling; default all)")
     ap.add_argument("--launch", type=int, nargs="+", metavar="N",
