@@ -52,3 +52,15 @@ def test_real_axis_verdict():
     assert fse_events(np.float32([180, 120]), 10.0, phases_deg=0.0).real_axis() == -1
     with pytest.raises(ValueError):
         mrf_events(np.float32([10, 20]), np.float32([1, 2, 3]))
+
+
+def test_mrf_builder_edges():
+    with pytest.raises(ValueError):
+        mrf_events(np.float32([]), 10.0)
+    one = mrf_events(np.float32([30.0]), 12.0, TI_ms=5.0)
+    assert one.events == 5 and one.outputs == 1
+    assert np.allclose(one.time_us, [5000.0])
+    two = mrf_events(np.float32([30.0, 40.0]), 12.0, repetitions=3)
+    assert two.events == 27 and two.outputs == 2
+    # The recorded samples are the last playing's: two trains after the first.
+    assert np.allclose(two.time_us, [2 * 24000.0, 2 * 24000.0 + 12000.0])

@@ -144,29 +144,10 @@ def mrf_events(flip_deg: Any, TR_ms: Any, TI_ms: Any = 0.0, phases_deg: Any = 0.
     turns = torch.deg2rad(_matched(phases_deg, angles))
     spacing_s = _matched(TR_ms, angles) * 1e-3
     n = int(angles.numel())
-    # Clock as compose() walks it: the inversion at 0, each repetition's
-    # events at the cursor, the cursor moved on by the readout's duration.
-    ti = TI_ms * 1e-3 if isinstance(TI_ms, (int, float)) else _as_tensor(TI_ms) * 1e-3
-    cursor: Any = 0.0 + ti
-    starts: list[Any] = []
-    for index in range(n):
-        starts.append(cursor)
-        cursor = cursor + spacing_s[index]
-    played_s = cursor
-    stamps: list[Any] = [1e6 * 0.0]
-    for start in starts:
-        stamp = 1e6 * start
-        stamps.extend([stamp, stamp, stamp, stamp])
+    if n == 0:
+        raise ValueError("an MRF train needs at least one pulse")
     per_rep = 1 + 4 * n
-    clock: list[Any] = []
-    tr_us = 1e6 * played_s
-    for rep in range(repetitions):
-        for stamp in stamps:
-            clock.append(tr_us * rep + stamp if rep else stamp)
-    if any(isinstance(v, torch.Tensor) for v in clock):
-        clock_t = torch.stack([torch.as_tensor(v, dtype=torch.float32).reshape(()) for v in clock])
-    else:
-        clock_t = torch.tensor(clock, dtype=torch.float64)
+    clock_t = _mrf_clock(spacing_s, TI_ms, n, repetitions)
     kind = np.zeros(per_rep, np.int32)
     action = np.zeros(per_rep, np.uint8)
     flip = np.zeros(per_rep, np.float32)
@@ -202,6 +183,39 @@ def mrf_events(flip_deg: Any, TR_ms: Any, TI_ms: Any = 0.0, phases_deg: Any = 0.
         output_index=output_index,
         time_us=clock_t.to(torch.float32).numpy()[recorded],
     )
+
+
+def _mrf_clock(spacing_s: torch.Tensor, TI_ms: Any, n: int, repetitions: int) -> torch.Tensor:
+    """Event times (us) of the MRF train, as compose() walks them.
+
+    The inversion sits at 0; repetition k's pulses start at the cursor, which
+    begins at TI and advances by each TR in turn; a later playing is offset
+    by the whole train's length. The arithmetic is the reference's, in the
+    precision it has there: the TRs are float32 seconds, so every cursor step
+    after the first is a float32 addition (a sequential float32 prefix sum
+    here), the first start keeps TI's own precision, and times are float32
+    products by 1e6 (``simulators/mrf.py:46-77``, ``_accelerators.py:1125``).
+    """
+    s32 = spacing_s.detach().to(torch.float32).cpu().numpy()
+    if isinstance(TI_ms, (int, float)):
+        ti = float(TI_ms) * 1e-3
+        first_stamp = np.float32(1e6 * ti)  # a Python float, rounded once
+        c0 = np.float32(ti)
+    else:
+        ti_t = _as_tensor(TI_ms) * 1e-3
+        c0 = np.float32(ti_t.to(torch.float32).item())
+        first_stamp = np.float32(np.float32(1e6) * c0)
+    # cursor[k] = start of pulse k; cursor[n] = the train's length.
+    cursor = np.cumsum(np.concatenate([np.float32([c0]), s32]), dtype=np.float32)
+    starts = np.float32(1e6) * cursor[:n]
+    starts[0] = first_stamp
+    stamps = np.concatenate([np.float32([0.0]), np.repeat(starts, 4)])
+    if n == 1 and repetitions == 1 and isinstance(TI_ms, (int, float)):
+        # No float32 value reaches the clock: it stays in double.
+        return torch.tensor([0.0] + [1e6 * ti] * 4, dtype=torch.float64)
+    tr_us = np.float32(1e6) * cursor[n]
+    clock = [stamps] + [np.float32(tr_us * np.float32(rep)) + stamps for rep in range(1, repetitions)]
+    return torch.from_numpy(np.concatenate(clock).astype(np.float32))
 
 
 def mrf_gradient_map(pulses: int, repetitions: int = 1) -> dict[str, np.ndarray]:
