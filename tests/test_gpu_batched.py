@@ -36,7 +36,7 @@ def _check_against_oracle(batch):
         assert max_rel(got.imag, ref) <= 1e-5, s
 
 
-@pytest.mark.parametrize("shape", [(2, 2, 2), (4, 4, 4), (8, 8, 2), (4, 1, 16)])
+@pytest.mark.parametrize("shape", [(2, 2, 2), (4, 4, 4), (8, 8, 2), (4, 1, 16), (16, 2, 8)])
 def test_batched_matches_oracle(cuda, shape):
     batch = make_batch(cuda, etls=(8, 13, 21, 32) if shape[0] == 2 else (8, 13, 21, 32, 47, 64))
     batch.out.fill_(float("nan"))

@@ -84,3 +84,24 @@ def test_program_key_changes_with_content():
     a = mrf_events(np.float32([10, 20]), 10.0)
     b = mrf_events(np.float32([10, 21]), 10.0)
     assert a.key() != b.key() and a.key() == mrf_events(np.float32([10, 20]), 10.0).key()
+
+
+def test_engine_facade_defaults_and_labels():
+    from torchsim_gb300 import EpgEngine
+    from torchsim_gb300.sequence import fse_events, mrf_events
+
+    mrf = mrf_events(np.float32([10, 20, 30]), 10.0, repetitions=2)
+    eng = EpgEngine()
+    assert eng.shifts_per_repetition(mrf) == 3
+    fse = fse_events(np.float32([180, 150]), 10.0, phases_deg=90.0)
+    assert eng.shifts_per_repetition(fse) == 4
+    # Samples are recorded by the ADC events of the last playing, in order.
+    assert mrf.sample_events().tolist() == [13 + 2, 13 + 6, 13 + 10]
+    assert fse.sample_events().tolist() == [2, 5]
+    assert mrf.echo.tolist() == [False] * 3 and fse.echo.tolist() == [True, True]
+    with pytest.raises(ValueError):
+        eng.simulate(mrf, {"T1": 1000.0, "T2": 80.0}, repetitions=3)
+    with pytest.raises(ValueError):
+        eng.simulate(mrf, {"T1": 1000.0, "T2": 80.0}, record="odd")
+    with pytest.raises(ValueError):
+        eng.simulate(mrf, {"T1": 1000.0})

@@ -4,6 +4,8 @@ Public API kept from the reference (FiRMLAB-Pisa/torchsim):
 
 * ``mrf_sim``, ``fse_sim`` — functional simulators with ``diff=`` Jacobians;
 * ``MRFSimulator``, ``FSESimulator`` — ``simulate`` / ``jacobian``;
+* ``EpgEngine().simulate(events, tissue)`` — a packed stream on the kernels,
+  with its sample labels (``SimulationResult``);
 * ``SequenceDesign``, ``Bounded``, ``crlb`` — sequence design through the
   adjoint kernel.
 
@@ -12,8 +14,9 @@ All compute runs in hand-written sm_103a CUDA kernels behind the C ABI in
 """
 
 from .design import Bounded, SequenceDesign, SequenceOptimization, crlb
-from .simulators import FSESimulator, MRFSimulator, fse_sim, mrf_sim
+from .simulators import (EpgEngine, FSESimulator, MRFSimulator, SimulationResult, fse_sim,
+                         mrf_sim)
 
-__all__ = ["Bounded", "FSESimulator", "MRFSimulator", "SequenceDesign", "SequenceOptimization",
-           "crlb", "fse_sim", "mrf_sim"]
+__all__ = ["Bounded", "EpgEngine", "FSESimulator", "MRFSimulator", "SequenceDesign",
+           "SequenceOptimization", "SimulationResult", "crlb", "fse_sim", "mrf_sim"]
 __version__ = "0.1.0"

@@ -160,7 +160,7 @@ class SequenceBatch:
 
     def candidates(self) -> list[tuple[int, int, int]]:
         cands = []
-        for orders in (2, 4, 8):
+        for orders in (2, 4, 8, 16):
             if (-(-self.states // orders) > 32).any():
                 continue
             for warps in (2, 4, 8):

@@ -5,8 +5,8 @@
 // The work list holds (sequence, voxel tile) units, largest first. Each CTA
 // takes the next unit from a global counter (one atomicAdd, no waiting on
 // other CTAs), stages that sequence's program in shared memory and runs the
-// forward sweep for its voxels. Orders per lane (R) are fixed at compile
-// time; lanes per voxel (L = ceil(states/R)) are per sequence, so one kernel
+// forward sweep for its voxels. Orders per lane (R, even) are fixed at
+// compile time; lanes per voxel (L = ceil(states/R)) are per sequence, so one kernel
 // serves every echo-train length: voxels take floor(32/L) slots of a warp and
 // the shift's cross-lane moves respect the voxel boundaries through the lane's
 // index within its voxel, exactly as in the fixed-shape sweep.
@@ -18,32 +18,54 @@ namespace {
 
 constexpr int kBatchOpChunk = 512;
 
-template <int R>
-__device__ __forceinline__ void shift_runtime(float (&p)[R], float (&m)[R], int q, int L,
-                                              bool kill, int kill_r) {
-    const float in_p = __shfl_up_sync(0xffffffffu, p[R - 1], 1);
-    const float in_m = __shfl_down_sync(0xffffffffu, m[0], 1);
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// One gradient shift of the lane's order pairs (orders 2k, 2k+1 in pair k)
+// with a per-sequence lane count L: F- moves one order down, F+ one order up,
+// F+[0] = -F-[0] on the voxel's first lane, nothing crosses a voxel's edge,
+// and the slot at order `states` is cleared (truncation).
+template <int RP>
+__device__ __forceinline__ void shift_pairs(float2 (&p)[RP], float2 (&m)[RP], int q, int L,
+                                            bool kill, int kill_r) {
+    const float in_p = __shfl_up_sync(0xffffffffu, p[RP - 1].y, 1);
+    const float in_m = __shfl_down_sync(0xffffffffu, m[0].x, 1);
+    const float top = (q == L - 1) ? 0.f : in_m;
 #pragma unroll
-    for (int r = 0; r < R - 1; ++r) m[r] = m[r + 1];
+    for (int k = 0; k < RP; ++k) {
+        m[k].x = m[k].y;
+        m[k].y = (k + 1 < RP) ? m[k + 1].x : top;
+    }
+    const float bottom = (q == 0) ? -m[0].x : in_p;
 #pragma unroll
-    for (int r = R - 1; r > 0; --r) p[r] = p[r - 1];
-    m[R - 1] = (q == L - 1) ? 0.f : in_m;
-    p[0] = (q == 0) ? -m[0] : in_p;
+    for (int k = RP - 1; k >= 0; --k) {
+        p[k].y = p[k].x;
+        p[k].x = (k > 0) ? p[k - 1].y : bottom;
+    }
     if (kill) {
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-            if (r == kill_r) p[r] = 0.f;
+        for (int k = 0; k < RP; ++k) {
+            if (2 * k == kill_r) p[k].x = 0.f;
+            if (2 * k + 1 == kill_r) p[k].y = 0.f;
+        }
     }
 }
 
 }  // namespace
 
+// Orders are held as pairs (R / 2 float2 per plane) and advanced with the
+// paired FP32 instructions; each pulse's sin/cos is evaluated once per voxel:
+// lane q of a voxel takes one of every L ops and the voxel's lanes exchange
+// the values by shuffle (all lanes of a warp run the same sequence, so the
+// shuffles are convergent).
 template <int R>
 __global__ void __launch_bounds__(256) epg_batched_kernel(
     const Op* __restrict__ ops, const tsg_batch_sequence* __restrict__ seqs,
     const tsg_batch_unit* __restrict__ units, int64_t unit_count, int* __restrict__ counter,
     const float* __restrict__ t1v, const float* __restrict__ t2v, const float* __restrict__ m0v,
     const float* __restrict__ b1v, float2* __restrict__ out) {
+    constexpr int RP = R / 2;
     __shared__ Op s_ops[kBatchOpChunk];
     __shared__ int s_unit;
     const int lane = threadIdx.x & 31;
@@ -60,6 +82,7 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
         const int vpw = 32 / L;
         const int q = lane % L;
         const int slot = lane / L;
+        const int first_lane = lane - q;
         const int local = (warp * vpw + slot);
         const bool active = slot < vpw && local < u.voxel_count;
         const int64_t voxel = sq.voxel_offset + u.voxel_begin + (active ? local : 0);
@@ -72,12 +95,13 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
         const int S = sq.states;
         const bool kill = L * R > S;
         const int kill_r = S - q * R;
-        float P[R], M[R], Z[R];
+        float2 P[RP], M[RP], Z[RP];
 #pragma unroll
-        for (int r = 0; r < R; ++r) P[r] = M[r] = Z[r] = 0.f;
-        if (q == 0) Z[0] = 1.f;
+        for (int k = 0; k < RP; ++k) P[k] = M[k] = Z[k] = dup(0.f);
+        if (q == 0) Z[0].x = 1.f;
         float last_dt = __int_as_float(0x7fffffff);
         float e1 = 1.f, e2 = 1.f;
+        const float2 neg1 = dup(-1.f);
         float2* orow = out + sq.output_offset + int64_t(u.voxel_begin + local) * sq.outputs;
         for (int base = 0; base < sq.op_count; base += kBatchOpChunk) {
             const int count = min(kBatchOpChunk, sq.op_count - base);
@@ -85,7 +109,20 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
             for (int i = threadIdx.x; i < count; i += blockDim.x)
                 s_ops[i] = ops[sq.op_offset + base + i];
             __syncthreads();
+            float my_si = 0.f, my_co = 1.f;
+            int g = L;  // ops since the voxel's lanes last evaluated sin/cos
             for (int i = 0; i < count; ++i) {
+                if (g == L) {
+                    g = 0;
+                    const int j = i + q;
+                    float sj = 0.f, cj = 1.f;
+                    if (j < count) {
+                        const Op oj = s_ops[j];
+                        if (op_rf(oj.code) == RF_ROTATE) sincosf(oj.flip * b1, &sj, &cj);
+                    }
+                    my_si = sj;
+                    my_co = cj;
+                }
                 const Op op = s_ops[i];
                 const uint32_t code = op.code;
                 if (code & OP_RELAX) {
@@ -94,42 +131,45 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                         e1 = expf(-r1 * op.dt);
                         e2 = expf(-r2 * op.dt);
                     }
+                    const float2 E1 = dup(e1), E2 = dup(e2);
 #pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        P[r] *= e2;
-                        M[r] *= e2;
-                        Z[r] *= e1;
+                    for (int k = 0; k < RP; ++k) {
+                        P[k] = mul2(P[k], E2);
+                        M[k] = mul2(M[k], E2);
+                        Z[k] = mul2(Z[k], E1);
                     }
-                    if (q == 0) Z[0] += 1.f - e1;
+                    if (q == 0) Z[0].x += 1.f - e1;
                 }
-                for (int s = 0; s < op_shift1(code); ++s) shift_runtime<R>(P, M, q, L, kill, kill_r);
+                for (int s = 0; s < op_shift1(code); ++s) shift_pairs<RP>(P, M, q, L, kill, kill_r);
                 const int rf = op_rf(code);
                 if (rf == RF_ROTATE) {
-                    float si, co;
-                    sincosf(op.flip * b1, &si, &co);
-                    const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
+                    const float si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
+                    const float co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
+                    const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
+                    const float2 hs = dup(0.5f * si), si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
 #pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const float p = P[r], m = M[r], z = Z[r];
-                        P[r] = fmaf(ch, p, fmaf(sh, m, -si * z));
-                        M[r] = fmaf(sh, p, fmaf(ch, m, si * z));
-                        Z[r] = fmaf(hs, p - m, co * z);
+                    for (int k = 0; k < RP; ++k) {
+                        const float2 p = P[k], m = M[k], z = Z[k];
+                        P[k] = fma2(ch, p, fma2(sh, m, mul2(nsi2, z)));
+                        M[k] = fma2(sh, p, fma2(ch, m, mul2(si2, z)));
+                        Z[k] = fma2(hs, fma2(neg1, m, p), mul2(co2, z));
                     }
                 } else if (rf == RF_INVERT) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) Z[r] = -Z[r];
+                    for (int k = 0; k < RP; ++k) Z[k] = mul2(Z[k], neg1);
                 }
-                for (int s = 0; s < op_shift2(code); ++s) shift_runtime<R>(P, M, q, L, kill, kill_r);
+                ++g;
+                for (int s = 0; s < op_shift2(code); ++s) shift_pairs<RP>(P, M, q, L, kill, kill_r);
                 if (code & OP_SPOIL1) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) P[r] = M[r] = 0.f;
+                    for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
                 }
                 if ((code & OP_RECORD) && q == 0 && active)
-                    __stcs(orow + op.record, make_float2(0.f, m0 * P[0]));
-                for (int s = 0; s < op_shift3(code); ++s) shift_runtime<R>(P, M, q, L, kill, kill_r);
+                    __stcs(orow + op.record, make_float2(0.f, m0 * P[0].x));
+                for (int s = 0; s < op_shift3(code); ++s) shift_pairs<RP>(P, M, q, L, kill, kill_r);
                 if (code & OP_SPOIL2) {
 #pragma unroll
-                    for (int r = 0; r < R; ++r) P[r] = M[r] = 0.f;
+                    for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
                 }
             }
         }
@@ -174,8 +214,13 @@ extern "C" int tsg_epg_batched_forward(const void* ops, const tsg_batch_sequence
                                                           tissue->t1_ms, tissue->t2_ms, tissue->m0,
                                                           tissue->b1, y);
             break;
+        case 16:
+            epg_batched_kernel<16><<<grid, block, 0, s>>>(o, sequences, units, unit_count, counter,
+                                                           tissue->t1_ms, tissue->t2_ms, tissue->m0,
+                                                           tissue->b1, y);
+            break;
         default:
-            return fail(TSG_ERR_UNSUPPORTED, "orders_per_lane must be 2, 4 or 8");
+            return fail(TSG_ERR_UNSUPPORTED, "orders_per_lane must be 2, 4, 8 or 16");
     }
     TSG_CUDA(cudaGetLastError());
     return TSG_OK;

@@ -67,6 +67,16 @@ class PackedEvents:
     action: np.ndarray  # uint8 (events,)
     output_index: np.ndarray  # int32 (events,)
     time_us: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    # Labels of the recorded samples: the playing each belongs to (builders
+    # record only the last of `repetitions`), and whether it is a spin echo.
+    repetitions: int = 1
+    echo: np.ndarray | None = None  # bool (outputs,)
+
+    def sample_events(self) -> np.ndarray:
+        """Index of the event that records each sample, (outputs,) int64."""
+        where = np.flatnonzero(self.output_index >= 0)
+        order = np.argsort(self.output_index[where], kind="stable")
+        return where[order].astype(np.int64)
 
     @property
     def trains(self) -> int:
@@ -182,6 +192,8 @@ def mrf_events(flip_deg: Any, TR_ms: Any, TI_ms: Any = 0.0, phases_deg: Any = 0.
         action=action_all,
         output_index=output_index,
         time_us=clock_t.to(torch.float32).numpy()[recorded],
+        repetitions=repetitions,
+        echo=np.zeros(n, bool),
     )
 
 
@@ -286,6 +298,7 @@ def fse_events(flip_deg: Any, ESP_ms: float, phases_deg: Any = 0.0, exc_flip: fl
         action=action,
         output_index=output_index,
         time_us=clock_t.to(torch.float32).numpy()[recorded],
+        echo=np.ones(n, bool),
     )
 
 

@@ -17,14 +17,15 @@ kernel pass together with the signal.
 from __future__ import annotations
 
 from collections.abc import Sequence
+from dataclasses import dataclass
 from typing import Any
 
 import numpy as np
 import torch
 
 from . import engine
-from .sequence import (PackedEvents, fse_events, mrf_events, mrf_gradient_map, played_flip_torch,
-                       program_for)
+from .sequence import (POST_SHIFT, PRE_SHIFT, SHIFT_AFTER, PackedEvents, fse_events, mrf_events,
+                       mrf_gradient_map, played_flip_torch, program_for)
 
 
 def _tensorish(value: Any) -> bool:
@@ -348,3 +349,100 @@ def fse_sim(flip, ESP: float, T1, T2, phases=0.0, TR=1e6, exc_flip: float = 90.0
         return model.simulate(**values)
     return model.jacobian(diff, **values)
 
+
+
+# ---- the direct route: a packed stream on the fused kernels ----------------
+
+
+@dataclass
+class SimulationResult:
+    """What one :meth:`EpgEngine.simulate` recorded (``sequence/_simulation.py:
+    239-264``): ``signal`` ``(*voxels, samples)`` complex64 and, per sample,
+    ``time_us``, ``event_index`` (the recording event of the stream),
+    ``repetition`` (the playing it belongs to) and ``echo`` (a spin echo)."""
+
+    signal: torch.Tensor
+    time_us: torch.Tensor
+    event_index: torch.Tensor
+    repetition: torch.Tensor
+    echo: torch.Tensor
+
+
+_WINDING = PRE_SHIFT | POST_SHIFT | SHIFT_AFTER
+_RECORD_MODES = ("all", "acquired", "echo")
+
+
+class EpgEngine:
+    """Runs a packed event stream on the fused EPG kernels: the role of the
+    reference's ``EpgEngine`` (``sequence/_simulation.py:267-484``) for a
+    stream a builder (:func:`mrf_events`, :func:`fse_events`) produced.
+    Tissue is a mapping of ``T1``, ``T2`` (required), ``M0``, ``B1``,
+    ``inv_efficiency``; shapes broadcast to the voxel batch."""
+
+    def shifts_per_repetition(self, events: PackedEvents) -> int:
+        """How far one playing winds the states (gradient actions counted
+        once per bit, ``_simulation.py:284-295``)."""
+        per_playing = events.events // max(events.repetitions, 1)
+        bits = events.action[:per_playing] & _WINDING
+        return int(sum(bin(int(b)).count("1") for b in bits))
+
+    def simulate(self, events: PackedEvents, tissue: dict[str, Any], *, repetitions: int = 1,
+                 record: str = "all", nstates: int | None = None,
+                 device: str | torch.device | None = None) -> SimulationResult:
+        """Simulate ``events`` for ``tissue`` and record its samples.
+
+        ``record``: ``"all"`` and ``"acquired"`` keep every sample the stream
+        records; ``"echo"`` keeps the spin echoes. ``nstates`` defaults to
+        ``max(8, min(64, 1 + winding))`` over the stream's playings. A packed
+        stream already carries its playings, so ``repetitions`` must be 1 (a
+        builder takes ``repetitions=k``)."""
+        if int(repetitions) != 1:
+            raise ValueError("a packed stream carries its playings: build it with repetitions=k")
+        if record not in _RECORD_MODES:
+            raise ValueError("record must be 'all', 'acquired', or 'echo'")
+        for required in ("T1", "T2"):
+            if required not in tissue:
+                raise ValueError(f"{required} is required")
+        if nstates is None:
+            winding = events.repetitions * self.shifts_per_repetition(events)
+            nstates = max(8, min(64, 1 + winding))
+        nstates = int(nstates)
+        if nstates < 1:
+            raise ValueError("nstates must be positive")
+        if events.real_axis() != 1:
+            raise NotImplementedError(
+                "only the real-subspace path is built on this accelerator: every RF pulse and "
+                "recorded sample must share one phase")
+        held = {k: tissue.get(k) for k in ("T1", "T2", "M0", "B1", "inv_efficiency")}
+        held = {k: v for k, v in held.items() if v is not None}
+        home = _home(held)
+        dev = engine.require_cuda(torch.device(device) if device is not None else
+                                  (home if home.type == "cuda" else None))
+        batch = _batch(held)
+        voxels = _numel(batch)
+
+        def declared(key):
+            value = held.get(key)
+            if value is None or (not _tensorish(value) and float(value) == 1.0):
+                return None
+            return value
+
+        with torch.cuda.device(dev):
+            maps = engine.tissue_maps(dev, voxels, held["T1"], held["T2"], declared("M0"),
+                                      declared("B1"), declared("inv_efficiency"))
+            signal = engine.forward(program_for(events, dev), maps, nstates)
+        signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
+        outputs = events.outputs
+        echo = events.echo if events.echo is not None else np.zeros(outputs, bool)
+        keep = np.arange(outputs) if record != "echo" else np.flatnonzero(echo[:outputs])
+        labels = dict(
+            time_us=torch.from_numpy(events.time_us[keep].astype(np.float32)),
+            event_index=torch.from_numpy(events.sample_events()[keep]),
+            repetition=torch.full((keep.size,), events.repetitions - 1, dtype=torch.int64),
+            echo=torch.from_numpy(echo[keep].copy()),
+        )
+        if record == "echo":
+            signal = signal[..., torch.from_numpy(keep).to(signal.device)]
+        if home.type != "cuda":
+            signal = signal.to(home)
+        return SimulationResult(signal=signal, **{k: v.to(signal.device) for k, v in labels.items()})
