@@ -70,6 +70,14 @@ typedef struct {
     const float* inversion;
 } tsg_tissue;
 
+/* Per-voxel transmit phase (radians) and off-resonance (Hz) of the complex
+ * path; each nullable (zero), the reference's B1phase and B0 buffers
+ * (sequence/_parameters.py:234-241). */
+typedef struct {
+    const float* b1_phase_rad;
+    const float* b0_hz;
+} tsg_offaxis;
+
 /* One general forward-mode direction (DEVICE pointers, all nullable):
  * per atom t1/t2/m0/b1/inversion, per (train, event) duration/flip. The
  * same directions simulate_real_jvp_range follows (_epg_cpu.cpp:3136-3285). */
@@ -144,6 +152,14 @@ int tsg_program_create(const float* duration_s, const int32_t* kind, const float
                        const uint8_t* action, const int32_t* output_index,
                        int64_t train_count, int64_t event_count, int unmerged,
                        const float* duration_tangent, tsg_program** out);
+/* The same compilation keeping each event's phase (train_count*event_count,
+ * radians): the program then also serves tsg_epg_forward_complex. Replaces
+ * the phase buffer the reference's complex kernel reads per event
+ * (_epg_cpu.cpp:4513-4532). */
+int tsg_program_create_phased(const float* duration_s, const int32_t* kind, const float* flip_rad,
+                              const float* phase_rad, const uint8_t* action,
+                              const int32_t* output_index, int64_t train_count,
+                              int64_t event_count, tsg_program** out);
 int tsg_program_destroy(tsg_program* program);
 /* The same compilation on the host only, for inspection: writes the op
  * count per train, the output count and up to `capacity` ops (all trains,
@@ -161,6 +177,18 @@ int tsg_program_info(const tsg_program* program, int64_t* train_count, int64_t* 
                      int64_t* output_count, int64_t* event_count);
 
 /* ---- device-resident kernels ------------------------------------------- */
+
+/* Complex forward (one pool, instant RF): RF and receiver phases of the
+ * events, per-voxel transmit phase and off-resonance. Replaces the complex
+ * kernel simulate_range<INSTANT, ONE> (_epg_cpu.cpp:4216-4566) that
+ * _epg_cpu.simulate runs when real_axis != 1 (_epg_cpu.cpp:10860-10900).
+ * `program` must come from tsg_program_create_phased. Outputs as for
+ * tsg_epg_forward: PLANES = the reference's (real, imag) planes of the
+ * recorded sample, COMPLEX_IJ = 1j times it, COMPLEX = it interleaved. */
+int tsg_epg_forward_complex(const tsg_program* program, const tsg_tissue* tissue,
+                            const tsg_offaxis* offaxis, int64_t atom_count, int64_t state_count,
+                            int layout, float* out_a, float* out_b, const tsg_launch* launch,
+                            void* stream);
 
 /* Forward. Signal layout (train, atom, output); see TSG_LAYOUT_*. For
  * TSG_LAYOUT_PLANES out_b is the imaginary plane; for COMPLEX_IJ out_b is

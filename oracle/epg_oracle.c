@@ -20,16 +20,24 @@
  *   run_forward           simulate_real_range              3041-3128
  *   run_tangent           simulate_real_jvp_range          3136-3285
  *   run_adjoint           simulate_real_vjp_range          5985-6232
+ *   run_forward_complex   simulate_range<INSTANT, ONE>     4216-4566
+ *                         with shift 2164-2174, rotate 2176-2208
  * Action bits are the packed action word (_epg_cpu.cpp:36-41,
  * sequence/_accelerators.py:77-84). Event kinds: 0 wait, 1 RF, 2 ADC
  * (sequence/_description.py:31-36). The work range enumerates (train, atom)
  * train-major and the output row of a work item is (train*atoms+atom)
  * (_epg_cpu.cpp:278-296).
  *
- * Out of scope, as in the real-subspace kernels: diffusion damping, flow,
- * pools, shaped/dynamic RF, off-resonance and RF phase (which leave the real
- * subspace). Null tissue pointers stand for the identity value (m0 = b1 =
- * inversion efficiency = 1), as the reference's feature mask does.
+ * The complex forward covers what leaves the real subspace on one pool with
+ * instant RF: RF and receiver phases, a transmit phase (B1phase) and
+ * off-resonance (B0) per voxel. Complex products are written out as
+ * std::complex<float> evaluates them (re = ac - bd, im = ad + bc, each
+ * product rounded, no contraction), so the FP32 port reproduces the
+ * reference's complex kernel too.
+ *
+ * Out of scope: diffusion damping, flow, pools, shaped/dynamic RF. Null
+ * tissue pointers stand for the identity value (m0 = b1 = inversion
+ * efficiency = 1, B1phase = B0 = 0), as the reference's feature mask does.
  */
 #include <math.h>
 #include <pthread.h>
@@ -438,11 +446,161 @@ static void run_adjoint(const oracle_case* c, const float* seed_imag,
     free(traj);
 }
 
+/* ---- the complex path (one pool, instant RF) ---------------------------- */
+
+/* Per-event RF / receiver phase (train_count*event_count) and the per-voxel
+ * transmit phase and off-resonance; each nullable (zero). */
+typedef struct {
+    const float* phase_rad;
+    const float* b1_phase_rad;
+    const float* b0_hz;
+} oracle_offaxis;
+
+typedef struct {
+    REAL re, im;
+} cplx;
+
+static inline cplx cmul(cplx a, cplx b) {
+    const REAL ac = a.re * b.re, bd = a.im * b.im, ad = a.re * b.im, bc = a.im * b.re;
+    cplx r = {ac - bd, ad + bc};
+    return r;
+}
+static inline cplx cadd(cplx a, cplx b) {
+    cplx r = {a.re + b.re, a.im + b.im};
+    return r;
+}
+static inline cplx cscale(REAL s, cplx a) {
+    cplx r = {s * a.re, s * a.im};
+    return r;
+}
+static inline cplx cconj(cplx a) {
+    cplx r = {a.re, -a.im};
+    return r;
+}
+static inline cplx cpolar(REAL rho, REAL theta) {
+    cplx r = {rho * COS(theta), rho * SIN(theta)};
+    return r;
+}
+
+/* F- takes order k+1, F+ takes order k-1, the top F- order is lost and
+ * F+[0] is the conjugate of the new F-[0] (_epg_cpu.cpp:2164-2174). */
+static void shift_complex(cplx* plus, cplx* minus, int64_t states) {
+    for (int64_t s = 0; s + 1 < states; ++s) minus[s] = minus[s + 1];
+    const cplx zero = {LIT(0.0), LIT(0.0)};
+    minus[states - 1] = zero;
+    for (int64_t s = states - 1; s > 0; --s) plus[s] = plus[s - 1];
+    plus[0] = cconj(minus[0]);
+}
+
+/* The pulse's 3x3 transition with flip alpha and phase phi
+ * (_epg_cpu.cpp:2176-2208). */
+static void rotate_complex(cplx* plus, cplx* minus, cplx* lon, int64_t states, REAL alpha,
+                           REAL phi) {
+    const REAL cosine = COS(alpha);
+    const REAL sine = SIN(alpha);
+    const REAL chs = LIT(0.5) * (LIT(1.0) + cosine);
+    const REAL shs = LIT(0.5) * (LIT(1.0) - cosine);
+    const cplx one = cpolar(LIT(1.0), phi);
+    const cplx two = cmul(one, one);
+    const cplx t00 = {chs, LIT(0.0)};
+    const cplx t01 = cscale(shs, two);
+    const cplx mis = {LIT(0.0), -sine}, pis = {LIT(0.0), sine};
+    const cplx mhs = {LIT(0.0), -(LIT(0.5) * sine)}, phs = {LIT(0.0), LIT(0.5) * sine};
+    const cplx t02 = cmul(mis, one);
+    const cplx t10 = cconj(t01);
+    const cplx t11 = t00;
+    const cplx t12 = cmul(pis, cconj(one));
+    const cplx t20 = cmul(mhs, cconj(one));
+    const cplx t21 = cmul(phs, one);
+    const cplx t22 = {cosine, LIT(0.0)};
+    for (int64_t s = 0; s < states; ++s) {
+        const cplx fp = plus[s], fm = minus[s], z = lon[s];
+        plus[s] = cadd(cadd(cmul(t00, fp), cmul(t01, fm)), cmul(t02, z));
+        minus[s] = cadd(cadd(cmul(t10, fp), cmul(t11, fm)), cmul(t12, z));
+        lon[s] = cadd(cadd(cmul(t20, fp), cmul(t21, fm)), cmul(t22, z));
+    }
+}
+
+/* Complex forward over work items [begin, end): both output planes are the
+ * recorded m0 * F+[0] demodulated by the receiver phase. */
+static void run_forward_complex(const oracle_case* c, const oracle_offaxis* o, int64_t begin,
+                                int64_t end, REAL* out_real, REAL* out_imag) {
+    const int64_t S = c->state_count;
+    cplx* plus = (cplx*)calloc((size_t)(3 * S), sizeof(cplx));
+    cplx* minus = plus + S;
+    cplx* lon = minus + S;
+    const int off_axis = o->b0_hz != NULL || o->b1_phase_rad != NULL;
+#if defined(REAL_IS_FLOAT)
+    const REAL pi = 3.14159265358979323846F;
+#else
+    const REAL pi = 3.14159265358979323846;
+#endif
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / c->atom_count;
+        const int64_t atom = work % c->atom_count;
+        const float* duration = c->duration_s + train * c->event_count;
+        const float* flip = c->flip_rad + train * c->event_count;
+        const float* phase = o->phase_rad ? o->phase_rad + train * c->event_count : NULL;
+        const int64_t out_base = (train * c->atom_count + atom) * c->output_count;
+        memset(plus, 0, sizeof(cplx) * (size_t)(3 * S));
+        lon[0].re = LIT(1.0);
+        const REAL r1 = LIT(1000.0) / (REAL)c->t1_ms[atom];
+        const REAL r2 = LIT(1000.0) / (REAL)c->t2_ms[atom];
+        const REAL b1 = tissue(c->b1, atom, LIT(1.0));
+        const REAL m0 = tissue(c->m0, atom, LIT(1.0));
+        const REAL eff = tissue(c->inversion, atom, LIT(1.0));
+        const REAL b1_phase = tissue(o->b1_phase_rad, atom, LIT(0.0));
+        const REAL b0 = tissue(o->b0_hz, atom, LIT(0.0));
+        for (int64_t e = 0; e < c->event_count; ++e) {
+            const REAL dt = (REAL)duration[e];
+            const REAL e1 = EXP(-r1 * dt);
+            const REAL e2 = EXP(-r2 * dt);
+            const REAL off = off_axis ? -LIT(2.0) * pi * b0 * dt : LIT(0.0);
+            cplx transverse = {e2, LIT(0.0)};
+            if (off_axis) transverse = cpolar(e2, off);
+            const cplx along = {e1, LIT(0.0)};
+            for (int64_t s = 0; s < S; ++s) {
+                plus[s] = cmul(plus[s], transverse);
+                minus[s] = cmul(minus[s], cconj(transverse));
+                lon[s] = cmul(lon[s], along);
+            }
+            lon[0].re += LIT(1.0) - e1;
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) shift_complex(plus, minus, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    const REAL f = -eff;
+                    for (int64_t s = 0; s < S; ++s) lon[s] = cscale(f, lon[s]);
+                } else {
+                    const REAL theta = (REAL)flip[e] * b1;
+                    const REAL phi = (phase ? (REAL)phase[e] : LIT(0.0)) + b1_phase;
+                    rotate_complex(plus, minus, lon, S, theta, phi);
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                const int64_t idx = out_base + c->output_index[e];
+                const cplx demod = cpolar(LIT(1.0), -(phase ? (REAL)phase[e] : LIT(0.0)));
+                const cplx v = cmul(cscale(m0, plus[0]), demod);
+                out_real[idx] = v.re;
+                out_imag[idx] = v.im;
+            }
+            if (a & A_POST_SHIFT) shift_complex(plus, minus, S);
+            if (a & A_SPOIL_AFTER) {
+                const cplx zero = {LIT(0.0), LIT(0.0)};
+                for (int64_t s = 0; s < S; ++s) plus[s] = minus[s] = zero;
+            } else if (a & A_SHIFT_AFTER) {
+                shift_complex(plus, minus, S);
+            }
+        }
+    }
+    free(plus);
+}
+
 /* ---- threaded drivers -------------------------------------------------- */
 
 typedef struct {
     const oracle_case* c;
     const oracle_direction* d;
+    const oracle_offaxis* o;
     int64_t begin, end;
     REAL* out_real;
     REAL* out_imag;
@@ -460,9 +618,23 @@ static void* tangent_job(void* p) {
     return NULL;
 }
 
+static void* complex_job(void* p) {
+    job* j = (job*)p;
+    run_forward_complex(j->c, j->o, j->begin, j->end, j->out_real, j->out_imag);
+    return NULL;
+}
+
+static void run_threads_o(void* (*fn)(void*), const oracle_case* c, const oracle_direction* d,
+                          const oracle_offaxis* o, REAL* out_real, REAL* out_imag, int threads);
+
 static void run_threads(void* (*fn)(void*), const oracle_case* c,
                         const oracle_direction* d, REAL* out_real, REAL* out_imag,
                         int threads) {
+    run_threads_o(fn, c, d, NULL, out_real, out_imag, threads);
+}
+
+static void run_threads_o(void* (*fn)(void*), const oracle_case* c, const oracle_direction* d,
+                          const oracle_offaxis* o, REAL* out_real, REAL* out_imag, int threads) {
     const int64_t work = c->atom_count * c->train_count;
     if (threads < 1) threads = 1;
     if (threads > 256) threads = 256;
@@ -473,6 +645,7 @@ static void run_threads(void* (*fn)(void*), const oracle_case* c,
     for (int t = 0; t < threads; ++t) {
         jobs[t].c = c;
         jobs[t].d = d;
+        jobs[t].o = o;
         jobs[t].begin = t * block < work ? t * block : work;
         jobs[t].end = (t + 1) * block < work ? (t + 1) * block : work;
         jobs[t].out_real = out_real;
@@ -495,6 +668,11 @@ void NAME(oracle_forward)(const oracle_case* c, REAL* out_real, REAL* out_imag,
 void NAME(oracle_tangent)(const oracle_case* c, const oracle_direction* d,
                           REAL* out_real, REAL* out_imag, int threads) {
     run_threads(tangent_job, c, d, out_real, out_imag, threads);
+}
+
+void NAME(oracle_forward_complex)(const oracle_case* c, const oracle_offaxis* o,
+                                  REAL* out_real, REAL* out_imag, int threads) {
+    run_threads_o(complex_job, c, NULL, o, out_real, out_imag, threads);
 }
 
 /* Single-threaded adjoint; gradient arrays must be zeroed by the caller. */

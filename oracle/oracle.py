@@ -46,6 +46,14 @@ class _Case(ctypes.Structure):
     ]
 
 
+class _Offaxis(ctypes.Structure):
+    _fields_ = [
+        ("phase_rad", ctypes.c_void_p),
+        ("b1_phase_rad", ctypes.c_void_p),
+        ("b0_hz", ctypes.c_void_p),
+    ]
+
+
 class _Direction(ctypes.Structure):
     _fields_ = [
         ("t1_ms", ctypes.c_void_p),
@@ -91,6 +99,11 @@ class Packed:
     m0: np.ndarray | None = None
     b1: np.ndarray | None = None
     inversion: np.ndarray | None = None
+    # The complex path only: per-event RF / receiver phase ((events,) or
+    # (trains, events)) and per-voxel transmit phase and off-resonance.
+    phase_rad: np.ndarray | None = None
+    b1_phase_rad: np.ndarray | None = None
+    b0_hz: np.ndarray | None = None
 
     @property
     def atom_count(self) -> int:
@@ -169,6 +182,31 @@ def forward(p: Packed, precision: str = "f64", threads: int = 1) -> np.ndarray:
     fn(ctypes.byref(c), ctypes.c_void_p(real.ctypes.data), ctypes.c_void_p(imag.ctypes.data),
        ctypes.c_int(threads))
     return imag
+
+
+def forward_complex(p: Packed, precision: str = "f64", threads: int = 1) -> np.ndarray:
+    """Recorded samples, complex: ``m0 * F+[0]`` demodulated by the receiver
+    phase, on the complex path (``simulate_range<INSTANT, ONE>``,
+    src/torchsim/_epg_cpu.cpp:4216-4566)."""
+    dtype, _ = _dtype(precision)
+    keep: list = []
+    c = _case(p, keep)
+    arrays = {
+        "phase_rad": None if p.phase_rad is None else _f32(
+            np.broadcast_to(p.phase_rad, (p.train_count, p.event_count))),
+        "b1_phase_rad": _f32(p.b1_phase_rad),
+        "b0_hz": _f32(p.b0_hz),
+    }
+    keep.append(arrays)
+    o = _Offaxis()
+    for name, value in arrays.items():
+        setattr(o, name, _ptr(value))
+    real = np.zeros(_shape(p), dtype=dtype)
+    imag = np.zeros(_shape(p), dtype=dtype)
+    fn = getattr(_library(), f"oracle_forward_complex_{precision}")
+    fn(ctypes.byref(c), ctypes.byref(o), ctypes.c_void_p(real.ctypes.data),
+       ctypes.c_void_p(imag.ctypes.data), ctypes.c_int(threads))
+    return real + 1j * imag
 
 
 def tangent(p: Packed, precision: str = "f64", threads: int = 1, **direction) -> np.ndarray:

@@ -3,7 +3,7 @@
 Run in a container that has the reference checkout (default /root/reference)
 and a C++ compiler:
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [CASE ...]
 
 It builds the reference's own CPU kernel with ``oracle/build_ref.sh``, imports
 the reference's Python package from a temporary copy, runs its public calls
@@ -226,6 +226,60 @@ def case_fse(ts, rec) -> dict:
     return out
 
 
+def case_fse_phase0(ts, rec) -> dict:
+    """Default-phase CPMG (refocusing at 0 deg, excitation at 90 deg): the
+    reference leaves the real subspace and runs its complex kernel."""
+    import torch
+    from torchsim.simulators import FSESimulator
+
+    rng = np.random.default_rng(5)
+    n, etl = 6, 10
+    t1 = rng.uniform(300, 3000, n).astype(np.float32)
+    t2 = rng.uniform(10, 300, n).astype(np.float32)
+    b1 = rng.uniform(0.7, 1.3, n).astype(np.float32)
+    flip = rng.uniform(100, 180, etl).astype(np.float32)
+    esp = 9.0
+    sim = FSESimulator(flip=torch.from_numpy(flip), ESP=esp, states=2 * etl)
+    rec.clear()
+    sig = sim.simulate(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2), B1=torch.from_numpy(b1))
+    fwd = [c for c in rec.calls if c["route"] == "_run_packed"][0]
+    out = {"flip_deg": flip, "esp_ms": np.float32(esp), "t1": t1, "t2": t2, "b1": b1,
+           "states": np.int64(2 * etl), "signal": _np(sig)}
+    out.update(_packed(fwd, ""))
+    out["real_axis"] = np.int64(rec.axis(fwd))
+    out["raw_forward"] = _np(fwd["result"])
+    return out
+
+
+def case_mrf_offaxis(ts, rec) -> dict:
+    """MRF with off-resonance (B0) and a transmit phase (B1phase) per voxel:
+    the complex kernel with phase turns in the relaxation and the pulses."""
+    import torch
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(6)
+    n, pulses = 8, 60
+    t1, t2, b1 = draw_tissue(rng, n)
+    b0 = rng.uniform(-40, 40, n).astype(np.float32)
+    b1p = rng.uniform(-0.5, 0.5, n).astype(np.float32)
+    m0 = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    sim = MRFSimulator(flip=torch.from_numpy(flip), TR=torch.from_numpy(tr), TI=15.0, states=12)
+    rec.clear()
+    sig = sim.simulate(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2), B1=torch.from_numpy(b1),
+                       B0=torch.from_numpy(b0), B1phase=torch.from_numpy(b1p),
+                       M0=torch.from_numpy(m0))
+    fwd = [c for c in rec.calls if c["route"] == "_run_packed"][0]
+    out = {"flip_deg": flip, "tr_ms": tr, "ti_ms": np.float32(15.0), "t1": t1, "t2": t2,
+           "b1": b1, "b0": b0, "b1_phase": b1p, "m0": m0, "states": np.int64(12),
+           "signal": _np(sig)}
+    out.update(_packed(fwd, ""))
+    out["real_axis"] = np.int64(rec.axis(fwd))
+    out["raw_forward"] = _np(fwd["result"])
+    return out
+
+
 def case_adjoint(ts, rec) -> dict:
     import torch
     from torchsim.simulators import MRFSimulator
@@ -298,8 +352,13 @@ def case_gn(ts, rec) -> dict:
             "unconverged": np.int64(est.unconverged)}
 
 
+CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis")
+
+
 def main() -> None:
-    root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = sys.argv[1:]
+    root = Path(args[0] if args and not args[0] in CASES else "/root/reference")
+    wanted = [a for a in args if a in CASES] or list(CASES)
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     ts = _import_reference(root)
     import torch
@@ -313,7 +372,10 @@ def main() -> None:
     _accelerators.detection = lambda kind, device: 0.0
     rec = _Recorder(_accelerators)
     for name, fn in (("mrf880", case_mrf880), ("mrf_prep", case_mrf_prep),
-                     ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn)):
+                     ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn),
+                     ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis)):
+        if name not in wanted:
+            continue
         data = fn(ts, rec)
         np.savez_compressed(HERE / f"{name}.npz", **data)
         print(f"wrote {name}.npz with {len(data)} arrays")

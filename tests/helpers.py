@@ -41,6 +41,16 @@ def packed_from_golden(d, prefix: str = "") -> O.Packed:
         inversion=d[prefix + "tissue_inversion_efficiency"])
 
 
+def packed_complex_from_golden(d, prefix: str = "") -> O.Packed:
+    """The packed inputs of a complex-path fixture: the real-path buffers plus
+    the event phases and the per-voxel transmit phase and off-resonance."""
+    p = packed_from_golden(d, prefix)
+    p.phase_rad = d[prefix + "event_phase"]
+    p.b1_phase_rad = d[prefix + "tissue_b1_phase_rad"]
+    p.b0_hz = d[prefix + "tissue_b0_hz"]
+    return p
+
+
 def max_rel(actual, expected) -> float:
     """max |a - e| / max |e|, the normalisation of the reference's CUDA parity
     tests (tests/sequence/test_cuda_parity.py:137-138)."""

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.helpers import max_rel, packed_from_golden
+from tests.helpers import max_rel, packed_complex_from_golden, packed_from_golden
 
 FORWARD_CASES = ["mrf880", "mrf_prep", "fse_cpmg"]
 KEYS = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1", "M0": "m0", "inv_efficiency": "inversion"}
@@ -91,3 +91,40 @@ def test_oracle_planted_mistake_is_caught(golden):
     p.state_count = 9  # truncating one order early changes the answer
     out = O.forward(p, "f64")
     assert max_rel(out, d["raw_forward"].imag) > 1e-5
+
+
+# ---- the complex path (RF phases, B0, B1phase) -------------------------------
+
+
+@pytest.mark.parametrize("name", ["fse_phase0", "mrf_offaxis"])
+def test_complex_fp32_port_is_bitwise_the_reference_kernel(golden, name):
+    d = golden(name)
+    assert int(d["real_axis"]) == -1  # the reference ran its complex kernel
+    got = O.forward_complex(packed_complex_from_golden(d), "f32").astype(np.complex64)
+    assert np.array_equal(got, d["raw_forward"])
+
+
+@pytest.mark.parametrize("name", ["fse_phase0", "mrf_offaxis"])
+def test_complex_fp64_oracle_matches_reference(golden, name):
+    d = golden(name)
+    got = O.forward_complex(packed_complex_from_golden(d), "f64")
+    assert max_rel(got, d["raw_forward"]) <= 2e-6
+
+
+def test_complex_public_mrf_signal_is_1j_raw(golden):
+    d = golden("mrf_offaxis")
+    raw = d["raw_forward"]
+    assert np.array_equal(d["signal"], (1j * raw).astype(np.complex64))
+
+
+def test_complex_oracle_reduces_to_the_real_one(golden):
+    """With every phase at 90 degrees and no B0 or B1phase the complex
+    recursion is the real one: the recorded sample is i * (real plane)."""
+    d = golden("fse_cpmg")
+    p = packed_complex_from_golden(d)
+    p.b1_phase_rad = None
+    p.b0_hz = None
+    full = O.forward_complex(p, "f64")
+    real = O.forward(packed_from_golden(d), "f64")
+    assert max_rel(full.imag, real) <= 1e-12
+    assert np.abs(full.real).max() <= 1e-12 * np.abs(real).max()

@@ -40,6 +40,10 @@ class Tissue(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("t1_ms", "t2_ms", "m0", "b1", "inversion")]
 
 
+class Offaxis(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("b1_phase_rad", "b0_hz")]
+
+
 class Direction(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in
                 ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s", "flip_rad")]
@@ -91,6 +95,8 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_probe_fp32x2": (_int, [_i64, _int, _int, _vp, _vp, ctypes.POINTER(ctypes.c_double)]),
     "tsg_program_create": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _int, _vp,
                                   ctypes.POINTER(_vp)]),
+    "tsg_program_create_phased": (_int, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64,
+                                         ctypes.POINTER(_vp)]),
     "tsg_program_destroy": (_int, [_vp]),
     "tsg_program_plan": (_int, [_vp, _vp, _vp, _vp, _vp, _i64, _i64, _int, _vp,
                                 ctypes.POINTER(_i64), ctypes.POINTER(_i64), _vp, _vp, _vp, _vp,
@@ -99,6 +105,8 @@ SIGNATURES: dict[str, tuple] = {
                                 ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "tsg_epg_forward": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _int, _vp, _vp,
                                ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_forward_complex": (_int, [_vp, ctypes.POINTER(Tissue), ctypes.POINTER(Offaxis), _i64,
+                                       _i64, _int, _vp, _vp, ctypes.POINTER(Launch), _vp]),
     "tsg_epg_forward_tangents": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.c_uint,
                                         ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, _int,
                                         _vp, _vp, _vp, _vp, ctypes.POINTER(Launch), _vp]),

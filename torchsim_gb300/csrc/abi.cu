@@ -166,19 +166,31 @@ using namespace tsg;
 
 extern "C" int tsg_version(void) { return 1; }
 
-extern "C" int tsg_program_create(const float* duration_s, const int32_t* kind,
-                                  const float* flip_rad, const uint8_t* action,
-                                  const int32_t* output_index, int64_t train_count,
-                                  int64_t event_count, int unmerged,
-                                  const float* duration_tangent, tsg_program** out) {
+namespace {
+
+int create_program(const float* duration_s, const int32_t* kind, const float* flip_rad,
+                   const float* phase_rad, const uint8_t* action, const int32_t* output_index,
+                   int64_t train_count, int64_t event_count, int unmerged,
+                   const float* duration_tangent, tsg_program** out) {
     if (!out) return fail(TSG_ERR_ARGUMENT, "null output handle");
     *out = nullptr;
     auto* prog = new tsg_program();
     int rc = compile_program(duration_s, kind, flip_rad, action, output_index, train_count,
-                             event_count, unmerged != 0, duration_tangent, &prog->host);
+                             event_count, unmerged != 0, duration_tangent, &prog->host, phase_rad);
     if (rc != TSG_OK) {
         delete prog;
         return rc;
+    }
+    if (!prog->host.phase.empty()) {
+        const size_t bytes = prog->host.phase.size() * sizeof(float2);
+        cudaError_t e = cudaMalloc(&prog->d_phase, bytes);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(prog->d_phase, prog->host.phase.data(), bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(prog->d_phase);
+            delete prog;
+            return cuda_fail(e, "cudaMemcpy(program phases)");
+        }
     }
     cudaGetDevice(&prog->device);
     const size_t n = prog->host.op.size();
@@ -198,12 +210,34 @@ extern "C" int tsg_program_create(const float* duration_s, const int32_t* kind,
         if (e3 != cudaSuccess || e4 != cudaSuccess) {
             cudaFree(prog->d_ops);
             cudaFree(prog->d_src);
+            cudaFree(prog->d_phase);
             delete prog;
             return cuda_fail(e3 != cudaSuccess ? e3 : e4, "cudaMemcpy(program)");
         }
     }
     *out = prog;
     return TSG_OK;
+}
+
+}  // namespace
+
+extern "C" int tsg_program_create(const float* duration_s, const int32_t* kind,
+                                  const float* flip_rad, const uint8_t* action,
+                                  const int32_t* output_index, int64_t train_count,
+                                  int64_t event_count, int unmerged,
+                                  const float* duration_tangent, tsg_program** out) {
+    return create_program(duration_s, kind, flip_rad, nullptr, action, output_index, train_count,
+                          event_count, unmerged, duration_tangent, out);
+}
+
+extern "C" int tsg_program_create_phased(const float* duration_s, const int32_t* kind,
+                                         const float* flip_rad, const float* phase_rad,
+                                         const uint8_t* action, const int32_t* output_index,
+                                         int64_t train_count, int64_t event_count,
+                                         tsg_program** out) {
+    if (!phase_rad && event_count > 0) return fail(TSG_ERR_ARGUMENT, "null phase buffer");
+    return create_program(duration_s, kind, flip_rad, phase_rad, action, output_index,
+                          train_count, event_count, 0, nullptr, out);
 }
 
 extern "C" int tsg_program_plan(const float* duration_s, const int32_t* kind,
@@ -233,6 +267,7 @@ extern "C" int tsg_program_destroy(tsg_program* program) {
     if (!program) return TSG_OK;
     cudaFree(program->d_ops);
     cudaFree(program->d_src);
+    cudaFree(program->d_phase);
     delete program;
     return TSG_OK;
 }

@@ -27,6 +27,8 @@ constexpr int SLOT_RELAX = 0, SLOT_SHIFT1 = 1, SLOT_RF = 2, SLOT_SHIFT2 = 3, SLO
 struct Builder {
     Op op{};
     OpSource src{-1, -1};
+    float2 ph{0.f, 0.f};  // phase of the op's pulse, of its receiver
+    std::vector<float2>* phases = nullptr;  // collected when event phases are given
     int pos = -1;  // last slot used; -1 = no op open
     int n[3] = {0, 0, 0};
 
@@ -36,8 +38,10 @@ struct Builder {
                    (uint32_t(n[2]) << OP_SHIFT3_SHIFT);
         ops.push_back(op);
         srcs.push_back(src);
+        if (phases) phases->push_back(ph);
         op = Op{};
         src = OpSource{-1, -1};
+        ph = float2{0.f, 0.f};
         pos = -1;
         n[0] = n[1] = n[2] = 0;
     }
@@ -72,7 +76,7 @@ struct Builder {
     }
 
     void place(Step s, float flip, int32_t record, int32_t event, std::vector<Op>& ops,
-               std::vector<OpSource>& srcs) {
+               std::vector<OpSource>& srcs, float phase = 0.f) {
         int slot = pos < 0 ? -1 : fit(s);
         if (slot < 0) {
             open(ops, srcs);
@@ -86,10 +90,12 @@ struct Builder {
                 op.code |= uint32_t(s == S_ROTATE ? RF_ROTATE : RF_INVERT) << OP_RF_SHIFT;
                 op.flip = s == S_ROTATE ? flip : 0.f;
                 src.rf_event = event;
+                if (s == S_ROTATE) ph.x = phase;
                 break;
             case SLOT_RECORD:
                 op.code |= OP_RECORD;
                 op.record = record;
+                ph.y = phase;
                 break;
             case SLOT_SPOIL1: op.code |= OP_SPOIL1; break;
             case SLOT_SPOIL2: op.code |= OP_SPOIL2; break;
@@ -104,7 +110,7 @@ struct Builder {
 int compile_program(const float* duration, const int32_t* kind, const float* flip,
                     const uint8_t* action, const int32_t* output_index, int64_t trains,
                     int64_t events, bool unmerged, const float* duration_tangent,
-                    HostProgram* out) {
+                    HostProgram* out, const float* phase) {
     if (trains < 1 || events < 0)
         return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
     if (events > 0 && (!duration || !kind || !flip || !action || !output_index))
@@ -121,11 +127,13 @@ int compile_program(const float* duration, const int32_t* kind, const float* fli
     }
     std::vector<std::vector<Op>> per_train(trains);
     std::vector<std::vector<OpSource>> per_src(trains);
+    std::vector<std::vector<float2>> per_phase(phase ? trains : 0);
     bool sequential = true;
     for (int64_t t = 0; t < trains; ++t) {
         auto& ops = per_train[t];
         auto& srcs = per_src[t];
         Builder b;
+        if (phase) b.phases = &per_phase[t];
         int32_t expected = 0;
         for (int64_t e = 0; e < events; ++e) {
             const int64_t te = t * events + e;
@@ -139,15 +147,16 @@ int compile_program(const float* duration, const int32_t* kind, const float* fli
                 b.src.dt_event = int32_t(e);
             }
             if (a & A_PRE_SHIFT) b.place(S_SHIFT, 0.f, 0, int32_t(e), ops, srcs);
+            const float pe = phase ? phase[te] : 0.f;
             if (kind[e] == 1) {
                 if (a & A_INVERSION)
                     b.place(S_INVERT, 0.f, 0, int32_t(e), ops, srcs);
                 else
-                    b.place(S_ROTATE, flip[te], 0, int32_t(e), ops, srcs);
+                    b.place(S_ROTATE, flip[te], 0, int32_t(e), ops, srcs, pe);
             } else if (kind[e] == 2 && (a & A_RECORD)) {
                 if (output_index[e] != expected) sequential = false;
                 expected = output_index[e] + 1;
-                b.place(S_RECORD, 0.f, output_index[e], int32_t(e), ops, srcs);
+                b.place(S_RECORD, 0.f, output_index[e], int32_t(e), ops, srcs, pe);
             }
             if (a & A_POST_SHIFT) b.place(S_SHIFT, 0.f, 0, int32_t(e), ops, srcs);
             if (a & A_SPOIL_AFTER)
@@ -170,6 +179,12 @@ int compile_program(const float* duration, const int32_t* kind, const float* fli
     for (int64_t t = 0; t < trains; ++t) {
         std::copy(per_train[t].begin(), per_train[t].end(), out->op.begin() + t * longest);
         std::copy(per_src[t].begin(), per_src[t].end(), out->src.begin() + t * longest);
+    }
+    out->phase.clear();
+    if (phase) {
+        out->phase.assign(size_t(trains) * longest, float2{0.f, 0.f});
+        for (int64_t t = 0; t < trains; ++t)
+            std::copy(per_phase[t].begin(), per_phase[t].end(), out->phase.begin() + t * longest);
     }
     return TSG_OK;
 }

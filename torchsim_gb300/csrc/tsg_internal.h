@@ -62,6 +62,9 @@ struct HostProgram {
     bool sequential_records = true;  // records appear as 0,1,2,... in op order
     std::vector<Op> op;              // [train][ops]
     std::vector<OpSource> src;       // [train][ops]
+    // With event phases (the complex path): per op the phase of its pulse
+    // and of its receiver, [train][ops] (radians; 0 where absent).
+    std::vector<float2> phase;
 };
 
 }  // namespace tsg
@@ -70,6 +73,7 @@ struct tsg_program {
     tsg::HostProgram host;
     tsg::Op* d_ops = nullptr;
     tsg::OpSource* d_src = nullptr;
+    float2* d_phase = nullptr;  // null unless built with event phases
     int device = 0;
 };
 
@@ -87,7 +91,7 @@ int cuda_fail(cudaError_t err, const char* where);
 int compile_program(const float* duration, const int32_t* kind, const float* flip,
                     const uint8_t* action, const int32_t* output_index, int64_t trains,
                     int64_t events, bool unmerged, const float* duration_tangent,
-                    HostProgram* out);
+                    HostProgram* out, const float* phase = nullptr);
 
 // Arguments of one sweep launch (forward, fused tangents, general tangent).
 struct SweepArgs {

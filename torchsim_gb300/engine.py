@@ -13,6 +13,7 @@ import ctypes
 from collections.abc import Sequence
 from dataclasses import dataclass
 
+import numpy as np
 import torch
 
 from . import _native
@@ -112,6 +113,43 @@ def forward(program: Program, tissue: TissueMaps, states: int, *, planes: bool =
                                       _native.LAYOUT_COMPLEX_IJ, res.data_ptr(), None,
                                       _native.launch_shape(launch), _stream()))
     return res
+
+
+def offaxis_maps(device: torch.device, voxels: int, B1phase=None, B0=None):
+    """(struct, tensors) of the per-voxel transmit phase (rad) and
+    off-resonance (Hz) for the complex kernel; absent maps stay null."""
+    keep = []
+
+    def flat(value):
+        if value is None:
+            return None
+        t = value if isinstance(value, torch.Tensor) else torch.as_tensor(
+            np.asarray(value, np.float32))
+        t = t.to(device=device, dtype=torch.float32).reshape(-1)
+        t = (t.expand(voxels) if t.numel() == 1 else t).contiguous()
+        if t.numel() != voxels:
+            raise ValueError(f"expected {voxels} values, got {t.numel()}")
+        keep.append(t)
+        return t.data_ptr()
+
+    return _native.Offaxis(flat(B1phase), flat(B0)), keep
+
+
+def forward_complex(program: Program, tissue: TissueMaps, states: int, offaxis=None, *,
+                    out: torch.Tensor | None = None, launch=None) -> torch.Tensor:
+    """Complex-path forward (RF / receiver phases, B1phase, B0): complex64
+    ``(trains*voxels, outputs)`` holding ``1j * m0 F+[0] e^{-i phase}``."""
+    if not program.phased:
+        raise ValueError("the complex kernel needs a program built with its event phases")
+    if out is None:
+        out = torch.empty((program.trains * tissue.voxels, program.outputs), dtype=torch.complex64,
+                          device=tissue.t1.device)
+    t = tissue.struct()
+    off = offaxis if offaxis is not None else _native.Offaxis(None, None)
+    _native.check(_native.library().tsg_epg_forward_complex(
+        program.handle, ctypes.byref(t), ctypes.byref(off), tissue.voxels, states,
+        _native.LAYOUT_COMPLEX_IJ, out.data_ptr(), None, _native.launch_shape(launch), _stream()))
+    return out
 
 
 def plan_tangents(names: Sequence[str]) -> tuple[int, list[int]]:

@@ -91,9 +91,10 @@ class PackedEvents:
         recorded = self.output_index[self.output_index >= 0]
         return int(recorded.max()) + 1 if recorded.size else 0
 
-    def key(self) -> str:
+    def key(self, with_phase: bool = False) -> str:
         h = hashlib.sha1()
-        for a in (self.duration, self.kind, self.flip, self.action, self.output_index):
+        arrays = (self.duration, self.kind, self.flip, self.action, self.output_index)
+        for a in (*arrays, self.phase) if with_phase else arrays:
             h.update(np.ascontiguousarray(a).tobytes())
             h.update(str(a.shape).encode())
         return h.hexdigest()
@@ -303,12 +304,16 @@ def fse_events(flip_deg: Any, ESP_ms: float, phases_deg: Any = 0.0, exc_flip: fl
 
 
 class Program:
-    """A compiled pulse program resident on the current CUDA device."""
+    """A compiled pulse program resident on the current CUDA device.
+
+    ``phased`` keeps each event's phase in the program (per op: the phase of
+    its pulse and of its receiver), which the complex kernel needs."""
 
     def __init__(self, events: PackedEvents, unmerged: bool = False,
-                 duration_tangent: np.ndarray | None = None) -> None:
+                 duration_tangent: np.ndarray | None = None, phased: bool = False) -> None:
         lib = _native.library()
         self.events = events
+        self.phased = phased
         dur = np.ascontiguousarray(events.duration, np.float32)
         kind = np.ascontiguousarray(events.kind, np.int32)
         flip = np.ascontiguousarray(events.flip, np.float32)
@@ -317,10 +322,19 @@ class Program:
         tangent = None if duration_tangent is None else np.ascontiguousarray(
             np.broadcast_to(duration_tangent, dur.shape), np.float32)
         handle = _native.ctypes.c_void_p()
-        _native.check(lib.tsg_program_create(
-            dur.ctypes.data, kind.ctypes.data, flip.ctypes.data, action.ctypes.data,
-            oi.ctypes.data, events.trains, events.events, int(unmerged),
-            None if tangent is None else tangent.ctypes.data, _native.ctypes.byref(handle)))
+        if phased:
+            if unmerged or tangent is not None:
+                raise ValueError("a phased program is compiled merged, without a duration tangent")
+            phase = np.ascontiguousarray(np.broadcast_to(events.phase, dur.shape), np.float32)
+            _native.check(lib.tsg_program_create_phased(
+                dur.ctypes.data, kind.ctypes.data, flip.ctypes.data, phase.ctypes.data,
+                action.ctypes.data, oi.ctypes.data, events.trains, events.events,
+                _native.ctypes.byref(handle)))
+        else:
+            _native.check(lib.tsg_program_create(
+                dur.ctypes.data, kind.ctypes.data, flip.ctypes.data, action.ctypes.data,
+                oi.ctypes.data, events.trains, events.events, int(unmerged),
+                None if tangent is None else tangent.ctypes.data, _native.ctypes.byref(handle)))
         self.handle = handle
         i64 = _native.ctypes.c_int64
         trains, ops, outputs, nev = i64(), i64(), i64(), i64()
@@ -345,15 +359,17 @@ _cache: dict[tuple, Program] = {}
 _cache_lock = threading.Lock()
 
 
-def program_for(events: PackedEvents, device: torch.device | None = None) -> Program:
-    """The compiled program of a stream, cached by content and device."""
+def program_for(events: PackedEvents, device: torch.device | None = None,
+                phased: bool = False) -> Program:
+    """The compiled program of a stream, cached by content and device
+    (``phased``: with the event phases, for the complex kernel)."""
     device = device or torch.device("cuda", torch.cuda.current_device())
-    key = (events.key(), device.index)
+    key = (events.key(phased), device.index, phased)
     with _cache_lock:
         hit = _cache.get(key)
         if hit is None:
             with torch.cuda.device(device):
-                hit = Program(events)
+                hit = Program(events, phased=phased)
             if len(_cache) > 64:
                 _cache.pop(next(iter(_cache)))
             _cache[key] = hit

@@ -58,6 +58,22 @@ def _home(values: dict[str, Any]) -> torch.device:
     return torch.device("cpu")
 
 
+def _nonzero(value: Any) -> bool:
+    if value is None:
+        return False
+    if isinstance(value, torch.Tensor):
+        return bool(value.ne(0).any())
+    return bool(np.any(np.asarray(value) != 0))
+
+
+def _leaves_real_subspace(events: PackedEvents, held: dict[str, Any]) -> bool:
+    """True when the stream's pulses and samples do not share one phase, or a
+    voxel carries off-resonance or a transmit phase: the complex kernel runs
+    (the reference's real_axis verdict, sequence/_accelerators.py:1953-2128)."""
+    return (events.real_axis() != 1 or _nonzero(held.get("B0"))
+            or _nonzero(held.get("B1phase")))
+
+
 class _EpgSimulator:
     """Shared mechanics: split properties from protocol, run, reshape."""
 
@@ -78,6 +94,8 @@ class _EpgSimulator:
             "M0": held.get("M0"),
             "B1": held.get("B1"),
             "inv": held.get("inv_efficiency"),
+            "B0": held.get("B0"),
+            "B1phase": held.get("B1phase"),
         }
 
     def _post(self, signal, jacobian, names, held, protocol, device):
@@ -101,10 +119,11 @@ class _EpgSimulator:
         dev = engine.require_cuda(torch.device(device) if device is not None else
                                   (home if home.type == "cuda" else None))
         events = self.events(repetitions=repetitions, **protocol)
-        if events.real_axis() != 1:
+        complex_path = _leaves_real_subspace(events, held)
+        if complex_path and names:
             raise NotImplementedError(
-                "only the real-subspace path is built on this accelerator: every RF pulse and "
-                "recorded sample must share one phase")
+                "Jacobians on the complex path (RF phases, B0, B1phase) are not built; the "
+                "signal is")
         batch = _batch(held)
         voxels = _numel(batch)
         maps = self._kernel_maps(held)
@@ -127,6 +146,14 @@ class _EpgSimulator:
             tissue = engine.tissue_maps(dev, voxels, maps["T1"], maps["T2"],
                                         declared("M0", maps["M0"]), declared("B1", maps["B1"]),
                                         declared("inv", maps["inv"]))
+            if complex_path:
+                off, keep = engine.offaxis_maps(dev, voxels, maps.get("B1phase"), maps.get("B0"))
+                program = program_for(events, dev, phased=True)
+                signal = engine.forward_complex(program, tissue, states, off)
+                del keep
+                signal, _ = self._post(signal, None, None, held, protocol, dev)
+                signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
+                return (signal.to(home) if home.type != "cuda" else signal), None
             program = program_for(events, dev)
             kernel_names = self._kernel_names(names) if names else None
             if kernel_names:
@@ -172,8 +199,9 @@ class _EpgSimulator:
                                   (home if home.type == "cuda" else None))
         plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in protocol.items()}
         events = self.events(repetitions=repetitions, **plain)
-        if events.real_axis() != 1:
-            raise NotImplementedError("only the real-subspace path is built on this accelerator")
+        if _leaves_real_subspace(events, held):
+            raise NotImplementedError(
+                "gradients on the complex path (RF phases, B0, B1phase) are not built")
         batch = _batch(held)
         voxels = _numel(batch)
         maps = self._kernel_maps(held)
@@ -225,7 +253,8 @@ class MRFSimulator(_EpgSimulator):
     the last playing."""
 
     properties = {"T1": "t1_ms", "T2": "t2_ms", "M0": "m0", "B1": "b1",
-                  "inv_efficiency": "inversion_efficiency"}
+                  "inv_efficiency": "inversion_efficiency", "B0": "b0_hz",
+                  "B1phase": "b1_phase_rad"}
     states = 10
 
     def events(self, *, flip, TR, TI=0.0, phases=0.0, repetitions=1) -> PackedEvents:
@@ -265,7 +294,8 @@ class FSESimulator(_EpgSimulator):
     (``fse.py:110-133``); the Jacobian carries them through by the chain
     rule."""
 
-    properties = {"T1": "t1_ms", "T2": "t2_ms", "M0": None, "B1": "b1"}
+    properties = {"T1": "t1_ms", "T2": "t2_ms", "M0": None, "B1": "b1", "B0": "b0_hz",
+                  "B1phase": "b1_phase_rad"}
     states = 10
 
     def events(self, *, flip, ESP, phases=0.0, exc_flip=90.0, exc_phase=90.0, TR=1e6,
@@ -377,7 +407,9 @@ class EpgEngine:
     reference's ``EpgEngine`` (``sequence/_simulation.py:267-484``) for a
     stream a builder (:func:`mrf_events`, :func:`fse_events`) produced.
     Tissue is a mapping of ``T1``, ``T2`` (required), ``M0``, ``B1``,
-    ``inv_efficiency``; shapes broadcast to the voxel batch."""
+    ``inv_efficiency``, ``B0`` (Hz), ``B1phase`` (rad); shapes broadcast to the
+    voxel batch. Streams that leave the real subspace run the complex
+    kernel."""
 
     def shifts_per_repetition(self, events: PackedEvents) -> int:
         """How far one playing winds the states (gradient actions counted
@@ -409,12 +441,10 @@ class EpgEngine:
         nstates = int(nstates)
         if nstates < 1:
             raise ValueError("nstates must be positive")
-        if events.real_axis() != 1:
-            raise NotImplementedError(
-                "only the real-subspace path is built on this accelerator: every RF pulse and "
-                "recorded sample must share one phase")
-        held = {k: tissue.get(k) for k in ("T1", "T2", "M0", "B1", "inv_efficiency")}
+        held = {k: tissue.get(k) for k in ("T1", "T2", "M0", "B1", "inv_efficiency", "B0",
+                                           "B1phase")}
         held = {k: v for k, v in held.items() if v is not None}
+        complex_path = _leaves_real_subspace(events, held)
         home = _home(held)
         dev = engine.require_cuda(torch.device(device) if device is not None else
                                   (home if home.type == "cuda" else None))
@@ -430,7 +460,13 @@ class EpgEngine:
         with torch.cuda.device(dev):
             maps = engine.tissue_maps(dev, voxels, held["T1"], held["T2"], declared("M0"),
                                       declared("B1"), declared("inv_efficiency"))
-            signal = engine.forward(program_for(events, dev), maps, nstates)
+            if complex_path:
+                off, keep = engine.offaxis_maps(dev, voxels, held.get("B1phase"), held.get("B0"))
+                signal = engine.forward_complex(program_for(events, dev, phased=True), maps,
+                                                nstates, off)
+                del keep
+            else:
+                signal = engine.forward(program_for(events, dev), maps, nstates)
         signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
         outputs = events.outputs
         echo = events.echo if events.echo is not None else np.zeros(outputs, bool)
