@@ -383,7 +383,9 @@ int tsg_gn_natural(const double* free_variables, int64_t voxel_count, const tsg_
 
 /* _epg_cpu.simulate (src/torchsim/_epg_cpu.cpp:10740-10926): pointers holds
  * the 26 packed buffers, the two output planes and the 13 tail slots (41
- * entries, :10794). Synchronous. */
+ * entries, :10794). real_axis == 1 runs the real-subspace kernel; any other
+ * value the complex one (event phases, B1phase, B0), as the reference
+ * switches between simulate_real_range and simulate_range. Synchronous. */
 int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, int64_t atom_count,
                      int64_t train_count, int64_t event_count, int64_t state_count,
                      int64_t output_count, int real_axis, int features);

@@ -278,12 +278,31 @@ def test_dropin_rejects_outside_subset(built_library, cuda, golden):
     arrays = [*tissue, *events, out, out.copy(), *([None] * 13)]
     ptrs = _pointer_array(arrays)
     n = d["event_kind"].size
-    assert built_library.tsg_epg_simulate(ptrs, len(arrays), 8, 1, n, 10, 880, -1,
-                                          FEATURES) == _native.TSG_ERR_UNSUPPORTED
+    assert built_library.tsg_epg_simulate_jvp(ptrs, len(arrays), 8, 1, n, 10, 880, -1,
+                                              FEATURES) != 0
     assert built_library.tsg_epg_simulate(ptrs, len(arrays) - 1, 8, 1, n, 10, 880, 1,
                                           FEATURES) == _native.TSG_ERR_ARGUMENT
     assert built_library.tsg_epg_simulate(ptrs, len(arrays), 8, 1, n, 0, 880, 1,
                                           FEATURES) == _native.TSG_ERR_ARGUMENT
+
+
+@pytest.mark.parametrize("name", ["fse_phase0", "mrf_offaxis"])
+def test_dropin_simulate_complex_path(built_library, cuda, golden, name):
+    """real_axis = -1: the drop-in runs the complex kernel, as the reference's
+    simulate switches to simulate_range."""
+    from torchsim_gb300 import _native
+
+    d = golden(name)
+    tissue, events = _packed_arrays(d)
+    V, P = d["raw_forward"].shape
+    out_r = np.full((V, P), 7.0, np.float32)
+    out_i = np.full((V, P), 7.0, np.float32)
+    arrays = [*tissue, *events, out_r, out_i, *([None] * 13)]
+    ptrs = _pointer_array(arrays)
+    features = FEATURES | 1  # off-axis buffers present
+    _native.check(built_library.tsg_epg_simulate(ptrs, len(arrays), V, 1, d["event_kind"].size,
+                                                 int(d["states"]), P, -1, features))
+    assert max_rel(out_r + 1j * out_i, d["raw_forward"]) <= SIGNAL_TOL
 
 
 def test_dropin_jvp_general_direction(built_library, cuda, golden):

@@ -495,15 +495,16 @@ void free_all(std::vector<void*>& owned, cudaStream_t s) {
 // The checks the real-subspace, single-pool subset needs of a pointer
 // sequence in the reference's order.
 int check_subset(void* const* ptrs, int64_t count, int64_t expected, int tail_begin,
-                 int64_t atoms, int real_axis, int features, int64_t trains) {
+                 int64_t atoms, int real_axis, int features, int64_t trains,
+                 bool complex_ok = false) {
     if (!ptrs || count != expected) return fail(TSG_ERR_ARGUMENT, "wrong number of buffer pointers");
-    if (real_axis != 1)
+    if (real_axis != 1 && !complex_ok)
         return fail(TSG_ERR_UNSUPPORTED, "only the real-subspace path (real_axis == 1) is built");
     for (int i = 0; i < TAIL_COUNT; ++i)
         if (ptrs[tail_begin + i] != nullptr)
             return fail(TSG_ERR_UNSUPPORTED, "transition tables, pools and per-voxel pulses are not built");
     if (features & F_MOVING) return fail(TSG_ERR_UNSUPPORTED, "flow is not built");
-    if (features & F_OFF_AXIS) {
+    if ((features & F_OFF_AXIS) && real_axis == 1) {
         // The caller established the real subspace; off-axis terms must be
         // zero for that verdict, so they are only checked here.
         for (int idx : {4, 5}) {
@@ -543,21 +544,29 @@ extern "C" int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, in
     constexpr int64_t expected = PACKED_COUNT + 2 + TAIL_COUNT;
     if (atom_count < 0 || train_count < 1 || event_count < 0 || state_count < 1 || output_count < 0)
         return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
+    // Off the real subspace (real_axis != 1) the complex kernel runs, as the
+    // reference's simulate switches to simulate_range (_epg_cpu.cpp:10860-10900).
     int rc = check_subset(pointers, pointer_count, expected, PACKED_COUNT + 2, atom_count,
-                          real_axis, features, train_count);
+                          real_axis, features, train_count, true);
     if (rc) return rc;
+    const bool complex_path = real_axis != 1;
     std::lock_guard<std::mutex> guard(g_dropin_mutex);
     const float* duration = static_cast<const float*>(pointers[TISSUE_COUNT + 0]);
     const int32_t* kind = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 1]);
     const float* flip = static_cast<const float*>(pointers[TISSUE_COUNT + 2]);
+    const float* phase = static_cast<const float*>(pointers[TISSUE_COUNT + 3]);
     const uint8_t* action = static_cast<const uint8_t*>(pointers[TISSUE_COUNT + 4]);
     const int32_t* oindex = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 5]);
     float* out_real = static_cast<float*>(pointers[PACKED_COUNT]);
     float* out_imag = static_cast<float*>(pointers[PACKED_COUNT + 1]);
     if (!out_real || !out_imag) return fail(TSG_ERR_ARGUMENT, "null output plane");
     tsg_program* prog = nullptr;
-    rc = tsg_program_create(duration, kind, flip, action, oindex, train_count, event_count, 0,
-                            nullptr, &prog);
+    if (complex_path)
+        rc = tsg_program_create_phased(duration, kind, flip, phase, action, oindex, train_count,
+                                       event_count, &prog);
+    else
+        rc = tsg_program_create(duration, kind, flip, action, oindex, train_count, event_count, 0,
+                                nullptr, &prog);
     if (rc) return rc;
     if (prog->host.outputs > output_count) {
         tsg_program_destroy(prog);
@@ -567,11 +576,16 @@ extern "C" int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, in
     std::vector<void*> owned;
     const size_t abytes = size_t(atom_count) * sizeof(float);
     void *t1, *t2, *m0 = nullptr, *b1 = nullptr, *inv = nullptr, *dr, *di;
+    void *b1p = nullptr, *b0 = nullptr;
     rc = upload(pointers[0], abytes, owned, &t1, s);
     if (!rc) rc = upload(pointers[1], abytes, owned, &t2, s);
     if (!rc && (features & F_DENSITY)) rc = upload(pointers[2], abytes, owned, &m0, s);
     if (!rc && (features & F_TRANSMIT)) rc = upload(pointers[3], abytes, owned, &b1, s);
     if (!rc && (features & F_INVERTING)) rc = upload(pointers[6], abytes, owned, &inv, s);
+    if (!rc && complex_path && (features & F_OFF_AXIS)) {
+        rc = upload(pointers[4], abytes, owned, &b1p, s);
+        if (!rc) rc = upload(pointers[5], abytes, owned, &b0, s);
+    }
     const size_t obytes = size_t(train_count) * size_t(atom_count) * size_t(output_count) * 4;
     if (!rc) rc = dense_device(obytes, owned, &dr, s);
     if (!rc) rc = dense_device(obytes, owned, &di, s);
@@ -586,8 +600,15 @@ extern "C" int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, in
                           static_cast<float*>(m0), static_cast<float*>(b1),
                           static_cast<float*>(inv)};
         prog->host.outputs = output_count;
-        rc = tsg_epg_forward(prog, &tissue, atom_count, state_count, TSG_LAYOUT_PLANES,
-                             static_cast<float*>(dr), static_cast<float*>(di), nullptr, s);
+        if (complex_path) {
+            tsg_offaxis off{static_cast<float*>(b1p), static_cast<float*>(b0)};
+            rc = tsg_epg_forward_complex(prog, &tissue, &off, atom_count, state_count,
+                                         TSG_LAYOUT_PLANES, static_cast<float*>(dr),
+                                         static_cast<float*>(di), nullptr, s);
+        } else {
+            rc = tsg_epg_forward(prog, &tissue, atom_count, state_count, TSG_LAYOUT_PLANES,
+                                 static_cast<float*>(dr), static_cast<float*>(di), nullptr, s);
+        }
     }
     if (!rc && obytes) {
         cudaError_t e1 = cudaMemcpyAsync(out_real, dr, obytes, cudaMemcpyDeviceToHost, s);
