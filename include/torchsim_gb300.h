@@ -190,6 +190,18 @@ int tsg_epg_forward_complex(const tsg_program* program, const tsg_tissue* tissue
                             int layout, float* out_a, float* out_b, const tsg_launch* launch,
                             void* stream);
 
+/* The complex forward with its Jacobian columns in the same pass: T1, T2 and
+ * B1 tangents (TSG_TANGENT_* bits; no inversion column) and the free M0
+ * column, laid out as tsg_epg_forward_tangents lays them out. Replaces the
+ * complex forward-mode kernel simulate_jvp_range (_epg_cpu.cpp:2470-3005)
+ * that Simulator.jacobian runs off the real subspace, one tangent per pass. */
+int tsg_epg_forward_tangents_complex(const tsg_program* program, const tsg_tissue* tissue,
+                                     const tsg_offaxis* offaxis, int64_t atom_count,
+                                     int64_t state_count, unsigned tangent_mask,
+                                     const int32_t* columns, int32_t column_count, int layout,
+                                     float* sig_a, float* sig_b, float* jac_a, float* jac_b,
+                                     const tsg_launch* launch, void* stream);
+
 /* Forward. Signal layout (train, atom, output); see TSG_LAYOUT_*. For
  * TSG_LAYOUT_PLANES out_b is the imaginary plane; for COMPLEX_IJ out_b is
  * unused. Follows simulate_real_range (_epg_cpu.cpp:3041-3128). */

@@ -248,6 +248,11 @@ def case_fse_phase0(ts, rec) -> dict:
     out.update(_packed(fwd, ""))
     out["real_axis"] = np.int64(rec.axis(fwd))
     out["raw_forward"] = _np(fwd["result"])
+    names = ("T1", "T2", "B1")
+    _, jac = sim.jacobian(names, T1=torch.from_numpy(t1), T2=torch.from_numpy(t2),
+                          B1=torch.from_numpy(b1))
+    out["jacobian"] = _np(jac)
+    out["jacobian_names"] = np.array(names)
     return out
 
 
@@ -277,6 +282,12 @@ def case_mrf_offaxis(ts, rec) -> dict:
     out.update(_packed(fwd, ""))
     out["real_axis"] = np.int64(rec.axis(fwd))
     out["raw_forward"] = _np(fwd["result"])
+    names = ("T1", "T2", "B1", "M0")
+    _, jac = sim.jacobian(names, T1=torch.from_numpy(t1), T2=torch.from_numpy(t2),
+                          B1=torch.from_numpy(b1), B0=torch.from_numpy(b0),
+                          B1phase=torch.from_numpy(b1p), M0=torch.from_numpy(m0))
+    out["jacobian"] = _np(jac)
+    out["jacobian_names"] = np.array(names)
     return out
 
 

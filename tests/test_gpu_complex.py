@@ -15,6 +15,7 @@ from tests.helpers import max_rel, packed_complex_from_golden, packed_from_event
 pytestmark = pytest.mark.gpu
 
 SIGNAL_TOL = 1e-5
+JACOBIAN_TOL = 1e-4
 
 
 def _run(cuda, d, launch=None, layout_planes=False):
@@ -69,8 +70,68 @@ def test_offaxis_mrf_matches_reference_signal(cuda, golden):
     sig = sim.simulate(T1=tt("t1"), T2=tt("t2"), B1=tt("b1"), B0=tt("b0"),
                        B1phase=tt("b1_phase"), M0=tt("m0"))
     assert max_rel(sig.cpu().numpy(), d["signal"]) <= SIGNAL_TOL
+    names = tuple(str(n) for n in d["jacobian_names"])
+    _, jac = sim.jacobian(names, T1=tt("t1"), T2=tt("t2"), B1=tt("b1"), B0=tt("b0"),
+                          B1phase=tt("b1_phase"), M0=tt("m0"))
+    for c, name in enumerate(names):
+        assert max_rel(jac[:, c].cpu().numpy(), d["jacobian"][:, c]) <= JACOBIAN_TOL, name
     with pytest.raises(NotImplementedError):
-        sim.jacobian(("T1",), T1=tt("t1"), T2=tt("t2"), B0=tt("b0"))
+        sim.jacobian(("inv_efficiency",), T1=tt("t1"), T2=tt("t2"), B0=tt("b0"),
+                     inv_efficiency=tt("t1") * 0 + 0.9)
+
+
+def test_default_phase_fse_jacobian_matches_reference(cuda, golden):
+    import torchsim_gb300 as ts
+
+    d = golden("fse_phase0")
+    tt = lambda k: torch.from_numpy(d[k]).to(cuda)
+    names = tuple(str(n) for n in d["jacobian_names"])
+    _, jac = ts.fse_sim(torch.from_numpy(d["flip_deg"]), float(d["esp_ms"]), tt("t1"), tt("t2"),
+                        B1=tt("b1"), states=int(d["states"]), diff=names)
+    for c, name in enumerate(names):
+        assert max_rel(jac[:, c].cpu().numpy(), d["jacobian"][:, c]) <= JACOBIAN_TOL, name
+
+
+@pytest.mark.parametrize("launch", [None, (5, 2, 4), (4, 4, 2), (8, 4, 4)])
+def test_complex_tangents_against_central_differences(cuda, golden, launch):
+    """Each column against central differences of the FP64 complex oracle."""
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import PackedEvents, Program
+
+    d = golden("mrf_offaxis")
+    ev = PackedEvents(duration=np.atleast_2d(d["event_duration"]), kind=d["event_kind"],
+                      flip=np.atleast_2d(d["event_flip"]), phase=np.atleast_2d(d["event_phase"]),
+                      action=d["event_action"], output_index=d["event_output_index"])
+    prog = Program(ev, phased=True)
+    t = lambda k: torch.from_numpy(d[k]).to(cuda)
+    V = d["tissue_t1_ms"].size
+    tissue = engine.tissue_maps(cuda, V, t("tissue_t1_ms"), t("tissue_t2_ms"), t("tissue_m0"),
+                                t("tissue_b1"), None)
+    off, keep = engine.offaxis_maps(cuda, V, t("tissue_b1_phase_rad"), t("tissue_b0_hz"))
+    names = ("T1", "T2", "B1", "M0")
+    S = int(d["states"])
+    if launch is not None and launch[0] * launch[1] < S:
+        pytest.skip("shape holds fewer orders than the case")
+    sig, jac = engine.forward_tangents_complex(prog, tissue, S, names, off, launch=launch)
+    got = -1j * jac.cpu().numpy()
+    p = packed_complex_from_golden(d)
+    p.inversion = None
+    keys = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1", "M0": "m0"}
+    for c, name in enumerate(names):
+        base = getattr(p, keys[name]).astype(np.float64)
+        h = 1e-4 * np.abs(base) + 1e-6
+        cols = []
+        for sign in (1, -1):
+            q = packed_complex_from_golden(d)
+            q.inversion = None
+            setattr(q, keys[name], (base + sign * h).astype(np.float32))
+            cols.append(O.forward_complex(q, "f64"))
+        # The perturbed inputs pass through float32: divide by the step they took.
+        step = ((base + h).astype(np.float32).astype(np.float64)
+                - (base - h).astype(np.float32).astype(np.float64))
+        fd = (cols[0] - cols[1]) / step[:, None]
+        assert max_rel(got[:, c], fd) <= 1e-3, name
+    assert max_rel(-1j * sig.cpu().numpy(), O.forward_complex(p, "f64")) <= SIGNAL_TOL
 
 
 def test_complex_kernel_is_deterministic_and_batch_independent(cuda):

@@ -107,6 +107,11 @@ SIGNATURES: dict[str, tuple] = {
                                ctypes.POINTER(Launch), _vp]),
     "tsg_epg_forward_complex": (_int, [_vp, ctypes.POINTER(Tissue), ctypes.POINTER(Offaxis), _i64,
                                        _i64, _int, _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_forward_tangents_complex": (_int, [_vp, ctypes.POINTER(Tissue), ctypes.POINTER(Offaxis),
+                                                _i64, _i64, ctypes.c_uint,
+                                                ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                                _int, _vp, _vp, _vp, _vp, ctypes.POINTER(Launch),
+                                                _vp]),
     "tsg_epg_forward_tangents": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.c_uint,
                                         ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, _int,
                                         _vp, _vp, _vp, _vp, ctypes.POINTER(Launch), _vp]),

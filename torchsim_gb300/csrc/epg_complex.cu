@@ -39,6 +39,20 @@ struct ComplexArgs {
     int layout;
     float* out_a;
     float* out_b;
+    // Forward-mode columns (tangent kernels): (train*atoms+atom, col, output).
+    float* jac_a;
+    float* jac_b;
+    int jac_cols;
+    int col_t1, col_t2, col_b1, col_m0;
+};
+
+// The tangent systems a kernel carries: bit 1 T1, bit 2 T2, bit 4 B1.
+template <int TM>
+struct Tangents {
+    static constexpr int T1 = (TM & 1) != 0, T2 = (TM & 2) != 0, B1 = (TM & 4) != 0;
+    static constexpr int N = T1 + T2 + B1;
+    static constexpr int NA = N > 0 ? N : 1;
+    static constexpr int I_T1 = 0, I_T2 = T1, I_B1 = T1 + T2;
 };
 
 // One plane pair (re, im) shifted one order: `up` moves toward higher orders
@@ -81,6 +95,47 @@ __device__ __forceinline__ void shift_complex(float2 (&pr)[RP], float2 (&pi)[RP]
     }
 }
 
+// The pulse's complex 3x3 in terms of (t00, t22) on the diagonal,
+// A = t01 = conj(t10), B = t12 = (B_r, B_i) with t02 = (B_r, -B_i), and
+// C = t21 = (C_r, C_i) with t20 = (C_r, -C_i). For the flip alpha and phase
+// phi: t00 = (1 + cos a)/2, t22 = cos a, A = (1 - cos a)/2 e^{2i phi},
+// B = i sin a e^{-i phi}, C = i (sin a / 2) e^{i phi}; its derivative in alpha
+// has the same form with (-sin a / 2, -sin a, sin a / 2 e^{2i phi},
+// i cos a e^{-i phi}, i (cos a / 2) e^{i phi}).
+struct Pulse {
+    float2 t00, t22, A_r, A_i, nA_i, B_r, B_i, nB_i, C_r, C_i, nC_i;
+};
+
+__device__ __forceinline__ Pulse pulse_of(float d00, float d22, float a, float bs, float cs,
+                                          float c2, float s2, float cp, float sp) {
+    // a: coefficient of e^{2i phi}; bs: of B (i bs e^{-i phi}); cs: of C.
+    Pulse u;
+    u.t00 = dup(d00);
+    u.t22 = dup(d22);
+    u.A_r = dup(a * c2);
+    u.A_i = dup(a * s2);
+    u.nA_i = dup(-a * s2);
+    u.B_r = dup(bs * sp);
+    u.B_i = dup(bs * cp);
+    u.nB_i = dup(-bs * cp);
+    u.C_r = dup(-cs * sp);
+    u.C_i = dup(cs * cp);
+    u.nC_i = dup(-cs * cp);
+    return u;
+}
+
+// (P, M, Z) -> pulse applied to (pr..zi); written to the six outputs.
+__device__ __forceinline__ void apply(const Pulse& u, float2 pr, float2 pi, float2 mr, float2 mi,
+                                      float2 zr, float2 zi, float2& opr, float2& opi, float2& omr,
+                                      float2& omi, float2& ozr, float2& ozi) {
+    opr = fma2(u.B_r, zr, fma2(u.B_i, zi, fma2(u.nA_i, mi, fma2(u.A_r, mr, mul2(u.t00, pr)))));
+    opi = fma2(u.B_r, zi, fma2(u.nB_i, zr, fma2(u.A_i, mr, fma2(u.A_r, mi, mul2(u.t00, pi)))));
+    omr = fma2(u.B_r, zr, fma2(u.nB_i, zi, fma2(u.A_i, pi, fma2(u.A_r, pr, mul2(u.t00, mr)))));
+    omi = fma2(u.B_r, zi, fma2(u.B_i, zr, fma2(u.nA_i, pr, fma2(u.A_r, pi, mul2(u.t00, mi)))));
+    ozr = fma2(u.C_r, mr, fma2(u.nC_i, mi, fma2(u.C_r, pr, fma2(u.C_i, pi, mul2(u.t22, zr)))));
+    ozi = fma2(u.C_r, mi, fma2(u.C_i, mr, fma2(u.C_r, pi, fma2(u.nC_i, pr, mul2(u.t22, zi)))));
+}
+
 __device__ __forceinline__ void put(int layout, float* a, float* b, int64_t idx, float re,
                                     float im) {
     if (layout == TSG_LAYOUT_PLANES) {
@@ -94,8 +149,11 @@ __device__ __forceinline__ void put(int layout, float* a, float* b, int64_t idx,
     }
 }
 
-template <int RP, int L>
+template <int RP, int L, int TM>
 __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
+    using TG = Tangents<TM>;
+    constexpr int NT = TG::N;
+    constexpr int NA = TG::NA;
     constexpr int R = 2 * RP;
     constexpr int VPW = 32 / L;
     __shared__ Op s_ops[kComplexOpChunk];
@@ -108,8 +166,10 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
     const int64_t train = blockIdx.y;
     const bool active = slot < VPW && atom < a.atoms;
     const int64_t ac = active ? atom : 0;
-    const float r1 = 1000.f / a.t1[ac];
-    const float r2 = 1000.f / a.t2[ac];
+    const float t1 = a.t1[ac], t2 = a.t2[ac];
+    const float r1 = 1000.f / t1;
+    const float r2 = 1000.f / t2;
+    const float w1 = 1000.f / (t1 * t1), w2 = 1000.f / (t2 * t2);
     const float m0 = a.m0 ? a.m0[ac] : 1.f;
     const float b1 = a.b1 ? a.b1[ac] : 1.f;
     const float eff = a.inv ? a.inv[ac] : 1.f;
@@ -120,15 +180,23 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
     const int kill_r = a.states - q * R;
 
     float2 Pr[RP], Pi[RP], Mr[RP], Mi[RP], Zr[RP], Zi[RP];
+    float2 dPr[NA][RP], dPi[NA][RP], dMr[NA][RP], dMi[NA][RP], dZr[NA][RP], dZi[NA][RP];
 #pragma unroll
-    for (int k = 0; k < RP; ++k) Pr[k] = Pi[k] = Mr[k] = Mi[k] = Zr[k] = Zi[k] = dup(0.f);
+    for (int k = 0; k < RP; ++k) {
+        Pr[k] = Pi[k] = Mr[k] = Mi[k] = Zr[k] = Zi[k] = dup(0.f);
+#pragma unroll
+        for (int j = 0; j < NA; ++j)
+            dPr[j][k] = dPi[j][k] = dMr[j][k] = dMi[j][k] = dZr[j][k] = dZi[j][k] = dup(0.f);
+    }
     if (q == 0) Zr[0].x = 1.f;
 
     const Op* ops = a.ops + train * a.n_ops;
     const float2* phase = a.phase + train * a.n_ops;
-    const int64_t out_base = (train * a.atoms + atom) * a.outputs;
+    const int64_t row = train * a.atoms + atom;
+    const int64_t out_base = row * a.outputs;
+    const int64_t jac_base = row * a.jac_cols * a.outputs;
     float last_dt = __int_as_float(0x7fffffff);
-    float e1 = 1.f, tr = 1.f, ti = 0.f;
+    float e1 = 1.f, tr = 1.f, ti = 0.f, k1 = 0.f, k2f = 0.f;
 
     for (int base = 0; base < a.n_ops; base += kComplexOpChunk) {
         const int count = min(kComplexOpChunk, a.n_ops - base);
@@ -146,6 +214,9 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
                     last_dt = op.dt;
                     e1 = expf(-r1 * op.dt);
                     const float e2 = expf(-r2 * op.dt);
+                    // d e1 / dT1 and (d e2 / dT2) / e2.
+                    k1 = e1 * (op.dt * w1);
+                    k2f = op.dt * w2;
                     tr = e2;
                     ti = 0.f;
                     if (off_axis) {
@@ -159,48 +230,90 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
                 const float2 E1 = dup(e1), T = dup(tr), Ti = dup(ti), nTi = dup(-ti);
 #pragma unroll
                 for (int k = 0; k < RP; ++k) {
+                    const float2 pr = Pr[k], pi = Pi[k], mr = Mr[k], mi = Mi[k], zr = Zr[k],
+                                 zi = Zi[k];
+#pragma unroll
+                    for (int j = 0; j < NT; ++j) {
+                        float2 xpr = dPr[j][k], xpi = dPi[j][k], xmr = dMr[j][k], xmi = dMi[j][k];
+                        if (TG::T2 && j == TG::I_T2) {
+                            // d(T F+)/dT2 = T (dF+ + k2f F+), likewise for F-.
+                            const float2 K = dup(k2f);
+                            xpr = fma2(K, pr, xpr);
+                            xpi = fma2(K, pi, xpi);
+                            xmr = fma2(K, mr, xmr);
+                            xmi = fma2(K, mi, xmi);
+                        }
+                        dPr[j][k] = fma2(nTi, xpi, mul2(T, xpr));
+                        dPi[j][k] = fma2(Ti, xpr, mul2(T, xpi));
+                        dMr[j][k] = fma2(Ti, xmi, mul2(T, xmr));
+                        dMi[j][k] = fma2(nTi, xmr, mul2(T, xmi));
+                        if (TG::T1 && j == TG::I_T1) {
+                            dZr[j][k] = fma2(E1, dZr[j][k], mul2(dup(k1), zr));
+                            dZi[j][k] = fma2(E1, dZi[j][k], mul2(dup(k1), zi));
+                        } else {
+                            dZr[j][k] = mul2(dZr[j][k], E1);
+                            dZi[j][k] = mul2(dZi[j][k], E1);
+                        }
+                    }
                     // F+ *= (tr + i ti), F- *= (tr - i ti), Z *= e1.
-                    const float2 pr = Pr[k], pi = Pi[k], mr = Mr[k], mi = Mi[k];
                     Pr[k] = fma2(nTi, pi, mul2(T, pr));
                     Pi[k] = fma2(Ti, pr, mul2(T, pi));
                     Mr[k] = fma2(Ti, mi, mul2(T, mr));
                     Mi[k] = fma2(nTi, mr, mul2(T, mi));
-                    Zr[k] = mul2(Zr[k], E1);
-                    Zi[k] = mul2(Zi[k], E1);
+                    Zr[k] = mul2(zr, E1);
+                    Zi[k] = mul2(zi, E1);
                 }
-                if (q == 0) Zr[0].x += 1.f - e1;
+                if (q == 0) {
+                    Zr[0].x += 1.f - e1;
+                    if constexpr (TG::T1) dZr[TG::I_T1][0].x -= k1;
+                }
             }
-            for (int s = 0; s < op_shift1(code); ++s)
+            for (int s = 0; s < op_shift1(code); ++s) {
                 shift_complex<RP, L>(Pr, Pi, Mr, Mi, q, kill, kill_r);
+#pragma unroll
+                for (int j = 0; j < NT; ++j)
+                    shift_complex<RP, L>(dPr[j], dPi[j], dMr[j], dMi[j], q, kill, kill_r);
+            }
             const int rf = op_rf(code);
             if (rf == RF_ROTATE) {
                 float sa, ca, sp, cp;
                 sincosf(op.flip * b1, &sa, &ca);
                 sincosf(s_ph[i].x + b1_phase, &sp, &cp);
-                const float ch = 0.5f * (1.f + ca), sh = 0.5f * (1.f - ca);
                 // e^{2i phi} from e^{i phi}.
                 const float c2 = cp * cp - sp * sp, s2 = 2.f * cp * sp;
-                const float2 T00 = dup(ch), T22 = dup(ca);
-                const float2 A_r = dup(sh * c2), A_i = dup(sh * s2), nA_i = dup(-sh * s2);
-                const float2 B_r = dup(sa * sp), B_i = dup(sa * cp), nB_i = dup(-sa * cp);
-                const float2 C_r = dup(-0.5f * sa * sp), C_i = dup(0.5f * sa * cp),
-                             nC_i = dup(-0.5f * sa * cp);
+                const Pulse u = pulse_of(0.5f * (1.f + ca), ca, 0.5f * (1.f - ca), sa, 0.5f * sa,
+                                         c2, s2, cp, sp);
+                Pulse du{};
+                if constexpr (TG::B1)
+                    du = pulse_of(-0.5f * sa, -sa, 0.5f * sa, ca, 0.5f * ca, c2, s2, cp, sp);
+                const float2 at = dup(op.flip);  // d alpha / d B1
 #pragma unroll
                 for (int k = 0; k < RP; ++k) {
                     const float2 pr = Pr[k], pi = Pi[k], mr = Mr[k], mi = Mi[k], zr = Zr[k],
                                  zi = Zi[k];
-                    // F+ = ch F+ + A F- + B' Z with A = sh e^{2i phi},
-                    //      B' = -i sa e^{i phi} = (sa sp, -sa cp).
-                    Pr[k] = fma2(B_r, zr, fma2(B_i, zi, fma2(nA_i, mi, fma2(A_r, mr, mul2(T00, pr)))));
-                    Pi[k] = fma2(B_r, zi, fma2(nB_i, zr, fma2(A_i, mr, fma2(A_r, mi, mul2(T00, pi)))));
-                    // F- = conj(A) F+ + ch F- + i sa e^{-i phi} Z = (sa sp, sa cp).
-                    Mr[k] = fma2(B_r, zr, fma2(nB_i, zi, fma2(A_i, pi, fma2(A_r, pr, mul2(T00, mr)))));
-                    Mi[k] = fma2(B_r, zi, fma2(B_i, zr, fma2(nA_i, pr, fma2(A_r, pi, mul2(T00, mi)))));
-                    // Z = -i sa/2 e^{-i phi} F+ + i sa/2 e^{i phi} F- + ca Z, with
-                    // -i sa/2 e^{-i phi} = (-sa/2 sp, -sa/2 cp) = (C_r, -C_i) and
-                    // i sa/2 e^{i phi} = (-sa/2 sp, sa/2 cp) = (C_r, C_i).
-                    Zr[k] = fma2(C_r, mr, fma2(nC_i, mi, fma2(C_r, pr, fma2(C_i, pi, mul2(T22, zr)))));
-                    Zi[k] = fma2(C_r, mi, fma2(C_i, mr, fma2(C_r, pi, fma2(nC_i, pr, mul2(T22, zi)))));
+#pragma unroll
+                    for (int j = 0; j < NT; ++j) {
+                        float2 opr, opi, omr, omi, ozr, ozi;
+                        apply(u, dPr[j][k], dPi[j][k], dMr[j][k], dMi[j][k], dZr[j][k], dZi[j][k],
+                              opr, opi, omr, omi, ozr, ozi);
+                        if (TG::B1 && j == TG::I_B1) {
+                            float2 vpr, vpi, vmr, vmi, vzr, vzi;
+                            apply(du, pr, pi, mr, mi, zr, zi, vpr, vpi, vmr, vmi, vzr, vzi);
+                            opr = fma2(at, vpr, opr);
+                            opi = fma2(at, vpi, opi);
+                            omr = fma2(at, vmr, omr);
+                            omi = fma2(at, vmi, omi);
+                            ozr = fma2(at, vzr, ozr);
+                            ozi = fma2(at, vzi, ozi);
+                        }
+                        dPr[j][k] = opr;
+                        dPi[j][k] = opi;
+                        dMr[j][k] = omr;
+                        dMi[j][k] = omi;
+                        dZr[j][k] = ozr;
+                        dZi[j][k] = ozi;
+                    }
+                    apply(u, pr, pi, mr, mi, zr, zi, Pr[k], Pi[k], Mr[k], Mi[k], Zr[k], Zi[k]);
                 }
             } else if (rf == RF_INVERT) {
                 const float2 f = dup(-eff);
@@ -208,27 +321,68 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
                 for (int k = 0; k < RP; ++k) {
                     Zr[k] = mul2(Zr[k], f);
                     Zi[k] = mul2(Zi[k], f);
+#pragma unroll
+                    for (int j = 0; j < NT; ++j) {
+                        dZr[j][k] = mul2(dZr[j][k], f);
+                        dZi[j][k] = mul2(dZi[j][k], f);
+                    }
                 }
             }
-            for (int s = 0; s < op_shift2(code); ++s)
+            for (int s = 0; s < op_shift2(code); ++s) {
                 shift_complex<RP, L>(Pr, Pi, Mr, Mi, q, kill, kill_r);
+#pragma unroll
+                for (int j = 0; j < NT; ++j)
+                    shift_complex<RP, L>(dPr[j], dPi[j], dMr[j], dMi[j], q, kill, kill_r);
+            }
             if (code & OP_SPOIL1) {
 #pragma unroll
-                for (int k = 0; k < RP; ++k) Pr[k] = Pi[k] = Mr[k] = Mi[k] = dup(0.f);
+                for (int k = 0; k < RP; ++k) {
+                    Pr[k] = Pi[k] = Mr[k] = Mi[k] = dup(0.f);
+#pragma unroll
+                    for (int j = 0; j < NT; ++j) dPr[j][k] = dPi[j][k] = dMr[j][k] = dMi[j][k] = dup(0.f);
+                }
             }
             if ((code & OP_RECORD) && q == 0 && active) {
-                // m0 F+[0] demodulated by the receiver phase.
+                // m0 F+[0] demodulated by the receiver phase, and its columns.
                 float sr, cr;
                 sincosf(s_ph[i].y, &sr, &cr);
-                const float vr = m0 * Pr[0].x, vi = m0 * Pi[0].x;
-                put(a.layout, a.out_a, a.out_b, out_base + op.record, vr * cr + vi * sr,
-                    vi * cr - vr * sr);
+                const int rec = op.record;
+                auto demod = [&](float xr, float xi, float& yr, float& yi) {
+                    yr = xr * cr + xi * sr;
+                    yi = xi * cr - xr * sr;
+                };
+                float yr, yi;
+                demod(Pr[0].x, Pi[0].x, yr, yi);
+                if (a.out_a) put(a.layout, a.out_a, a.out_b, out_base + rec, m0 * yr, m0 * yi);
+                if constexpr (NT > 0) {
+                    if (a.col_m0 >= 0)
+                        put(a.layout, a.jac_a, a.jac_b, jac_base + a.col_m0 * a.outputs + rec, yr, yi);
+                    const int cols[3] = {a.col_t1, a.col_t2, a.col_b1};
+                    const int idx[3] = {TG::I_T1, TG::I_T2, TG::I_B1};
+                    const bool has[3] = {bool(TG::T1), bool(TG::T2), bool(TG::B1)};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        if (!has[c] || cols[c] < 0) continue;
+                        float dr, di;
+                        demod(dPr[idx[c]][0].x, dPi[idx[c]][0].x, dr, di);
+                        put(a.layout, a.jac_a, a.jac_b, jac_base + cols[c] * a.outputs + rec,
+                            m0 * dr, m0 * di);
+                    }
+                }
             }
-            for (int s = 0; s < op_shift3(code); ++s)
+            for (int s = 0; s < op_shift3(code); ++s) {
                 shift_complex<RP, L>(Pr, Pi, Mr, Mi, q, kill, kill_r);
+#pragma unroll
+                for (int j = 0; j < NT; ++j)
+                    shift_complex<RP, L>(dPr[j], dPi[j], dMr[j], dMi[j], q, kill, kill_r);
+            }
             if (code & OP_SPOIL2) {
 #pragma unroll
-                for (int k = 0; k < RP; ++k) Pr[k] = Pi[k] = Mr[k] = Mi[k] = dup(0.f);
+                for (int k = 0; k < RP; ++k) {
+                    Pr[k] = Pi[k] = Mr[k] = Mi[k] = dup(0.f);
+#pragma unroll
+                    for (int j = 0; j < NT; ++j) dPr[j][k] = dPi[j][k] = dMr[j][k] = dMi[j][k] = dup(0.f);
+                }
             }
         }
     }
@@ -237,33 +391,71 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
 struct ComplexEntry {
     int orders_per_lane;
     int lanes_per_voxel;
+    int tangents;
     void (*launch)(const ComplexArgs&, dim3, dim3, cudaStream_t);
 };
 
-template <int RP, int L>
+template <int RP, int L, int TM>
 void launch_complex(const ComplexArgs& a, dim3 grid, dim3 block, cudaStream_t s) {
-    epg_complex_kernel<RP, L><<<grid, block, 0, s>>>(a);
+    epg_complex_kernel<RP, L, TM><<<grid, block, 0, s>>>(a);
 }
 
-#define TSG_COMPLEX_ENTRY(R, L) {R, L, &launch_complex<(R) / 2, L>}
+#define TSG_COMPLEX_ENTRY(R, L, TM) {R, L, TM, &launch_complex<(R) / 2, L, TM>}
 
 const ComplexEntry kComplex[] = {
-    TSG_COMPLEX_ENTRY(10, 1), TSG_COMPLEX_ENTRY(6, 2),  TSG_COMPLEX_ENTRY(4, 4),
-    TSG_COMPLEX_ENTRY(4, 5),  TSG_COMPLEX_ENTRY(2, 10), TSG_COMPLEX_ENTRY(4, 8),
-    TSG_COMPLEX_ENTRY(4, 16), TSG_COMPLEX_ENTRY(4, 32),
+    TSG_COMPLEX_ENTRY(10, 1, 0), TSG_COMPLEX_ENTRY(6, 2, 0),  TSG_COMPLEX_ENTRY(4, 4, 0),
+    TSG_COMPLEX_ENTRY(4, 5, 0),  TSG_COMPLEX_ENTRY(2, 10, 0), TSG_COMPLEX_ENTRY(4, 8, 0),
+    TSG_COMPLEX_ENTRY(4, 16, 0), TSG_COMPLEX_ENTRY(4, 32, 0),
+    // Tangent kernels: T1|T2 and T1|T2|B1.
+    TSG_COMPLEX_ENTRY(2, 5, 3),  TSG_COMPLEX_ENTRY(4, 4, 3),  TSG_COMPLEX_ENTRY(4, 5, 3),
+    TSG_COMPLEX_ENTRY(2, 10, 3), TSG_COMPLEX_ENTRY(4, 8, 3),  TSG_COMPLEX_ENTRY(4, 16, 3),
+    TSG_COMPLEX_ENTRY(4, 32, 3), TSG_COMPLEX_ENTRY(2, 5, 7),  TSG_COMPLEX_ENTRY(4, 4, 7),
+    TSG_COMPLEX_ENTRY(4, 5, 7),  TSG_COMPLEX_ENTRY(2, 10, 7), TSG_COMPLEX_ENTRY(4, 8, 7),
+    TSG_COMPLEX_ENTRY(4, 16, 7), TSG_COMPLEX_ENTRY(4, 32, 7),
 };
 
-}  // namespace
+// The entry of a tangent family for a state count and launch request.
+const ComplexEntry* choose_complex(int tangents, int64_t states, const tsg_launch* want) {
+    const int want_l = want ? want->lanes_per_voxel : 0;
+    const int want_r = want ? want->orders_per_lane : 0;
+    const ComplexEntry* best = nullptr;
+    double best_waste = 1e30;
+    for (const ComplexEntry& e : kComplex) {
+        if (e.tangents != tangents) continue;
+        const int padded = e.orders_per_lane * e.lanes_per_voxel;
+        if (padded < states) continue;
+        if (want_l > 0 && e.lanes_per_voxel != want_l) continue;
+        if (want_r > 0 && e.orders_per_lane != want_r) continue;
+        const int vpw = 32 / e.lanes_per_voxel;
+        // Fewest idle order slots per warp, fewer lanes per voxel first.
+        const double waste = double(32 * e.orders_per_lane) / double(vpw * states) *
+                             (1.0 + 0.05 * (e.lanes_per_voxel - 1));
+        if (waste < best_waste) {
+            best_waste = waste;
+            best = &e;
+        }
+    }
+    return best;
+}
 
-}  // namespace tsg
+int launch_complex_sweep(const tsg_program* program, const ComplexArgs& base, int tangents,
+                         int64_t atom_count, int64_t state_count, const tsg_launch* launch_shape,
+                         cudaStream_t stream) {
+    const int warps = (launch_shape && launch_shape->warps_per_block > 0) ? launch_shape->warps_per_block : 4;
+    if (warps < 1 || warps > 8) return fail(TSG_ERR_ARGUMENT, "warps_per_block must be 1..8");
+    const ComplexEntry* best = choose_complex(tangents, state_count, launch_shape);
+    if (!best) return fail(TSG_ERR_UNSUPPORTED, "no complex kernel for this state count / launch shape");
+    const int vpb = warps * (32 / best->lanes_per_voxel);
+    const int64_t blocks = (atom_count + vpb - 1) / vpb;
+    if (blocks > 0x7fffffffLL) return fail(TSG_ERR_CAPACITY, "launch too large");
+    best->launch(base, dim3(unsigned(blocks), unsigned(program->host.trains)), dim3(32 * warps),
+                 stream);
+    TSG_CUDA(cudaGetLastError());
+    return TSG_OK;
+}
 
-using namespace tsg;
-
-extern "C" int tsg_epg_forward_complex(const tsg_program* program, const tsg_tissue* tissue,
-                                       const tsg_offaxis* offaxis, int64_t atom_count,
-                                       int64_t state_count, int layout, float* out_a,
-                                       float* out_b, const tsg_launch* launch_shape,
-                                       void* stream) {
+int complex_common(const tsg_program* program, const tsg_tissue* tissue, int64_t atom_count,
+                   int64_t state_count, int layout) {
     if (!program) return fail(TSG_ERR_ARGUMENT, "null program");
     if (!tissue || (atom_count > 0 && (!tissue->t1_ms || !tissue->t2_ms)))
         return fail(TSG_ERR_ARGUMENT, "t1 and t2 are required");
@@ -273,32 +465,13 @@ extern "C" int tsg_epg_forward_complex(const tsg_program* program, const tsg_tis
         return fail(TSG_ERR_ARGUMENT, "the complex path needs a program built with event phases");
     if (layout != TSG_LAYOUT_PLANES && layout != TSG_LAYOUT_COMPLEX_IJ && layout != TSG_LAYOUT_COMPLEX)
         return fail(TSG_ERR_ARGUMENT, "unknown output layout");
-    if (layout == TSG_LAYOUT_PLANES ? (!out_a || !out_b) : !out_a)
-        return fail(TSG_ERR_ARGUMENT, "null output buffer");
-    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
     if (program->host.trains > 65535) return fail(TSG_ERR_CAPACITY, "more than 65535 trains");
-    const int want_l = launch_shape ? launch_shape->lanes_per_voxel : 0;
-    const int want_r = launch_shape ? launch_shape->orders_per_lane : 0;
-    const int warps = (launch_shape && launch_shape->warps_per_block > 0) ? launch_shape->warps_per_block : 4;
-    if (warps < 1 || warps > 8) return fail(TSG_ERR_ARGUMENT, "warps_per_block must be 1..8");
-    // Without a request: the entry with the fewest idle order slots per warp,
-    // one voxel per lane first.
-    const ComplexEntry* best = nullptr;
-    double best_waste = 1e30;
-    for (const ComplexEntry& e : kComplex) {
-        const int padded = e.orders_per_lane * e.lanes_per_voxel;
-        if (padded < state_count) continue;
-        if (want_l > 0 && e.lanes_per_voxel != want_l) continue;
-        if (want_r > 0 && e.orders_per_lane != want_r) continue;
-        const int vpw = 32 / e.lanes_per_voxel;
-        const double waste = double(32 * e.orders_per_lane) / double(vpw * state_count) *
-                             (1.0 + 0.05 * (e.lanes_per_voxel - 1));
-        if (waste < best_waste) {
-            best_waste = waste;
-            best = &e;
-        }
-    }
-    if (!best) return fail(TSG_ERR_UNSUPPORTED, "no complex kernel for this state count / launch shape");
+    return TSG_OK;
+}
+
+ComplexArgs complex_args(const tsg_program* program, const tsg_tissue* tissue,
+                         const tsg_offaxis* offaxis, int64_t atom_count, int64_t state_count,
+                         int layout) {
     ComplexArgs a{};
     a.ops = program->d_ops;
     a.phase = program->d_phase;
@@ -314,13 +487,67 @@ extern "C" int tsg_epg_forward_complex(const tsg_program* program, const tsg_tis
     a.b1_phase = offaxis ? offaxis->b1_phase_rad : nullptr;
     a.b0 = offaxis ? offaxis->b0_hz : nullptr;
     a.layout = layout;
+    a.col_t1 = a.col_t2 = a.col_b1 = a.col_m0 = -1;
+    return a;
+}
+
+}  // namespace
+
+}  // namespace tsg
+
+using namespace tsg;
+
+extern "C" int tsg_epg_forward_complex(const tsg_program* program, const tsg_tissue* tissue,
+                                       const tsg_offaxis* offaxis, int64_t atom_count,
+                                       int64_t state_count, int layout, float* out_a,
+                                       float* out_b, const tsg_launch* launch_shape,
+                                       void* stream) {
+    int rc = complex_common(program, tissue, atom_count, state_count, layout);
+    if (rc) return rc;
+    if (layout == TSG_LAYOUT_PLANES ? (!out_a || !out_b) : !out_a)
+        return fail(TSG_ERR_ARGUMENT, "null output buffer");
+    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+    ComplexArgs a = complex_args(program, tissue, offaxis, atom_count, state_count, layout);
     a.out_a = out_a;
     a.out_b = out_b;
-    const int vpb = warps * (32 / best->lanes_per_voxel);
-    const int64_t blocks = (atom_count + vpb - 1) / vpb;
-    if (blocks > 0x7fffffffLL) return fail(TSG_ERR_CAPACITY, "launch too large");
-    best->launch(a, dim3(unsigned(blocks), unsigned(program->host.trains)), dim3(32 * warps),
-                 static_cast<cudaStream_t>(stream));
-    TSG_CUDA(cudaGetLastError());
-    return TSG_OK;
+    return launch_complex_sweep(program, a, 0, atom_count, state_count, launch_shape,
+                                static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tsg_epg_forward_tangents_complex(const tsg_program* program, const tsg_tissue* tissue,
+                                                const tsg_offaxis* offaxis, int64_t atom_count,
+                                                int64_t state_count, unsigned tangent_mask,
+                                                const int32_t* columns, int32_t column_count,
+                                                int layout, float* sig_a, float* sig_b,
+                                                float* jac_a, float* jac_b,
+                                                const tsg_launch* launch_shape, void* stream) {
+    int rc = complex_common(program, tissue, atom_count, state_count, layout);
+    if (rc) return rc;
+    if (!columns || column_count < 0) return fail(TSG_ERR_ARGUMENT, "null column map");
+    if (tangent_mask & ~unsigned(TSG_TANGENT_T1 | TSG_TANGENT_T2 | TSG_TANGENT_B1))
+        return fail(TSG_ERR_UNSUPPORTED, "the complex path carries T1, T2 and B1 tangents");
+    if (columns[3] >= 0) return fail(TSG_ERR_UNSUPPORTED, "no inversion-efficiency column on the complex path");
+    const unsigned bits[3] = {TSG_TANGENT_T1, TSG_TANGENT_T2, TSG_TANGENT_B1};
+    for (int i = 0; i < 5; ++i)
+        if (columns[i] >= column_count) return fail(TSG_ERR_ARGUMENT, "column out of range");
+    for (int i = 0; i < 3; ++i)
+        if (columns[i] >= 0 && !(tangent_mask & bits[i]))
+            return fail(TSG_ERR_ARGUMENT, "column given for a tangent not in the mask");
+    if (layout == TSG_LAYOUT_PLANES ? (!jac_a || !jac_b) : !jac_a)
+        return fail(TSG_ERR_ARGUMENT, "null Jacobian buffer");
+    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+    ComplexArgs a = complex_args(program, tissue, offaxis, atom_count, state_count, layout);
+    a.out_a = sig_a;
+    a.out_b = sig_b;
+    if (layout == TSG_LAYOUT_PLANES && (!sig_a || !sig_b)) a.out_a = a.out_b = nullptr;
+    a.jac_a = jac_a;
+    a.jac_b = jac_b;
+    a.jac_cols = column_count;
+    a.col_t1 = columns[0];
+    a.col_t2 = columns[1];
+    a.col_b1 = columns[2];
+    a.col_m0 = columns[4];
+    const int family = (tangent_mask & TSG_TANGENT_B1) ? 7 : 3;
+    return launch_complex_sweep(program, a, family, atom_count, state_count, launch_shape,
+                                static_cast<cudaStream_t>(stream));
 }

@@ -152,6 +152,31 @@ def forward_complex(program: Program, tissue: TissueMaps, states: int, offaxis=N
     return out
 
 
+def forward_tangents_complex(program: Program, tissue: TissueMaps, states: int,
+                             names: Sequence[str], offaxis=None, *, launch=None):
+    """Complex-path signal and Jacobian columns ``names`` (T1, T2, B1, M0) in
+    one pass: ``(signal (rows, P), jacobian (rows, k, P))`` complex64 holding
+    ``1j * m0 F+[0] e^{-i phase}`` and its derivatives."""
+    if not program.phased:
+        raise ValueError("the complex kernel needs a program built with its event phases")
+    mask, columns = plan_tangents(names)
+    if columns[3] >= 0:
+        raise NotImplementedError("no inversion-efficiency column on the complex path")
+    rows = program.trains * tissue.voxels
+    k = len(names)
+    device = tissue.t1.device
+    sig = torch.empty((rows, program.outputs), dtype=torch.complex64, device=device)
+    jac = torch.empty((rows, k, program.outputs), dtype=torch.complex64, device=device)
+    t = tissue.struct()
+    off = offaxis if offaxis is not None else _native.Offaxis(None, None)
+    cols = (ctypes.c_int32 * 5)(*columns)
+    _native.check(_native.library().tsg_epg_forward_tangents_complex(
+        program.handle, ctypes.byref(t), ctypes.byref(off), tissue.voxels, states, mask, cols, k,
+        _native.LAYOUT_COMPLEX_IJ, sig.data_ptr(), None, jac.data_ptr(), None,
+        _native.launch_shape(launch), _stream()))
+    return sig, jac
+
+
 def plan_tangents(names: Sequence[str]) -> tuple[int, list[int]]:
     """Tangent mask and the 5-slot column map for an ordered list of names."""
     mask = 0

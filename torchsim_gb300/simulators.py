@@ -120,10 +120,6 @@ class _EpgSimulator:
                                   (home if home.type == "cuda" else None))
         events = self.events(repetitions=repetitions, **protocol)
         complex_path = _leaves_real_subspace(events, held)
-        if complex_path and names:
-            raise NotImplementedError(
-                "Jacobians on the complex path (RF phases, B0, B1phase) are not built; the "
-                "signal is")
         batch = _batch(held)
         voxels = _numel(batch)
         maps = self._kernel_maps(held)
@@ -146,16 +142,26 @@ class _EpgSimulator:
             tissue = engine.tissue_maps(dev, voxels, maps["T1"], maps["T2"],
                                         declared("M0", maps["M0"]), declared("B1", maps["B1"]),
                                         declared("inv", maps["inv"]))
+            kernel_names = self._kernel_names(names) if names else None
             if complex_path:
                 off, keep = engine.offaxis_maps(dev, voxels, maps.get("B1phase"), maps.get("B0"))
                 program = program_for(events, dev, phased=True)
-                signal = engine.forward_complex(program, tissue, states, off)
+                if kernel_names:
+                    signal, jac = engine.forward_tangents_complex(program, tissue, states,
+                                                                  kernel_names, off)
+                else:
+                    signal, jac = engine.forward_complex(program, tissue, states, off), None
                 del keep
-                signal, _ = self._post(signal, None, None, held, protocol, dev)
+                signal, jac = self._post(signal, jac, names, held, protocol, dev)
                 signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
-                return (signal.to(home) if home.type != "cuda" else signal), None
+                if jac is not None:
+                    jac = (jac.reshape(*batch, *jac.shape[-2:]) if batch
+                           else jac.reshape(jac.shape[-2:]))
+                if home.type != "cuda":
+                    signal = signal.to(home)
+                    jac = None if jac is None else jac.to(home)
+                return signal, jac
             program = program_for(events, dev)
-            kernel_names = self._kernel_names(names) if names else None
             if kernel_names:
                 signal, jac = engine.forward_tangents(program, tissue, states, kernel_names)
             else:
