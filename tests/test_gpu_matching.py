@@ -1,0 +1,107 @@
+"""Dictionary matching on the tensor cores against an exhaustive FP64 search
+(the reference's DictionaryMatcher semantics, estimators/_dictionary.py:
+329-420: normalized |<s, d>|, top-k, least-squares scale and density)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def exhaustive(signals: np.ndarray, atoms: np.ndarray, k: int):
+    s = signals.astype(np.complex128)
+    d = atoms.astype(np.complex128)
+    sn = s / np.maximum(np.linalg.norm(s, axis=1, keepdims=True), 1e-30)
+    dn = d / np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-30)
+    scores = np.abs(sn @ dn.conj().T)
+    order = np.argsort(-scores, axis=1, kind="stable")[:, :k]
+    return scores, order
+
+
+def make_case(rng, V, A, P, kind):
+    if kind == "real":
+        atoms = rng.standard_normal((A, P)).astype(np.float32).astype(np.complex64)
+    elif kind == "imaginary":
+        atoms = (1j * rng.standard_normal((A, P))).astype(np.complex64)
+    else:
+        atoms = (rng.standard_normal((A, P)) + 1j * rng.standard_normal((A, P))).astype(np.complex64)
+    truth = rng.integers(0, A, V)
+    scale = (rng.uniform(0.5, 2.0, V) * np.exp(1j * rng.uniform(-np.pi, np.pi, V)))
+    noise = 0.05 * (rng.standard_normal((V, P)) + 1j * rng.standard_normal((V, P)))
+    signals = (atoms[truth] * scale[:, None] + noise * np.abs(atoms).mean()).astype(np.complex64)
+    return signals, atoms, truth
+
+
+@pytest.mark.parametrize("kind", ["real", "imaginary", "complex"])
+@pytest.mark.parametrize("V,A,P", [(300, 1000, 100), (64, 37, 880), (1, 5, 8)])
+def test_match_equals_exhaustive_search(cuda, kind, V, A, P):
+    from torchsim_gb300 import DictionaryMatcher
+
+    rng = np.random.default_rng(V + A + P)
+    signals, atoms, truth = make_case(rng, V, A, P, kind)
+    k = min(3, A)
+    params = rng.uniform(0, 1, (A, 2)).astype(np.float32)
+    matcher = DictionaryMatcher(dictionary=torch.from_numpy(atoms), parameters=torch.from_numpy(params),
+                                top_k=k, query_chunk_size=128)
+    res = matcher.match(torch.from_numpy(signals).to(cuda))
+    scores, order = exhaustive(signals, atoms, k)
+    idx = res.indices.cpu().numpy()
+    got = res.scores.cpu().numpy()
+    best = scores[np.arange(V), order[:, 0]]
+    # The chosen atoms score what the FP64 search says they score ...
+    assert np.abs(got - np.take_along_axis(scores, idx, 1)).max() <= 2e-6
+    # ... and the first is the best, up to FP32 ties.
+    assert np.all(scores[np.arange(V), idx[:, 0]] >= best - 2e-6)
+    assert np.mean(idx[:, 0] == order[:, 0]) >= 0.99
+    if A > 1:
+        assert np.all(np.diff(got, axis=1) <= 1e-7)  # best first
+    # Least-squares scale and density of the first candidate.
+    d = atoms[idx[:, 0]].astype(np.complex128)
+    scale = np.sum(d.conj() * signals, axis=1) / np.sum(np.abs(d) ** 2, axis=1)
+    assert np.abs(res.scales[:, 0].cpu().numpy() - scale).max() <= 1e-4 * np.abs(scale).max()
+    assert np.abs(res.densities[:, 0].cpu().numpy() - np.abs(scale)).max() <= 1e-4 * np.abs(scale).max()
+    np.testing.assert_array_equal(res.parameters.cpu().numpy(), params[idx])
+
+
+def test_match_recovers_mrf_dictionary_atoms(cuda):
+    """A dictionary from the MRF simulator (on the imaginary axis) and noisy,
+    scaled, phase-turned signals of its own atoms."""
+    import torchsim_gb300 as ts
+
+    rng = np.random.default_rng(3)
+    flip = np.concatenate([np.linspace(5, 60, 100), np.linspace(60, 2, 100)]).astype(np.float32)
+    t1 = np.geomspace(100, 4000, 40)
+    t2 = np.geomspace(5, 500, 30)
+    g1, g2 = np.meshgrid(t1, t2, indexing="ij")
+    keep = g2 < g1
+    T1 = torch.from_numpy(g1[keep].astype(np.float32)).to(cuda)
+    T2 = torch.from_numpy(g2[keep].astype(np.float32)).to(cuda)
+    dictionary = ts.mrf_sim(torch.from_numpy(flip), 10.0, T1, T2, states=10)
+    matcher = ts.DictionaryMatcher(dictionary=dictionary, parameters=torch.stack((T1, T2), 1))
+    truth = rng.integers(0, dictionary.shape[0], 500)
+    phase = torch.from_numpy(np.exp(1j * rng.uniform(-3, 3, 500)).astype(np.complex64)).to(cuda)
+    noise = torch.from_numpy((rng.standard_normal((500, 200)) + 1j * rng.standard_normal((500, 200)))
+                             .astype(np.complex64)).to(cuda) * 1e-3
+    measured = dictionary[torch.from_numpy(truth).to(cuda)] * (0.7 * phase[:, None]) + noise
+    maps = matcher(measured)
+    got = maps.cpu().numpy()
+    want = np.stack((g1[keep], g2[keep]), 1)[truth]
+    assert np.mean(np.all(np.isclose(got, want, rtol=1e-5), axis=1)) >= 0.99
+    res = matcher.match(measured)
+    np.testing.assert_allclose(res.densities[:, 0].cpu().numpy(), 0.7, rtol=2e-2)
+
+
+def test_match_argument_errors(cuda):
+    from torchsim_gb300 import DictionaryMatcher
+
+    atoms = torch.ones((4, 16), dtype=torch.complex64)
+    with pytest.raises(ValueError):
+        DictionaryMatcher(dictionary=atoms, top_k=9)
+    with pytest.raises(NotImplementedError):
+        DictionaryMatcher(dictionary=atoms, groups=2)
+    m = DictionaryMatcher(dictionary=atoms)
+    with pytest.raises(ValueError):
+        m.match(torch.ones((3, 15), dtype=torch.complex64))

@@ -7,16 +7,20 @@ Public API kept from the reference (FiRMLAB-Pisa/torchsim):
 * ``EpgEngine().simulate(events, tissue)`` — a packed stream on the kernels,
   with its sample labels (``SimulationResult``);
 * ``SequenceDesign``, ``Bounded``, ``crlb`` — sequence design through the
-  adjoint kernel.
+  adjoint kernel;
+* ``DictionaryMatcher``, ``MatchResult`` — dictionary matching on the tensor
+  cores.
 
 All compute runs in hand-written sm_103a CUDA kernels behind the C ABI in
 ``include/torchsim_gb300.h``; there is no CPU fallback.
 """
 
 from .design import Bounded, SequenceDesign, SequenceOptimization, crlb
+from .matching import DictionaryMatcher, MatchResult
 from .simulators import (EpgEngine, FSESimulator, MRFSimulator, SimulationResult, fse_sim,
                          mrf_sim)
 
-__all__ = ["Bounded", "EpgEngine", "FSESimulator", "MRFSimulator", "SequenceDesign",
-           "SequenceOptimization", "SimulationResult", "crlb", "fse_sim", "mrf_sim"]
+__all__ = ["Bounded", "DictionaryMatcher", "EpgEngine", "FSESimulator", "MRFSimulator",
+           "MatchResult", "SequenceDesign", "SequenceOptimization", "SimulationResult", "crlb",
+           "fse_sim", "mrf_sim"]
 __version__ = "0.1.0"

@@ -135,6 +135,9 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_gn_step": (_int, [ctypes.POINTER(GNState), _i64, ctypes.POINTER(GNConfig), _vp]),
     "tsg_gn_judge": (_int, [ctypes.POINTER(GNState), _i64, ctypes.POINTER(GNConfig), _vp]),
     "tsg_gn_natural": (_int, [_vp, _i64, ctypes.POINTER(GNConfig), _vp, _vp]),
+    "tsg_match_screen": (_int, [_vp, _i64, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "tsg_match_rescore": (_int, [_vp, _i64, _vp, _i64, _i64, _vp, _int, _vp, _vp, _vp]),
+    "tsg_match_candidates": (_int, []),
     "tsg_epg_simulate_vjp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
                                     _int, _int]),
     "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,

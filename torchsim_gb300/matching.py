@@ -1,0 +1,185 @@
+"""Dictionary matching: the best atoms of a simulated dictionary per voxel.
+
+The interface is the reference's ``DictionaryMatcher`` / ``MatchResult``
+(``estimators/_dictionary.py:18-420``): atoms and signals are normalized, a
+voxel's score against an atom is ``|<s, d>|`` (``_grouped.py:212-240``), and a
+match returns the top-k atoms with their scores, the complex least-squares
+scale (proton density and receive phase), its size and the atoms' parameter
+values.
+
+The search is one tensor-core kernel per chunk of voxels
+(``tsg_match_screen``): bf16 products accumulated in FP32 in tensor memory,
+with the selection of each voxel's best few atoms fused into the epilogue, so
+the voxel x atom score matrix never exists. The few candidates are then
+rescored exactly in FP32 against the complex signals (``tsg_match_rescore``)
+and the top k kept, so the bf16 screen only narrows which atoms are compared.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import torch
+
+from . import _native, engine
+
+__all__ = ["DictionaryMatcher", "MatchResult"]
+
+
+@dataclass(frozen=True)
+class MatchResult:
+    """Best atoms per voxel (``(..., k)``): ``parameters`` ``(..., k, n)`` (or
+    None without parameter values), ``indices``, ``scores`` (the normalized
+    ``|<s, d>|``), ``scales`` (complex least-squares scale) and ``densities``
+    (``|scale|``)."""
+
+    parameters: torch.Tensor | None
+    indices: torch.Tensor
+    scores: torch.Tensor
+    scales: torch.Tensor
+    densities: torch.Tensor
+
+
+def _normalized(x: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    norm = torch.linalg.vector_norm(x, dim=-1).clamp_min(torch.finfo(torch.float32).eps)
+    return x / norm[:, None], norm
+
+
+def _pad8(x: torch.Tensor) -> torch.Tensor:
+    extra = (-x.shape[-1]) % 8
+    return torch.nn.functional.pad(x, (0, extra)) if extra else x
+
+
+class DictionaryMatcher:
+    """Match signals against ``dictionary`` ``(atoms, contrasts)`` by normalized
+    complex inner products; ``parameters`` ``(atoms, n)`` are returned for the
+    matched atoms. ``top_k`` (1..8) candidates per voxel; voxels are matched
+    ``query_chunk_size`` at a time. Group matching (``groups``) is not built."""
+
+    def __init__(self, acquisition=None, *, dictionary: torch.Tensor | None = None,
+                 parameters: torch.Tensor | None = None, query_chunk_size: int = 65536,
+                 dictionary_chunk_size: int = 16384, top_k: int = 1, groups: int | None = None,
+                 prune: float = 5e-3, device: torch.device | str | None = None) -> None:
+        if acquisition is not None:
+            raise NotImplementedError("simulate the dictionary first and pass dictionary=")
+        if groups is not None:
+            raise NotImplementedError("group matching is not built")
+        if query_chunk_size < 1 or dictionary_chunk_size < 1:
+            raise ValueError("chunk sizes must be positive")
+        if not 1 <= top_k <= _native.library().tsg_match_candidates():
+            raise ValueError("top_k must be between 1 and 8")
+        if not 0.0 <= prune < 1.0:
+            raise ValueError(f"prune must be in [0, 1), got {prune}")
+        self.query_chunk_size = int(query_chunk_size)
+        self.dictionary_chunk_size = int(dictionary_chunk_size)
+        self.top_k = int(top_k)
+        self.device = engine.require_cuda(torch.device(device) if device is not None else None)
+        self.dictionary = None
+        if dictionary is not None:
+            self.fit(dictionary, parameters)
+
+    @property
+    def fitted(self) -> bool:
+        return self.dictionary is not None
+
+    def fit(self, dictionary: torch.Tensor, parameters: torch.Tensor | None = None):
+        """Adopt ``dictionary`` (and the parameter values of its atoms)."""
+        d = torch.as_tensor(dictionary)
+        if d.ndim != 2 or d.shape[0] < 1:
+            raise ValueError("dictionary must have shape (atoms, contrasts)")
+        if self.top_k > d.shape[0]:
+            raise ValueError("top_k must be between one and the atom count")
+        d = d.to(self.device, torch.complex64)
+        self.dictionary = d
+        self.normalized, norm = _normalized(d)
+        self.power = norm.square()
+        re, im = self.normalized.real, self.normalized.imag
+        # A real dictionary (or one on the imaginary axis, as the MRF signal
+        # 1j*s is) scores like its real profile: |<s, e^{i c} d>| = |<s, d>|.
+        if not bool(im.ne(0).any()):
+            self._screen_atoms, self._complex_atoms = re, False
+        elif not bool(re.ne(0).any()):
+            self._screen_atoms, self._complex_atoms = im, False
+        else:
+            self._screen_atoms, self._complex_atoms = torch.cat((re, im), dim=1), True
+        self._screen_atoms = _pad8(self._screen_atoms).to(torch.bfloat16).contiguous()
+        if parameters is None:
+            self.parameter_values = None
+        else:
+            p = torch.as_tensor(parameters, dtype=torch.float32, device=self.device)
+            p = p[:, None] if p.ndim == 1 else p
+            if p.ndim != 2 or p.shape[0] != d.shape[0]:
+                raise ValueError("parameters must have shape (atoms, parameters)")
+            self.parameter_values = p
+        return self
+
+    def _queries(self, s: torch.Tensor) -> torch.Tensor:
+        """Two bf16 rows per voxel whose products with the screen atoms are
+        Re and Im of <s, d>."""
+        if self._complex_atoms:
+            a = torch.cat((s.real, s.imag), dim=1)
+            b = torch.cat((s.imag, -s.real), dim=1)
+        else:
+            a, b = s.real, s.imag
+        rows = torch.stack((a, b), dim=1).reshape(2 * s.shape[0], -1)
+        return _pad8(rows).to(torch.bfloat16).contiguous()
+
+    @torch.no_grad()
+    def match(self, signals: torch.Tensor) -> MatchResult:
+        """Top-k atoms, scores, scales, densities and parameters per voxel."""
+        if not self.fitted:
+            raise RuntimeError("the matcher has no dictionary to match against")
+        signals = torch.as_tensor(signals)
+        if signals.shape[-1] != self.dictionary.shape[-1]:
+            raise ValueError("signal and dictionary contrast counts differ")
+        sample_shape = signals.shape[:-1]
+        flat = signals.reshape(-1, signals.shape[-1]).to(self.device, torch.complex64)
+        lib = _native.library()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        A, P = self.dictionary.shape
+        screen_k = self._screen_atoms.shape[1]
+        m = lib.tsg_match_candidates()
+        error = torch.zeros(1, dtype=torch.int32, device=self.device)
+        scores, indices = [], []
+        for chunk in flat.split(self.query_chunk_size):
+            V = chunk.shape[0]
+            s_hat, _ = _normalized(chunk)
+            queries = self._queries(s_hat)
+            cand_s = torch.empty((V, m), dtype=torch.float32, device=self.device)
+            cand_i = torch.empty((V, m), dtype=torch.int32, device=self.device)
+            _native.check(lib.tsg_match_screen(
+                queries.data_ptr(), 2 * V, self._screen_atoms.data_ptr(), A, screen_k,
+                cand_s.data_ptr(), cand_i.data_ptr(), error.data_ptr(), stream))
+            sc = torch.empty((V, self.top_k), dtype=torch.float32, device=self.device)
+            ix = torch.empty((V, self.top_k), dtype=torch.int64, device=self.device)
+            s_hat = s_hat.contiguous()
+            _native.check(lib.tsg_match_rescore(
+                s_hat.data_ptr(), V, self.normalized.data_ptr(), A, P, cand_i.data_ptr(),
+                self.top_k, sc.data_ptr(), ix.data_ptr(), stream))
+            scores.append(sc)
+            indices.append(ix)
+        if int(error.item()) != 0:
+            raise _native.NativeError(_native.TSG_ERR_CUDA,
+                                      f"matching kernel stopped waiting (stage {int(error.item())})")
+        scores = torch.cat(scores) if scores else torch.empty((0, self.top_k), device=self.device)
+        indices = (torch.cat(indices) if indices
+                   else torch.empty((0, self.top_k), dtype=torch.int64, device=self.device))
+        signal_norm = torch.linalg.vector_norm(flat, dim=-1).clamp_min(torch.finfo(torch.float32).eps)
+        densities = signal_norm[:, None] * scores / self.power[indices].sqrt()
+        atoms = self.dictionary[indices]
+        scales = torch.sum(atoms.conj() * flat[:, None, :], dim=-1) / self.power[indices]
+        shape = (*sample_shape, self.top_k)
+        params = None
+        if self.parameter_values is not None:
+            params = self.parameter_values[indices].reshape(*shape, -1)
+        return MatchResult(parameters=params, indices=indices.reshape(shape),
+                           scores=scores.reshape(shape), scales=scales.reshape(shape),
+                           densities=densities.reshape(shape))
+
+    def __call__(self, signals: torch.Tensor) -> torch.Tensor:
+        """Best parameter values (indices without parameters), per voxel."""
+        result = self.match(signals)
+        if result.parameters is None:
+            return result.indices[..., 0]
+        return result.parameters[..., 0, :]
