@@ -395,8 +395,8 @@ int tsg_gn_natural(const double* free_variables, int64_t voxel_count, const tsg_
 
 /* Screens every voxel against every atom on the tensor cores and writes each
  * voxel's best tsg_match_candidates() atoms by |<s, d>|^2, best first.
- * queries: bf16 (query_rows x k), two rows per voxel whose products with an
- * atom row are Re and Im of <s, d>; atoms: bf16 (atom_count x k); k a
+ * queries: fp16 (query_rows x k), two rows per voxel whose products with an
+ * atom row are Re and Im of <s, d>; atoms: fp16 (atom_count x k); k a
  * multiple of 8; both 16-byte aligned, DEVICE. candidate_scores / _index:
  * (query_rows / 2) x candidates. `error` (device int, zero on entry) is set
  * if a pipeline wait ran out. Replaces the chunked FP32 products and top-k of
@@ -406,12 +406,12 @@ int tsg_match_screen(const void* queries, int64_t query_rows, const void* atoms,
                      int32_t* candidate_index, int* error, void* stream);
 /* Exact FP32 |<s, d>| of each voxel's candidates against the normalized
  * complex64 signals (voxels x samples) and atoms (atom_count x samples);
- * writes the best top_k (1..candidates) scores and atom indices, best
+ * writes the best top_k (1..8) scores and atom indices, best
  * first. DEVICE pointers. */
 int tsg_match_rescore(const void* signals, int64_t voxels, const void* atoms, int64_t atom_count,
                       int64_t samples, const int32_t* candidate_index, int top_k, float* scores,
                       int64_t* index, void* stream);
-/* Candidates the screen keeps per voxel (8). */
+/* Candidates the screen keeps per voxel (16). */
 int tsg_match_candidates(void);
 
 /* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */

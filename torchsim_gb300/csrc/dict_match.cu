@@ -4,15 +4,18 @@
 // every normalized measurement against every normalized atom by |<s, d>|
 // through chunked FP32 matrix products (_grouped.py:212-240) and keeps the
 // top k. Here one kernel does the product and the selection without ever
-// writing the score matrix: queries (two rows per voxel) and atoms are bf16
+// writing the score matrix: queries (two rows per voxel) and atoms are fp16
 // K-major tiles brought by TMA into a 4-stage shared-memory ring;
 // `tcgen05.mma` (issued by one thread) accumulates a 128 x 256 tile in tensor
 // memory, double-buffered so the epilogue of one atom tile overlaps the MMAs of
-// the next; four epilogue warps read the accumulator with `tcgen05.ld`, pair
-// each voxel's two rows into |<s, d>|^2 and keep its best kScreen atoms. A
-// second kernel rescores those candidates exactly in FP32 against the complex
-// signals and atoms and keeps the top k, so the bf16 screen decides only which
-// few atoms are compared exactly.
+// the next; four epilogue warps read the accumulator with `tcgen05.ld`. The
+// two lanes holding a voxel's rows exchange one value per pair of atoms, so
+// each lane forms |<s, d>|^2 for every other atom and keeps its best kScreen
+// (a voxel keeps 2 * kScreen); a chunk of 32 atoms whose best does not beat a
+// lane's current last place costs no insertion work. A second kernel rescores
+// those candidates exactly in FP32 against the complex signals and atoms and
+// keeps the top k, so the fp16 screen decides only which few atoms are
+// compared exactly.
 //
 // Rows of the query matrix: voxel v owns rows 2v and 2v+1. For real atoms
 // (an SSFP fingerprint) they are (Re s_v, Im s_v) against the atom; for
@@ -30,7 +33,8 @@ namespace tsg {
 namespace {
 
 constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
-constexpr int kScreen = 8;
+constexpr int kScreen = 8;           // per lane
+constexpr int kCand = 2 * kScreen;    // per voxel
 constexpr int SMEM_A = BM * BK * 2;
 constexpr int SMEM_B = BN * BK * 2;
 constexpr int STAGE_BYTES = SMEM_A + SMEM_B;
@@ -60,7 +64,7 @@ __device__ __forceinline__ void arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-// Shared-memory matrix descriptor of a K-major bf16 tile with 128-byte
+// Shared-memory matrix descriptor of a K-major 16-bit tile with 128-byte
 // swizzle: 8-row groups 1024 bytes apart, rows of 128 bytes.
 __device__ __forceinline__ uint64_t tile_desc(uint32_t addr) {
     uint64_t d = 0;
@@ -72,10 +76,9 @@ __device__ __forceinline__ uint64_t tile_desc(uint32_t addr) {
     return d;
 }
 
-// kind::f16 instruction descriptor: FP32 accumulate, bf16 A and B, both
-// K-major, M = BM, N = BN.
-constexpr uint32_t kInstr = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) |
-                            (uint32_t(BM >> 4) << 24);
+// kind::f16 instruction descriptor: FP32 accumulate, fp16 A and B (format
+// 0), both K-major, M = BM, N = BN.
+constexpr uint32_t kInstr = (1u << 4) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
 
 struct ScreenShared {
     uint64_t full[STAGES];
@@ -214,9 +217,12 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
     } else {
-        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = tile rows.
+        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = tile rows. A
+        // voxel's rows sit on lanes 2i (Re) and 2i+1 (Im); lane parity p
+        // scores the atoms of column parity p.
         const int quarter = warp & 3;
         const int r = quarter * 32 + lane;
+        const int parity = lane & 1;
         float best_s[kScreen];
         int best_i[kScreen];
 #pragma unroll
@@ -224,7 +230,6 @@ __global__ void __launch_bounds__(kThreads, 1)
             best_s[k] = -1.f;
             best_i[k] = -1;
         }
-        const bool even = (lane & 1) == 0;
         for (int n = 0; n < n_tiles && !*abort; ++n) {
             const int b = n & 1;
             const uint32_t use = uint32_t(n >> 1);
@@ -240,24 +245,36 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * BN + c * 32);
                 TSG_LD32(v, taddr);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                float sc[16];
+                float chunk_best = -1.f;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float x = __uint_as_float(v[j]);
-                    const float x2 = x * x;
-                    const float score = x2 + __shfl_xor_sync(0xffffffffu, x2, 1);
-                    const int atom = n * BN + c * 32 + j;
-                    if (even && atom < atoms && score > best_s[kScreen - 1]) {
-                        best_s[kScreen - 1] = score;
-                        best_i[kScreen - 1] = atom;
+                for (int j = 0; j < 16; ++j) {
+                    const float x0 = __uint_as_float(v[2 * j]), x1 = __uint_as_float(v[2 * j + 1]);
+                    // Send the partner the value of its column; keep our own.
+                    const float mine = parity ? x1 : x0;
+                    const float other = __shfl_xor_sync(0xffffffffu, parity ? x0 : x1, 1);
+                    sc[j] = fmaf(mine, mine, other * other);
+                    chunk_best = fmaxf(chunk_best, sc[j]);
+                }
+                if (chunk_best > best_s[kScreen - 1]) {
+                    const int atom0 = n * BN + c * 32 + parity;
+#pragma unroll 1
+                    for (int j = 0; j < 16; ++j) {
+                        const int atom = atom0 + 2 * j;
+                        const float score = sc[j];
+                        if (atom < atoms && score > best_s[kScreen - 1]) {
+                            best_s[kScreen - 1] = score;
+                            best_i[kScreen - 1] = atom;
 #pragma unroll
-                        for (int k = kScreen - 1; k > 0; --k) {
-                            if (best_s[k] > best_s[k - 1]) {
-                                const float ts = best_s[k];
-                                best_s[k] = best_s[k - 1];
-                                best_s[k - 1] = ts;
-                                const int ti = best_i[k];
-                                best_i[k] = best_i[k - 1];
-                                best_i[k - 1] = ti;
+                            for (int k = kScreen - 1; k > 0; --k) {
+                                if (best_s[k] > best_s[k - 1]) {
+                                    const float ts = best_s[k];
+                                    best_s[k] = best_s[k - 1];
+                                    best_s[k - 1] = ts;
+                                    const int ti = best_i[k];
+                                    best_i[k] = best_i[k - 1];
+                                    best_i[k - 1] = ti;
+                                }
                             }
                         }
                     }
@@ -266,13 +283,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             arrive(smem_u32(&sh->tempty[b]));
         }
-        const int64_t row = row0 + r;
-        if (even && row < rows) {
+        const int64_t row = row0 + (r & ~1);
+        if (row < rows) {
             const int64_t voxel = row >> 1;
 #pragma unroll
             for (int k = 0; k < kScreen; ++k) {
-                cand_score[voxel * kScreen + k] = best_s[k];
-                cand_index[voxel * kScreen + k] = best_i[k];
+                cand_score[voxel * kCand + parity * kScreen + k] = best_s[k];
+                cand_index[voxel * kCand + parity * kScreen + k] = best_i[k];
             }
         }
     }
@@ -298,11 +315,11 @@ __global__ void rescore_kernel(const float2* __restrict__ signals, const float2*
     const int lane = threadIdx.x & 31;
     if (voxel >= voxels) return;
     const float2* s = signals + voxel * samples;
-    float best_s[kScreen];
-    int best_i[kScreen];
+    float best_s[kCand];
+    int best_i[kCand];
 #pragma unroll
-    for (int k = 0; k < kScreen; ++k) {
-        const int a = cand[voxel * kScreen + k];
+    for (int k = 0; k < kCand; ++k) {
+        const int a = cand[voxel * kCand + k];
         float re = 0.f, im = 0.f;
         if (a >= 0) {
             const float2* d = atoms + int64_t(a) * samples;
@@ -325,7 +342,7 @@ __global__ void rescore_kernel(const float2* __restrict__ signals, const float2*
     // Descending by score, ties to the lower atom index.
     for (int k = 0; k < top_k; ++k) {
         int pick = k;
-        for (int j = k + 1; j < kScreen; ++j) {
+        for (int j = k + 1; j < kCand; ++j) {
             const bool better = best_s[j] > best_s[pick] ||
                                 (best_s[j] == best_s[pick] && best_i[j] >= 0 &&
                                  (best_i[pick] < 0 || best_i[j] < best_i[pick]));
@@ -367,7 +384,7 @@ int tile_map(CUtensorMap* map, const void* base, int64_t rows, int64_t k, int bo
     const cuuint64_t strides[1] = {cuuint64_t(k) * 2};
     const cuuint32_t box[2] = {cuuint32_t(BK), cuuint32_t(box_rows)};
     const cuuint32_t elem[2] = {1, 1};
-    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims,
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims,
                           strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
                           CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -428,4 +445,4 @@ extern "C" int tsg_match_rescore(const void* signals, int64_t voxels, const void
     return TSG_OK;
 }
 
-extern "C" int tsg_match_candidates(void) { return kScreen; }
+extern "C" int tsg_match_candidates(void) { return kCand; }

@@ -8,11 +8,12 @@ scale (proton density and receive phase), its size and the atoms' parameter
 values.
 
 The search is one tensor-core kernel per chunk of voxels
-(``tsg_match_screen``): bf16 products accumulated in FP32 in tensor memory,
-with the selection of each voxel's best few atoms fused into the epilogue, so
-the voxel x atom score matrix never exists. The few candidates are then
-rescored exactly in FP32 against the complex signals (``tsg_match_rescore``)
-and the top k kept, so the bf16 screen only narrows which atoms are compared.
+(``tsg_match_screen``): fp16 products (normalized values, 11-bit significand)
+accumulated in FP32 in tensor memory, with the selection of each voxel's best
+16 atoms fused into the epilogue, so the voxel x atom score matrix never
+exists. The candidates are then rescored exactly in FP32 against the complex
+signals (``tsg_match_rescore``) and the top k kept, so the fp16 screen only
+narrows which atoms are compared exactly.
 """
 
 from __future__ import annotations
@@ -67,7 +68,7 @@ class DictionaryMatcher:
             raise NotImplementedError("group matching is not built")
         if query_chunk_size < 1 or dictionary_chunk_size < 1:
             raise ValueError("chunk sizes must be positive")
-        if not 1 <= top_k <= _native.library().tsg_match_candidates():
+        if not 1 <= top_k <= 8:
             raise ValueError("top_k must be between 1 and 8")
         if not 0.0 <= prune < 1.0:
             raise ValueError(f"prune must be in [0, 1), got {prune}")
@@ -103,7 +104,7 @@ class DictionaryMatcher:
             self._screen_atoms, self._complex_atoms = im, False
         else:
             self._screen_atoms, self._complex_atoms = torch.cat((re, im), dim=1), True
-        self._screen_atoms = _pad8(self._screen_atoms).to(torch.bfloat16).contiguous()
+        self._screen_atoms = _pad8(self._screen_atoms).to(torch.float16).contiguous()
         if parameters is None:
             self.parameter_values = None
         else:
@@ -115,7 +116,7 @@ class DictionaryMatcher:
         return self
 
     def _queries(self, s: torch.Tensor) -> torch.Tensor:
-        """Two bf16 rows per voxel whose products with the screen atoms are
+        """Two fp16 rows per voxel whose products with the screen atoms are
         Re and Im of <s, d>."""
         if self._complex_atoms:
             a = torch.cat((s.real, s.imag), dim=1)
@@ -123,7 +124,7 @@ class DictionaryMatcher:
         else:
             a, b = s.real, s.imag
         rows = torch.stack((a, b), dim=1).reshape(2 * s.shape[0], -1)
-        return _pad8(rows).to(torch.bfloat16).contiguous()
+        return _pad8(rows).to(torch.float16).contiguous()
 
     @torch.no_grad()
     def match(self, signals: torch.Tensor) -> MatchResult:
