@@ -396,7 +396,8 @@ int tsg_gn_natural(const double* free_variables, int64_t voxel_count, const tsg_
 /* Screens every voxel against every atom on the tensor cores and writes each
  * voxel's best tsg_match_candidates() atoms by |<s, d>|^2, best first.
  * queries: fp16 (query_rows x k), two rows per voxel whose products with an
- * atom row are Re and Im of <s, d>; atoms: fp16 (atom_count x k); k a
+ * atom row are Re and Im of <s, d>; atoms: fp16 (tsg_match_screen_rows(atom_count)
+ * x k, rows permuted as described there); k a
  * multiple of 8; both 16-byte aligned, DEVICE. candidate_scores / _index:
  * (query_rows / 2) x candidates. `error` (device int, zero on entry) is set
  * if a pipeline wait ran out. Replaces the chunked FP32 products and top-k of
@@ -411,8 +412,12 @@ int tsg_match_screen(const void* queries, int64_t query_rows, const void* atoms,
 int tsg_match_rescore(const void* signals, int64_t voxels, const void* atoms, int64_t atom_count,
                       int64_t samples, const int32_t* candidate_index, int top_k, float* scores,
                       int64_t* index, void* stream);
-/* Candidates the screen keeps per voxel (16). */
+/* Candidates the screen keeps per voxel (32). */
 int tsg_match_candidates(void);
+/* Rows of the atom matrix tsg_match_screen reads for atom_count atoms (a
+ * multiple of 64): atom i sits at row (i & 1) | ((i >> 1) & 1) << 5 |
+ * ((i >> 2) & 15) << 1 | (i & ~63); the other rows are zero. */
+int tsg_match_screen_rows(int64_t atom_count);
 
 /* ---- drop-ins for the reference's native boundary (HOST pointers) ------ */
 

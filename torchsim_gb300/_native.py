@@ -138,6 +138,7 @@ SIGNATURES: dict[str, tuple] = {
     "tsg_match_screen": (_int, [_vp, _i64, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
     "tsg_match_rescore": (_int, [_vp, _i64, _vp, _i64, _i64, _vp, _int, _vp, _vp, _vp]),
     "tsg_match_candidates": (_int, []),
+    "tsg_match_screen_rows": (_int, [_i64]),
     "tsg_epg_simulate_vjp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
                                     _int, _int]),
     "tsg_epg_simulate": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64, _int,

@@ -8,11 +8,13 @@
 // K-major tiles brought by TMA into a 4-stage shared-memory ring;
 // `tcgen05.mma` (issued by one thread) accumulates a 128 x 256 tile in tensor
 // memory, double-buffered so the epilogue of one atom tile overlaps the MMAs of
-// the next; four epilogue warps read the accumulator with `tcgen05.ld`. The
-// two lanes holding a voxel's rows exchange one value per pair of atoms, so
-// each lane forms |<s, d>|^2 for every other atom and keeps its best kScreen
-// (a voxel keeps 2 * kScreen); a chunk of 32 atoms whose best does not beat a
-// lane's current last place costs no insertion work. A second kernel rescores
+// the next; eight epilogue warps (two per TMEM lane quarter, each taking every
+// other 32-column chunk) read the accumulator with `tcgen05.ld`. The two lanes
+// holding a voxel's rows exchange one value per pair of atoms; each (warp,
+// lane) keeps its best kScreen atoms of one (chunk parity, column parity)
+// class, so a voxel keeps kCand = 32; the atoms are stored permuted so that
+// neighbouring atoms land in different classes. A chunk of atoms whose best
+// does not beat a lane's current last place costs no insertion work. A second kernel rescores
 // those candidates exactly in FP32 against the complex signals and atoms and
 // keeps the top k, so the fp16 screen decides only which few atoms are
 // compared exactly.
@@ -34,12 +36,16 @@ namespace {
 
 constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
 constexpr int kScreen = 8;           // per lane
-constexpr int kCand = 2 * kScreen;    // per voxel
+constexpr int kHalves = 2;            // epilogue warps per TMEM lane quarter
+constexpr int kCand = 2 * kHalves * kScreen;  // per voxel
 constexpr int SMEM_A = BM * BK * 2;
 constexpr int SMEM_B = BN * BK * 2;
 constexpr int STAGE_BYTES = SMEM_A + SMEM_B;
 constexpr int TMEM_COLS = 2 * BN;
-constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM, warps 2-5 epilogue
+constexpr int kEpilogueThreads = 128 * kHalves;
+// warp 0 TMA, warp 1 MMA + TMEM, warps 2.. epilogue (each lane quarter twice:
+// one warp per half of the accumulator's columns).
+constexpr int kThreads = 64 + kEpilogueThreads;
 constexpr long long kWaitLimit = 1LL << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -58,6 +64,15 @@ __device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
         if (ok) return true;
     }
     return false;
+}
+
+// The screen matrix stores atom i at row pos(i), which moves bit 1 of i to
+// bit 5 and bits 2-5 down by one, within blocks of 64: consecutive atoms then
+// alternate in column parity and in 32-column chunk parity, so they fall in
+// four different candidate lists of the voxel (dictionaries put neighbouring
+// atoms next to each other). This is the inverse: the atom at row `pos`.
+__host__ __device__ __forceinline__ int stored_atom(int pos) {
+    return (pos & 1) | (((pos >> 5) & 1) << 1) | (((pos >> 1) & 15) << 2) | (pos & ~63);
 }
 
 __device__ __forceinline__ void arrive(uint32_t bar) {
@@ -102,15 +117,15 @@ struct ScreenShared {
 
 __global__ void __launch_bounds__(kThreads, 1)
     screen_kernel(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap amap,
-                  int64_t rows, int64_t atoms, int k_tiles, float* cand_score, int32_t* cand_index,
-                  int* error) {
+                  int64_t rows, int64_t atoms, int64_t stored_rows, int k_tiles, float* cand_score,
+                  int32_t* cand_index, int* error) {
     extern __shared__ uint8_t s_raw[];
     uint8_t* tiles = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(s_raw) + 1023) & ~uintptr_t(1023));
     ScreenShared* sh = reinterpret_cast<ScreenShared*>(tiles + STAGES * STAGE_BYTES);
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int64_t row0 = int64_t(blockIdx.x) * BM;
-    const int n_tiles = int((atoms + BN - 1) / BN);
+    const int n_tiles = int((stored_rows + BN - 1) / BN);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -119,7 +134,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int b = 0; b < 2; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sh->tfull[b])));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&sh->tempty[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&sh->tempty[b])),
+                         "r"(kEpilogueThreads));
         }
         sh->abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -217,10 +233,12 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
         }
     } else {
-        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = tile rows. A
-        // voxel's rows sit on lanes 2i (Re) and 2i+1 (Im); lane parity p
-        // scores the atoms of column parity p.
+        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = tile rows, in
+        // the columns of its half of the accumulator. A voxel's rows sit on
+        // lanes 2i (Re) and 2i+1 (Im); lane parity p scores the atoms of
+        // column parity p.
         const int quarter = warp & 3;
+        const int half = (warp - 2) / 4;
         const int r = quarter * 32 + lane;
         const int parity = lane & 1;
         float best_s[kScreen];
@@ -240,7 +258,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll 1
-            for (int c = 0; c < BN / 32; ++c) {
+            for (int cc = 0; cc < BN / 64; ++cc) {
+                // The warp of half h takes the 32-column chunks of parity h.
+                const int c = 2 * cc + half;
                 uint32_t v[32];
                 const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * BN + c * 32);
                 TSG_LD32(v, taddr);
@@ -257,10 +277,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     chunk_best = fmaxf(chunk_best, sc[j]);
                 }
                 if (chunk_best > best_s[kScreen - 1]) {
-                    const int atom0 = n * BN + c * 32 + parity;
+                    const int pos0 = n * BN + c * 32 + parity;
 #pragma unroll 1
                     for (int j = 0; j < 16; ++j) {
-                        const int atom = atom0 + 2 * j;
+                        const int atom = stored_atom(pos0 + 2 * j);
                         const float score = sc[j];
                         if (atom < atoms && score > best_s[kScreen - 1]) {
                             best_s[kScreen - 1] = score;
@@ -288,8 +308,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int64_t voxel = row >> 1;
 #pragma unroll
             for (int k = 0; k < kScreen; ++k) {
-                cand_score[voxel * kCand + parity * kScreen + k] = best_s[k];
-                cand_index[voxel * kCand + parity * kScreen + k] = best_i[k];
+                cand_score[voxel * kCand + (half * 2 + parity) * kScreen + k] = best_s[k];
+                cand_index[voxel * kCand + (half * 2 + parity) * kScreen + k] = best_i[k];
             }
         }
     }
@@ -317,7 +337,7 @@ __global__ void rescore_kernel(const float2* __restrict__ signals, const float2*
     const float2* s = signals + voxel * samples;
     float best_s[kCand];
     int best_i[kCand];
-#pragma unroll
+#pragma unroll 4
     for (int k = 0; k < kCand; ++k) {
         const int a = cand[voxel * kCand + k];
         float re = 0.f, im = 0.f;
@@ -398,6 +418,10 @@ int tile_map(CUtensorMap* map, const void* base, int64_t rows, int64_t k, int bo
 
 using namespace tsg;
 
+extern "C" int tsg_match_screen_rows(int64_t atom_count) {
+    return int((atom_count + 63) / 64 * 64);
+}
+
 extern "C" int tsg_match_screen(const void* queries, int64_t query_rows, const void* atoms,
                                 int64_t atom_count, int64_t k, float* candidate_scores,
                                 int32_t* candidate_index, int* error, void* stream) {
@@ -414,15 +438,17 @@ extern "C" int tsg_match_screen(const void* queries, int64_t query_rows, const v
     if (query_rows > (int64_t(1) << 31) || atom_count > (int64_t(1) << 31) - BN)
         return fail(TSG_ERR_CAPACITY, "matrix too large");
     CUtensorMap qmap, amap;
+    const int64_t stored_rows = (atom_count + 63) / 64 * 64;
     int rc = tile_map(&qmap, queries, query_rows, k, BM);
-    if (!rc) rc = tile_map(&amap, atoms, atom_count, k, BN);
+    if (!rc) rc = tile_map(&amap, atoms, stored_rows, k, BN);
     if (rc) return rc;
     const size_t smem = 1024 + STAGES * STAGE_BYTES + sizeof(ScreenShared);
     TSG_CUDA(cudaFuncSetAttribute(screen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     const int k_tiles = int((k + BK - 1) / BK);
     const unsigned blocks = unsigned((query_rows + BM - 1) / BM);
     screen_kernel<<<blocks, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(
-        qmap, amap, query_rows, atom_count, k_tiles, candidate_scores, candidate_index, error);
+        qmap, amap, query_rows, atom_count, stored_rows, k_tiles, candidate_scores,
+        candidate_index, error);
     TSG_CUDA(cudaGetLastError());
     return TSG_OK;
 }
@@ -431,7 +457,7 @@ extern "C" int tsg_match_rescore(const void* signals, int64_t voxels, const void
                                  int64_t atom_count, int64_t samples,
                                  const int32_t* candidate_index, int top_k, float* scores,
                                  int64_t* index, void* stream) {
-    if (voxels < 0 || atom_count < 1 || samples < 1 || top_k < 1 || top_k > kScreen)
+    if (voxels < 0 || atom_count < 1 || samples < 1 || top_k < 1 || top_k > 8)
         return fail(TSG_ERR_ARGUMENT, "invalid rescoring dimensions (top_k must be 1..8)");
     if (voxels == 0) return TSG_OK;
     if (!signals || !atoms || !candidate_index || !scores || !index)

@@ -10,7 +10,7 @@ values.
 The search is one tensor-core kernel per chunk of voxels
 (``tsg_match_screen``): fp16 products (normalized values, 11-bit significand)
 accumulated in FP32 in tensor memory, with the selection of each voxel's best
-16 atoms fused into the epilogue, so the voxel x atom score matrix never
+32 atoms fused into the epilogue, so the voxel x atom score matrix never
 exists. The candidates are then rescored exactly in FP32 against the complex
 signals (``tsg_match_rescore``) and the top k kept, so the fp16 screen only
 narrows which atoms are compared exactly.
@@ -104,7 +104,18 @@ class DictionaryMatcher:
             self._screen_atoms, self._complex_atoms = im, False
         else:
             self._screen_atoms, self._complex_atoms = torch.cat((re, im), dim=1), True
-        self._screen_atoms = _pad8(self._screen_atoms).to(torch.float16).contiguous()
+        screen = _pad8(self._screen_atoms).to(torch.float16)
+        # The kernel reads atom i from row pos(i) (bit 1 of i moved to bit 5,
+        # bits 2-5 down by one, within blocks of 64) of a matrix padded to a
+        # multiple of 64 rows, so neighbouring atoms fall in different
+        # candidate lists.
+        A = screen.shape[0]
+        rows = int(_native.library().tsg_match_screen_rows(A))
+        i = torch.arange(A, device=self.device)
+        pos = (i & 1) | (((i >> 1) & 1) << 5) | (((i >> 2) & 15) << 1) | (i & ~63)
+        stored = torch.zeros((rows, screen.shape[1]), dtype=torch.float16, device=self.device)
+        stored[pos] = screen
+        self._screen_atoms = stored
         if parameters is None:
             self.parameter_values = None
         else:
@@ -139,7 +150,7 @@ class DictionaryMatcher:
         lib = _native.library()
         stream = torch.cuda.current_stream(self.device).cuda_stream
         A, P = self.dictionary.shape
-        screen_k = self._screen_atoms.shape[1]
+        screen_k = self._screen_atoms.shape[1]  # rows: the padded, permuted atoms
         m = lib.tsg_match_candidates()
         error = torch.zeros(1, dtype=torch.int32, device=self.device)
         scores, indices = [], []
