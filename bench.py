@@ -577,10 +577,11 @@ def match_section(torch, device, voxels: int = 65536, repeats: int = 3) -> dict:
     s_hat = measured / torch.linalg.vector_norm(measured, dim=-1, keepdim=True)
     queries = matcher._queries(s_hat)
     k = matcher._screen_atoms.shape[1]
-    cand_s = torch.empty((voxels, 8), dtype=torch.float32, device=device)
-    cand_i = torch.empty((voxels, 8), dtype=torch.int32, device=device)
-    err = torch.zeros(1, dtype=torch.int32, device=device)
     lib = _native.library()
+    cands = lib.tsg_match_candidates()
+    cand_s = torch.empty((voxels, cands), dtype=torch.float32, device=device)
+    cand_i = torch.empty((voxels, cands), dtype=torch.int32, device=device)
+    err = torch.zeros(1, dtype=torch.int32, device=device)
 
     def screen():
         _native.check(lib.tsg_match_screen(queries.data_ptr(), 2 * voxels,
