@@ -291,6 +291,91 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                     goto after_rf;
                 }
             }
+            // The folded tangent step keeps more values live than the
+            // unfolded one; under a tight register budget (5 or more blocks
+            // per SM) the spills it causes cost more than it saves.
+            if constexpr (NT > 0 && !GEN && MINB < 5) {
+                if (relax && rf == RF_ROTATE && n1 == 0) {
+                    // Relaxation folded into the rotation for the primal and
+                    // every tangent: with X0 the state before the interval,
+                    // X = E X0 + r and dX = E dX0 + dE X0 (+ dr), so the pulse
+                    // acts through R E on X0, on dX0 + E^-1 dE X0 (T2 adds
+                    // dt w2 (p, m), T1 dt w1 z), and the recovery r and its
+                    // T1 derivative enter order 0 after the fact.
+                    float si, co;
+                    if constexpr (L > 1) {
+                        si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
+                        co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
+                    } else {
+                        sincosf(op.flip * b1, &si, &co);
+                    }
+                    const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
+                    const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
+                    const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
+                    const float2 czp = dup(hs * e2), czz = dup(co * e1);
+                    const float2 cvw = dup(0.5f * co * e2);  // V = d(Zn)/d alpha
+                    float at_b1 = 0.f;
+                    if constexpr (S::B1) at_b1 = op.flip;
+                    const float2 g1 = dup(op.dt * w1), g2 = dup(op.dt * w2);
+#pragma unroll
+                    for (int k = 0; k < RP; ++k) {
+                        const float2 p = P[k], m = M[k], z = Z[k];
+                        const float2 w = fma2(neg1, m, p);
+                        const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
+                        const float2 Pn = fma2(cpp, p, fma2(cpm, m, nt));
+                        const float2 Mn = fma2(cpm, p, fma2(cpp, m, t));
+                        const float2 Zn = fma2(czp, w, mul2(czz, z));
+                        float2 V = dup(0.f);
+                        if constexpr (S::B1) V = fma2(cvw, w, nt);
+#pragma unroll
+                        for (int j = 0; j < NT; ++j) {
+                            float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
+                            if (S::T1 && j == S::I_T1) dz = fma2(g1, z, dz);
+                            if (S::T2 && j == S::I_T2) {
+                                dp = fma2(g2, p, dp);
+                                dm = fma2(g2, m, dm);
+                            }
+                            const float2 dt_ = mul2(cpz, dz), ndt = mul2(ncpz, dz);
+                            float2 np = fma2(cpp, dp, fma2(cpm, dm, ndt));
+                            float2 nm = fma2(cpm, dp, fma2(cpp, dm, dt_));
+                            float2 nz = fma2(czp, fma2(neg1, dm, dp), mul2(czz, dz));
+                            if (S::B1 && j == S::I_B1) {
+                                // d alpha / d B1 = flip: (-Zn, Zn, V) of the relaxed state.
+                                np = fma2(dup(-at_b1), Zn, np);
+                                nm = fma2(dup(at_b1), Zn, nm);
+                                nz = fma2(dup(at_b1), V, nz);
+                            }
+                            dP[j][k] = np;
+                            dM[j][k] = nm;
+                            dZ[j][k] = nz;
+                        }
+                        P[k] = Pn;
+                        M[k] = Mn;
+                        Z[k] = Zn;
+                    }
+                    if (q == 0) {
+                        // The recovery (1 - e1) of order 0 and its T1
+                        // derivative (-k1) through the pulse: R (0, 0, c) =
+                        // (-si c, si c, co c); for B1 the recovery also moves
+                        // Zn (used above without it) and V by (co, -si) c.
+                        const float rec = 1.f - e1;
+                        if constexpr (S::B1) {
+                            dP[S::I_B1][0].x = fmaf(-at_b1 * co, rec, dP[S::I_B1][0].x);
+                            dM[S::I_B1][0].x = fmaf(at_b1 * co, rec, dM[S::I_B1][0].x);
+                            dZ[S::I_B1][0].x = fmaf(-at_b1 * si, rec, dZ[S::I_B1][0].x);
+                        }
+                        if constexpr (S::T1) {
+                            dP[S::I_T1][0].x = fmaf(si, k1, dP[S::I_T1][0].x);
+                            dM[S::I_T1][0].x = fmaf(-si, k1, dM[S::I_T1][0].x);
+                            dZ[S::I_T1][0].x = fmaf(-co, k1, dZ[S::I_T1][0].x);
+                        }
+                        P[0].x = fmaf(-si, rec, P[0].x);
+                        M[0].x = fmaf(si, rec, M[0].x);
+                        Z[0].x = fmaf(co, rec, Z[0].x);
+                    }
+                    goto after_rf;
+                }
+            }
             if (relax) {
                 const float2 E1 = dup(e1), E2 = dup(e2);
                 float e1g = 0.f, e2g = 0.f;
