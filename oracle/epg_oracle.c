@@ -20,6 +20,8 @@
  *   run_forward           simulate_real_range              3041-3128
  *   run_tangent           simulate_real_jvp_range          3136-3285
  *   run_adjoint           simulate_real_vjp_range          5985-6232
+ *   run_second            simulate_real_vjp_jvp_range      7028-7330
+ *                         (dual arithmetic 346-365, 407-418, 768-775, 6964-6967)
  *   run_forward_complex   simulate_range<INSTANT, ONE>     4216-4566
  *                         with shift 2164-2174, rotate 2176-2208
  * Action bits are the packed action word (_epg_cpu.cpp:36-41,
@@ -446,6 +448,222 @@ static void run_adjoint(const oracle_case* c, const float* seed_imag,
     free(traj);
 }
 
+/* ---- second order: forward over reverse ---------------------------------- */
+
+/* A value and its derivative along one direction, with the reference's
+ * DualFloat products (_epg_cpu.cpp:346-365): the tangent of a*b is
+ * a.t*b.v + a.v*b.t, in that order. */
+typedef struct {
+    REAL v, t;
+} dual;
+
+static inline dual dl(REAL v, REAL t) {
+    dual r;
+    r.v = v;
+    r.t = t;
+    return r;
+}
+static inline dual dadd(dual a, dual b) { return dl(a.v + b.v, a.t + b.t); }
+static inline dual dsub(dual a, dual b) { return dl(a.v - b.v, a.t - b.t); }
+static inline dual dmul(dual a, dual b) { return dl(a.v * b.v, a.t * b.v + a.v * b.t); }
+static inline dual dscale(REAL a, dual b) { return dl(a * b.v, a * b.t); }
+static inline dual dexp(dual a) {
+    const REAL v = EXP(a.v);
+    return dl(v, v * a.t);
+}
+static inline dual dinv_square(dual a) {
+    const REAL inverse = LIT(1.0) / (a.v * a.v);
+    return dl(inverse, LIT(-2.0) * a.t * inverse / a.v);
+}
+
+static void dshift(dual* plus, dual* minus, int64_t states) {
+    for (int64_t s = 0; s + 1 < states; ++s) minus[s] = minus[s + 1];
+    minus[states - 1] = dl(LIT(0.0), LIT(0.0));
+    for (int64_t s = states - 1; s > 0; --s) plus[s] = plus[s - 1];
+    plus[0] = dsub(dl(LIT(0.0), LIT(0.0)), minus[0]);
+}
+
+static void dshift_adjoint(dual* plus_bar, dual* minus_bar, int64_t states) {
+    const dual carry = dsub(dl(LIT(0.0), LIT(0.0)), plus_bar[0]);
+    for (int64_t s = 0; s + 1 < states; ++s) plus_bar[s] = plus_bar[s + 1];
+    plus_bar[states - 1] = dl(LIT(0.0), LIT(0.0));
+    for (int64_t s = states - 1; s > 0; --s) minus_bar[s] = minus_bar[s - 1];
+    minus_bar[0] = dl(LIT(0.0), LIT(0.0));
+    if (states > 1) minus_bar[1] = dadd(minus_bar[1], carry);
+}
+
+/* The first-order adjoint run in dual numbers along direction d, with the
+ * seed on the imaginary output plane (_epg_cpu.cpp:7028-7330): the value
+ * parts of the gradients are J^T seed (the gradient with respect to the
+ * direction), the tangent parts the derivative of that along d (the
+ * curvature, the gradient of <seed, J d> with respect to the inputs).
+ * Gradients add into value[7] and curve[7], each ordered t1, t2, m0, b1,
+ * inversion (per atom), flip, duration (per train and event). Tissue
+ * directions follow the reference's feature flags: m0, b1 and inversion
+ * carry their direction only where the property itself is given. */
+static void run_second(const oracle_case* c, const oracle_direction* d, const float* seed_imag,
+                       int64_t begin, int64_t end, REAL* const* value, REAL* const* curve) {
+    const int64_t S = c->state_count;
+    const int64_t E = c->event_count;
+    const dual zero = dl(LIT(0.0), LIT(0.0));
+    const dual one = dl(LIT(1.0), LIT(0.0));
+    dual* traj = (dual*)malloc(sizeof(dual) * (size_t)(E > 0 ? E : 1) * (size_t)(3 * S));
+    dual* buf = (dual*)calloc((size_t)(9 * S), sizeof(dual));
+    dual *plus = buf, *minus = buf + S, *lon = buf + 2 * S;
+    dual *pb = buf + 3 * S, *mb = buf + 4 * S, *zb = buf + 5 * S;
+    dual *ps = buf + 6 * S, *ms = buf + 7 * S, *zs = buf + 8 * S;
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / c->atom_count;
+        const int64_t atom = work % c->atom_count;
+        const int64_t ebase = train * E;
+        const float* duration = c->duration_s + ebase;
+        const float* flip = c->flip_rad + ebase;
+        const int64_t out_base = (train * c->atom_count + atom) * c->output_count;
+        const dual t1 = dl((REAL)c->t1_ms[atom], tissue(d->t1_ms, atom, LIT(0.0)));
+        const dual t2 = dl((REAL)c->t2_ms[atom], tissue(d->t2_ms, atom, LIT(0.0)));
+        const dual m0 = c->m0 ? dl((REAL)c->m0[atom], tissue(d->m0, atom, LIT(0.0))) : one;
+        const dual b1 = c->b1 ? dl((REAL)c->b1[atom], tissue(d->b1, atom, LIT(0.0))) : one;
+        const dual inversion =
+            c->inversion ? dl((REAL)c->inversion[atom], tissue(d->inversion, atom, LIT(0.0)))
+                         : one;
+        const dual r1 = dl(LIT(1000.0) / t1.v, LIT(-1000.0) * t1.t / (t1.v * t1.v));
+        const dual r2 = dl(LIT(1000.0) / t2.v, LIT(-1000.0) * t2.t / (t2.v * t2.v));
+        for (int64_t s = 0; s < 9 * S; ++s) buf[s] = zero;
+        lon[0] = one;
+        for (int64_t e = 0; e < E; ++e) {
+            dual* slot = traj + e * 3 * S;
+            memcpy(slot, plus, sizeof(dual) * (size_t)(3 * S));
+            const dual dt = dl((REAL)duration[e],
+                               d->duration_s ? (REAL)d->duration_s[ebase + e] : LIT(0.0));
+            const dual e1 = dexp(dsub(zero, dmul(r1, dt)));
+            const dual e2 = dexp(dsub(zero, dmul(r2, dt)));
+            for (int64_t s = 0; s < S; ++s) {
+                plus[s] = dmul(plus[s], e2);
+                minus[s] = dmul(minus[s], e2);
+                lon[s] = dmul(lon[s], e1);
+            }
+            lon[0] = dadd(lon[0], dsub(one, e1));
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) dshift(plus, minus, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    const dual efficiency = dsub(zero, inversion);
+                    for (int64_t s = 0; s < S; ++s) lon[s] = dmul(lon[s], efficiency);
+                } else {
+                    const dual fl = dl((REAL)flip[e],
+                                       d->flip_rad ? (REAL)d->flip_rad[ebase + e] : LIT(0.0));
+                    const dual alpha = dmul(fl, b1);
+                    const dual co = dl(COS(alpha.v), -SIN(alpha.v) * alpha.t);
+                    const dual si = dl(SIN(alpha.v), COS(alpha.v) * alpha.t);
+                    const dual ch = dscale(LIT(0.5), dadd(one, co));
+                    const dual sh = dscale(LIT(0.5), dsub(one, co));
+                    const dual hs = dscale(LIT(0.5), si);
+                    for (int64_t s = 0; s < S; ++s) {
+                        const dual p = plus[s], m = minus[s], z = lon[s];
+                        plus[s] = dsub(dadd(dmul(ch, p), dmul(sh, m)), dmul(si, z));
+                        minus[s] = dadd(dadd(dmul(sh, p), dmul(ch, m)), dmul(si, z));
+                        lon[s] = dadd(dsub(dmul(hs, p), dmul(hs, m)), dmul(co, z));
+                    }
+                }
+            }
+            if (a & A_POST_SHIFT) dshift(plus, minus, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) plus[s] = minus[s] = zero;
+            } else if (a & A_SHIFT_AFTER) {
+                dshift(plus, minus, S);
+            }
+        }
+        for (int64_t s = 0; s < 3 * S; ++s) pb[s] = zero;
+        dual gt1 = zero, gt2 = zero, gm0 = zero, gb1 = zero, ginv = zero;
+        for (int64_t e = E - 1; e >= 0; --e) {
+            const dual* slot = traj + e * 3 * S;
+            const uint8_t a = c->action[e];
+            const dual dt = dl((REAL)duration[e],
+                               d->duration_s ? (REAL)d->duration_s[ebase + e] : LIT(0.0));
+            const dual e1 = dexp(dsub(zero, dmul(r1, dt)));
+            const dual e2 = dexp(dsub(zero, dmul(r2, dt)));
+            for (int64_t s = 0; s < S; ++s) {
+                ps[s] = dmul(slot[s], e2);
+                ms[s] = dmul(slot[S + s], e2);
+                zs[s] = dmul(slot[2 * S + s], e1);
+            }
+            zs[0] = dadd(zs[0], dsub(one, e1));
+            if (a & A_PRE_SHIFT) dshift(ps, ms, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) pb[s] = mb[s] = zero;
+            } else if (a & A_SHIFT_AFTER) {
+                dshift_adjoint(pb, mb, S);
+            }
+            if (a & A_POST_SHIFT) dshift_adjoint(pb, mb, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    const dual efficiency = dsub(zero, inversion);
+                    for (int64_t s = 0; s < S; ++s) {
+                        ginv = dsub(ginv, dmul(zb[s], zs[s]));
+                        zb[s] = dmul(zb[s], efficiency);
+                    }
+                } else {
+                    const dual fl = dl((REAL)flip[e],
+                                       d->flip_rad ? (REAL)d->flip_rad[ebase + e] : LIT(0.0));
+                    const dual alpha = dmul(fl, b1);
+                    const dual co = dl(COS(alpha.v), -SIN(alpha.v) * alpha.t);
+                    const dual si = dl(SIN(alpha.v), COS(alpha.v) * alpha.t);
+                    const dual ch = dscale(LIT(0.5), dadd(one, co));
+                    const dual sh = dscale(LIT(0.5), dsub(one, co));
+                    const dual hs = dscale(LIT(0.5), si);
+                    const dual hco = dscale(LIT(0.5), co);
+                    dual ga = zero;
+                    for (int64_t s = 0; s < S; ++s) {
+                        const dual p = ps[s], m = ms[s], z = zs[s];
+                        const dual pbs = pb[s], mbs = mb[s], zbs = zb[s];
+                        ga = dadd(dadd(dadd(ga, dmul(pbs, dsub(dsub(dmul(hs, m), dmul(hs, p)),
+                                                                dmul(co, z)))),
+                                       dmul(mbs, dadd(dsub(dmul(hs, p), dmul(hs, m)), dmul(co, z)))),
+                                  dmul(zbs, dsub(dsub(dmul(hco, p), dmul(hco, m)), dmul(si, z))));
+                        pb[s] = dadd(dadd(dmul(ch, pbs), dmul(sh, mbs)), dmul(hs, zbs));
+                        mb[s] = dsub(dadd(dmul(sh, pbs), dmul(ch, mbs)), dmul(hs, zbs));
+                        zb[s] = dadd(dadd(dmul(dsub(zero, si), pbs), dmul(si, mbs)), dmul(co, zbs));
+                    }
+                    const dual gf = dmul(ga, b1);
+                    value[5][ebase + e] += gf.v;
+                    curve[5][ebase + e] += gf.t;
+                    gb1 = dadd(gb1, dmul(ga, fl));
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                const dual sd = dl((REAL)seed_imag[out_base + c->output_index[e]], LIT(0.0));
+                gm0 = dadd(gm0, dmul(sd, ps[0]));
+                pb[0] = dadd(pb[0], dmul(sd, m0));
+            }
+            if (a & A_PRE_SHIFT) dshift_adjoint(pb, mb, S);
+            dual ge1 = dsub(zero, zb[0]);
+            dual ge2 = zero;
+            for (int64_t s = 0; s < S; ++s) {
+                ge2 = dadd(dadd(ge2, dmul(pb[s], slot[s])), dmul(mb[s], slot[S + s]));
+                ge1 = dadd(ge1, dmul(zb[s], slot[2 * S + s]));
+                pb[s] = dmul(pb[s], e2);
+                mb[s] = dmul(mb[s], e2);
+                zb[s] = dmul(zb[s], e1);
+            }
+            const dual scale1 = dmul(dmul(e1, dt), dscale(LIT(1000.0), dinv_square(t1)));
+            const dual scale2 = dmul(dmul(e2, dt), dscale(LIT(1000.0), dinv_square(t2)));
+            gt1 = dadd(gt1, dmul(ge1, scale1));
+            gt2 = dadd(gt2, dmul(ge2, scale2));
+            /* Atoms of a train add into one slot per event, in this order. */
+            const dual acc = dl(value[6][ebase + e], curve[6][ebase + e]);
+            const dual gd = dsub(dsub(acc, dmul(ge1, dmul(r1, e1))), dmul(ge2, dmul(r2, e2)));
+            value[6][ebase + e] = gd.v;
+            curve[6][ebase + e] = gd.t;
+        }
+        const dual g[5] = {gt1, gt2, gm0, gb1, ginv};
+        for (int k = 0; k < 5; ++k) {
+            value[k][atom] += g[k].v;
+            curve[k][atom] += g[k].t;
+        }
+    }
+    free(buf);
+    free(traj);
+}
+
 /* ---- the complex path (one pool, instant RF) ---------------------------- */
 
 /* Per-event RF / receiver phase (train_count*event_count) and the per-voxel
@@ -673,6 +891,14 @@ void NAME(oracle_tangent)(const oracle_case* c, const oracle_direction* d,
 void NAME(oracle_forward_complex)(const oracle_case* c, const oracle_offaxis* o,
                                   REAL* out_real, REAL* out_imag, int threads) {
     run_threads_o(complex_job, c, NULL, o, out_real, out_imag, threads);
+}
+
+/* Single-threaded forward over reverse; value[7] and curve[7] (t1, t2, m0,
+ * b1, inversion per atom; flip, duration per train and event) must be
+ * zeroed by the caller. */
+void NAME(oracle_second)(const oracle_case* c, const oracle_direction* d, const float* seed_imag,
+                         REAL* const* value, REAL* const* curve) {
+    run_second(c, d, seed_imag, 0, c->atom_count * c->train_count, value, curve);
 }
 
 /* Single-threaded adjoint; gradient arrays must be zeroed by the caller. */

@@ -266,6 +266,61 @@ def adjoint(p: Packed, seed_imag: np.ndarray, precision: str = "f64") -> dict[st
     return grads
 
 
+def _direction(p: Packed, direction: dict, keep: list) -> _Direction:
+    d = _Direction()
+    shape = (p.train_count, p.event_count)
+    direction = dict(direction)
+    for name in ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s", "flip_rad"):
+        value = direction.pop(name, None)
+        if value is None:
+            continue
+        if name in ("duration_s", "flip_rad"):
+            value = np.broadcast_to(np.asarray(value, np.float32), shape)
+        else:
+            value = np.broadcast_to(np.asarray(value, np.float32), (p.atom_count,))
+        value = _f32(value)
+        keep.append(value)
+        setattr(d, name, _ptr(value))
+    if direction:
+        raise ValueError(f"unknown tangent directions {sorted(direction)}")
+    return d
+
+
+SECOND_ORDER = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")
+
+
+def second(p: Packed, seed_imag: np.ndarray, precision: str = "f64",
+           **direction) -> tuple[dict[str, np.ndarray], dict[str, np.ndarray]]:
+    """Forward over reverse: the first-order adjoint for a seed on the
+    imaginary output plane, differentiated along ``direction`` (names as
+    :func:`tangent`). Returns ``(values, curvature)``: the gradient of
+    ``<seed, J d>`` with respect to the direction (``J^T seed``) and with
+    respect to the inputs, each keyed ``t1_ms, t2_ms, m0, b1, inversion``
+    (per atom) and ``flip_rad, duration_s`` (per event, or per train and
+    event). Follows ``simulate_real_vjp_jvp_range``
+    (src/torchsim/_epg_cpu.cpp:7028-7330)."""
+    dtype, _ = _dtype(precision)
+    keep: list = []
+    c = _case(p, keep)
+    d = _direction(p, direction, keep)
+    seed = _f32(np.broadcast_to(seed_imag, _shape(p)))
+    sides = []
+    for _ in range(2):
+        g = {n: np.zeros(p.atom_count, dtype=dtype) for n in SECOND_ORDER[:5]}
+        for n in SECOND_ORDER[5:]:
+            g[n] = np.zeros((p.train_count, p.event_count), dtype=dtype)
+        sides.append(g)
+    ptrs = [(ctypes.c_void_p * 7)(*[side[n].ctypes.data for n in SECOND_ORDER])
+            for side in sides]
+    fn = getattr(_library(), f"oracle_second_{precision}")
+    fn(ctypes.byref(c), ctypes.byref(d), ctypes.c_void_p(seed.ctypes.data), ptrs[0], ptrs[1])
+    if p.train_count == 1:
+        for side in sides:
+            for n in SECOND_ORDER[5:]:
+                side[n] = side[n][0]
+    return sides[0], sides[1]
+
+
 def cpu_threads() -> int:
     """Host cores this process may use."""
     try:

@@ -60,7 +60,7 @@ class _Recorder:
         for name in ("_auto_real_axis", "_auto_real_axis_adjoint"):
             self._orig[name] = getattr(accelerators, name)
             setattr(accelerators, name, self._verdict(name))
-        for name in ("_run_packed", "_run_packed_jvp", "_run_packed_vjp"):
+        for name in ("_run_packed", "_run_packed_jvp", "_run_packed_vjp", "_run_packed_vjp_jvp"):
             self._orig[name] = getattr(accelerators, name)
             setattr(accelerators, name, self._wrap(name))
 
@@ -332,6 +332,87 @@ def case_adjoint(ts, rec) -> dict:
     return out
 
 
+def case_second(ts, rec) -> dict:
+    """Second order. A Cramer-Rao cost of the (T1, T2) Jacobian differentiated
+    with respect to the flip angles and TRs: the reference's design route
+    (``_NativeEpgJvp.backward`` -> ``_run_packed_vjp_jvp``, one call per
+    Jacobian column), and one direct forward-over-reverse call with a general
+    direction (every tissue property, duration and flip) and a random seed."""
+    import torch
+    from torchsim.optim import crlb
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(5)
+    n, pulses = 3, 30
+    t1, t2, b1 = draw_tissue(rng, n)
+    m0 = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    theta = torch.from_numpy(flip).clone().requires_grad_(True)
+    tau = torch.from_numpy(tr).clone().requires_grad_(True)
+    tissue = dict(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2), B1=torch.from_numpy(b1),
+                  M0=torch.from_numpy(m0))
+    rec.clear()
+    sig, jac = MRFSimulator(flip=theta, TR=tau, states=8).jacobian(("T1", "T2"), **tissue)
+    scale = torch.stack((tissue["T1"], tissue["T2"]), dim=-1)
+    loss = (crlb(jac) / scale.square()).sum()
+    loss.backward()
+    out = {"flip_deg": flip, "tr_ms": tr, "t1": t1, "t2": t2, "b1": b1, "m0": m0,
+           "states": np.int64(8), "signal": _np(sig), "jacobian": _np(jac), "loss": _np(loss),
+           "grad_flip_deg": _np(theta.grad), "grad_tr_ms": _np(tau.grad)}
+    calls = [c for c in rec.calls if c["route"] == "_run_packed_vjp_jvp"]
+    names = (*TISSUE_NAMES, "duration", "flip", "phase")
+    out["design_calls"] = np.int64(len(calls))
+    for k, call in enumerate(calls):
+        args = call["args"]
+        out.update(_packed(call, f"design{k}_"))
+        for name, value in zip(names, args[2], strict=True):
+            out[f"design{k}_tangent_{name}"] = _np(value)
+        out[f"design{k}_seed"] = _np(args[3])
+        curvature, values = call["result"]
+        for name, value in zip(names, curvature, strict=False):
+            out[f"design{k}_curvature_{name}"] = _np(value)
+        for name, value in zip(names, values, strict=False):
+            out[f"design{k}_value_{name}"] = _np(value)
+    # The direct call: the packed buffers of a plain forward of the same case.
+    rec.clear()
+    with torch.no_grad():
+        MRFSimulator(flip=torch.from_numpy(flip), TR=torch.from_numpy(tr), states=8).simulate(
+            **tissue, inv_efficiency=torch.from_numpy(rng.uniform(0.8, 1.0, n).astype(np.float32)))
+    fwd = [c for c in rec.calls if c["route"] == "_run_packed"][0]
+    packed_tissue, events = fwd["args"][0], fwd["args"][1]
+    output_count = int(fwd["result"].shape[-1])
+    gen = torch.Generator().manual_seed(6)
+    tangents = []
+    for name, value in zip(names, (*packed_tissue, events[0], events[2], events[3]), strict=True):
+        if name in ("t1_ms", "t2_ms", "m0", "b1", "inversion_efficiency", "duration", "flip"):
+            t = torch.randn(value.shape, generator=gen, dtype=value.dtype)
+            t = t * (100.0 if name in ("t1_ms", "t2_ms") else 1e-3 if name == "duration" else 0.1)
+        else:
+            t = torch.zeros_like(value)
+        tangents.append(t)
+    seed = torch.randn((n, output_count), generator=gen, dtype=torch.complex64)
+    rec.clear()
+    curvature, values = _accelerators_of(ts)._run_packed_vjp_jvp(
+        tuple(packed_tissue), tuple(events), tuple(tangents), seed, state_count=8,
+        output_count=output_count, threads=1, real_axis=1)
+    out.update(_packed(fwd, "direct_"))
+    for name, value in zip(names, tangents, strict=True):
+        out[f"direct_tangent_{name}"] = _np(value)
+    out["direct_seed"] = _np(seed)
+    for name, value in zip(names, curvature, strict=False):
+        out[f"direct_curvature_{name}"] = _np(value)
+    for name, value in zip(names, values, strict=False):
+        out[f"direct_value_{name}"] = _np(value)
+    return out
+
+
+def _accelerators_of(ts):
+    from torchsim.sequence import _accelerators
+
+    return _accelerators
+
+
 def case_gn(ts, rec) -> dict:
     """The reference's NonlinearLeastSquares (Levenberg-Marquardt, default
     loop: TrustRegion, direct, 20 iterations) on noisy MRF signals."""
@@ -363,7 +444,8 @@ def case_gn(ts, rec) -> dict:
             "unconverged": np.int64(est.unconverged)}
 
 
-CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis")
+CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
+         "mrf_second")
 
 
 def main() -> None:
@@ -384,7 +466,8 @@ def main() -> None:
     rec = _Recorder(_accelerators)
     for name, fn in (("mrf880", case_mrf880), ("mrf_prep", case_mrf_prep),
                      ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn),
-                     ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis)):
+                     ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
+                     ("mrf_second", case_second)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

@@ -128,3 +128,71 @@ def test_complex_oracle_reduces_to_the_real_one(golden):
     real = O.forward(packed_from_golden(d), "f64")
     assert max_rel(full.imag, real) <= 1e-12
     assert np.abs(full.real).max() <= 1e-12 * np.abs(real).max()
+
+
+# ---- second order (forward over reverse) -------------------------------------
+
+SECOND_NAMES = {"t1_ms": "t1_ms", "t2_ms": "t2_ms", "m0": "m0", "b1": "b1",
+                "inversion": "inversion_efficiency", "flip_rad": "flip",
+                "duration_s": "duration"}
+
+
+def second_case(d, prefix: str):
+    """The packed inputs, direction and seed of one recorded forward-over-
+    reverse call of the mrf_second fixture."""
+    p = packed_from_golden(d, prefix)
+    direction = {k: d[f"{prefix}tangent_{v}"] for k, v in SECOND_NAMES.items()}
+    return p, direction, d[f"{prefix}seed"].imag
+
+
+@pytest.mark.parametrize("prefix", ["design0_", "design1_", "direct_"])
+@pytest.mark.parametrize("precision,tol", [("f32", 0.0), ("f64", 5e-6)])
+def test_oracle_second_order_matches_reference(golden, prefix, precision, tol):
+    """Both the value side (J^T seed) and the curvature side of
+    ``_run_packed_vjp_jvp``: the CRLB design's two column calls (one-hot T2,
+    T1 directions) and a direct call along every tissue property, duration
+    and flip at once. The FP32 port is bitwise the reference's kernel."""
+    d = golden("mrf_second")
+    p, direction, seed = second_case(d, prefix)
+    values, curvature = O.second(p, seed, precision, **direction)
+    for mine, ref in SECOND_NAMES.items():
+        assert max_rel(values[mine], d[f"{prefix}value_{ref}"]) <= tol, ("value", mine)
+        assert max_rel(curvature[mine], d[f"{prefix}curvature_{ref}"]) <= tol, ("curve", mine)
+
+
+def test_oracle_second_order_is_the_derivative_of_the_adjoint(golden):
+    """The curvature side against central differences of the first-order
+    adjoint stepped along the direction (FP64), and the value side against the
+    adjoint itself."""
+    d = golden("mrf_second")
+    p, direction, seed = second_case(d, "direct_")
+    values, curvature = O.second(p, seed, "f64", **direction)
+    first = O.adjoint(p, seed, "f64")
+    for name in ("t1_ms", "t2_ms", "m0", "b1", "flip_rad", "duration_s"):
+        assert max_rel(values[name], first[name]) <= 1e-12, name
+    h = 1e-3
+
+    def stepped(sign):
+        q = packed_from_golden(d, "direct_")
+        for name, attr in (("t1_ms", "t1_ms"), ("t2_ms", "t2_ms"), ("m0", "m0"), ("b1", "b1"),
+                           ("inversion", "inversion"), ("duration_s", "duration_s"),
+                           ("flip_rad", "flip_rad")):
+            base = np.asarray(getattr(q, attr), np.float64)
+            setattr(q, attr, base + sign * h * np.asarray(direction[name], np.float64))
+        return O.adjoint(q, seed, "f64")
+
+    # The packed inputs are FP32, so the step is applied in FP64 and rounded;
+    # h keeps that rounding well below the difference.
+    up, down = stepped(1.0), stepped(-1.0)
+    for name in ("t1_ms", "t2_ms", "m0", "b1", "flip_rad", "duration_s"):
+        fd = (up[name] - down[name]) / (2 * h)
+        assert max_rel(curvature[name], fd) <= 1e-3, name
+
+
+def test_oracle_second_order_planted_mistake_is_caught(golden):
+    """A direction the checker drops must show up against the fixture."""
+    d = golden("mrf_second")
+    p, direction, seed = second_case(d, "direct_")
+    direction.pop("duration_s")
+    _, curvature = O.second(p, seed, "f64", **direction)
+    assert max_rel(curvature["flip_rad"], d["direct_curvature_flip"]) > 1e-3
