@@ -285,6 +285,51 @@ int tsg_epg_adjoint_noalloc(const tsg_program* program, const tsg_tissue* tissue
 /* TSG_STATIC_SCRATCH_BYTES, as built into the library. */
 int64_t tsg_static_scratch_bytes(void);
 
+/* ---- second order: the adjoint of the tangent sweep --------------------- */
+
+/* Sizes for the second-order sweeps along direction_count (1-3) directions:
+ * the trajectory (every op's entry state of the signal state and of each
+ * tangent, and every recorded F+[0]) and the workspace the caller allocates.
+ * event_directions: whether any direction has duration or flip tangents. */
+int tsg_epg_second_plan(const tsg_program* program, int64_t atom_count, int64_t state_count,
+                        int direction_count, int event_directions, const tsg_launch* launch,
+                        int64_t* trajectory_bytes, int64_t* workspace_bytes);
+
+/* Forward of the signal and its derivatives along `directions` (DEVICE
+ * pointers, tsg_direction per direction) in one pass, storing the trajectory
+ * the reverse sweep reads. Signal (train, atom, output) and derivatives
+ * (train, atom, K + with_m0, output) in `layout` (nullable); with with_m0 the
+ * last column is the derivative along M0 (F+[0] itself), which needs no
+ * tangent state. The program must have been compiled with every direction's
+ * duration tangent (or unmerged). */
+int tsg_epg_second_forward(const tsg_program* program, const tsg_tissue* tissue,
+                           int64_t atom_count, int64_t state_count,
+                           const tsg_direction* directions, int direction_count, int with_m0,
+                           int layout,
+                           float* sig_a, float* sig_b, float* jac_a, float* jac_b,
+                           void* trajectory, void* workspace, const tsg_launch* launch,
+                           void* stream);
+
+/* The reverse sweep of that forward for the loss
+ *   L = <seed_signal, s> + sum_k <seed_derivatives[k], J d_k>
+ * (seeds as tsg_epg_adjoint takes them; seed_signal nullable, the
+ * derivative seeds laid out as the forward writes the derivatives, with the
+ * M0 column's when with_m0). Adds dL/d(inputs) into
+ * `curvature` (for seed_signal alone this is the first-order adjoint, for the
+ * derivative seeds the second-order term) and, into values[k], dL/d(d_k):
+ * J^T seed_k over the tissue directions, and for a single direction also its
+ * duration and flip. The reference's forward over reverse
+ * (simulate_real_vjp_jvp_range, _epg_cpu.cpp:7028-7330) does one direction
+ * per call; this sweep takes up to three. Deterministic (fixed-order sums). */
+int tsg_epg_second_reverse(const tsg_program* program, const tsg_tissue* tissue,
+                           int64_t atom_count, int64_t state_count,
+                           const tsg_direction* directions, int direction_count, int with_m0,
+                           const float* seed_signal, const float* seed_derivatives,
+                           int seed_layout, const void* trajectory,
+                           const tsg_gradients* curvature, const tsg_gradients* values,
+                           void* workspace, int64_t workspace_bytes, const tsg_launch* launch,
+                           void* stream);
+
 /* ---- many sequences in one persistent launch ---------------------------- */
 
 /* One sequence of a batch. Its ops are op_count consecutive entries of the
@@ -446,6 +491,17 @@ int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count, int64_t a
 int tsg_epg_simulate_vjp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
                          int64_t train_count, int64_t event_count, int64_t state_count,
                          int64_t output_count, int real_axis, int features);
+
+/* _epg_cpu.simulate_vjp_jvp (src/torchsim/_epg_cpu.cpp:11572-11760): 26
+ * packed buffers, 20 tangents, two seed planes, 20 value gradients and 20
+ * curvature gradients (each 17 tissue, then duration, flip, phase), 13 tail
+ * slots (101). The value side is J^T seed, the curvature side the gradient
+ * of <seed, J tangent> with respect to the inputs. Compiled unmerged;
+ * gradients are written (not accumulated); phase and the tissue directions
+ * the real subspace divides out are written as zero. Synchronous. */
+int tsg_epg_simulate_vjp_jvp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
+                             int64_t train_count, int64_t event_count, int64_t state_count,
+                             int64_t output_count, int real_axis, int features);
 
 #ifdef __cplusplus
 }

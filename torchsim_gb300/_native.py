@@ -145,6 +145,18 @@ SIGNATURES: dict[str, tuple] = {
                                 _int]),
     "tsg_epg_simulate_jvp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
                                     _int, _int]),
+    "tsg_epg_simulate_vjp_jvp": (_int, [ctypes.POINTER(_vp), _i64, _i64, _i64, _i64, _i64, _i64,
+                                        _int, _int]),
+    "tsg_epg_second_plan": (_int, [_vp, _i64, _i64, _int, _int, ctypes.POINTER(Launch),
+                                   ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "tsg_epg_second_forward": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64,
+                                      ctypes.POINTER(Direction), _int, _int, _int, _vp, _vp, _vp,
+                                      _vp,
+                                      _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_second_reverse": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64,
+                                      ctypes.POINTER(Direction), _int, _int, _vp, _vp, _int, _vp,
+                                      ctypes.POINTER(Gradients), ctypes.POINTER(Gradients), _vp,
+                                      _i64, ctypes.POINTER(Launch), _vp]),
 }
 
 _lib: ctypes.CDLL | None = None

@@ -383,6 +383,176 @@ def adjoint(program: Program, tissue: TissueMaps, states: int, seed: torch.Tenso
     return grads
 
 
+# ---- second order ------------------------------------------------------------
+
+# Keys of one forward-mode direction: per voxel (tissue), per (train, event)
+# (duration, flip).
+DIRECTION_KEYS = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s", "flip_rad")
+MAX_SECOND_DIRECTIONS = 3
+
+
+def _direction_structs(directions: Sequence[dict[str, torch.Tensor]]):
+    arr = (_native.Direction * max(len(directions), 1))()
+    for i, d in enumerate(directions):
+        for key in DIRECTION_KEYS:
+            value = d.get(key)
+            setattr(arr[i], key, None if value is None else value.data_ptr())
+    return arr
+
+
+def second_plan(program: Program, voxels: int, states: int, directions: int,
+                event_directions: bool = False, launch=None) -> tuple[int, int]:
+    """(trajectory bytes, workspace bytes) of the second-order sweeps."""
+    tb = ctypes.c_int64()
+    wb = ctypes.c_int64()
+    _native.check(_native.library().tsg_epg_second_plan(
+        program.handle, voxels, states, int(directions), int(event_directions),
+        _native.launch_shape(launch), ctypes.byref(tb), ctypes.byref(wb)))
+    return tb.value, wb.value
+
+
+def _has_event_directions(directions) -> bool:
+    return any(d.get("duration_s") is not None or d.get("flip_rad") is not None
+               for d in directions)
+
+
+def second_forward(program: Program, tissue: TissueMaps, states: int,
+                   directions: Sequence[dict[str, torch.Tensor]], *, with_m0: bool = False,
+                   trajectory: torch.Tensor | None = None, workspace: torch.Tensor | None = None,
+                   launch=None):
+    """Signal and its derivatives along ``directions`` (1-3 dicts of device
+    tensors keyed as :data:`DIRECTION_KEYS`; with ``with_m0`` a last column,
+    the derivative along M0) in ONE pass that stores the trajectory the
+    reverse sweep reads. Returns ``(signal (rows, P), derivatives (rows, K
+    [+1], P), trajectory, workspace)``, complex64 holding ``1j * i*m0*F+[0]``
+    and its derivatives."""
+    k = len(directions)
+    rows = program.trains * tissue.voxels
+    device = tissue.t1.device
+    evdir = _has_event_directions(directions)
+    tb, wb = second_plan(program, tissue.voxels, states, k, evdir, launch)
+    if trajectory is None or trajectory.numel() < tb:
+        trajectory = torch.empty(max(tb, 4), dtype=torch.uint8, device=device)
+    if workspace is None or workspace.numel() < wb:
+        workspace = torch.empty(max(wb, 4), dtype=torch.uint8, device=device)
+    sig = torch.empty((rows, program.outputs), dtype=torch.complex64, device=device)
+    jac = torch.empty((rows, k + int(with_m0), program.outputs), dtype=torch.complex64,
+                      device=device)
+    t = tissue.struct()
+    dirs = _direction_structs(directions)
+    _native.check(_native.library().tsg_epg_second_forward(
+        program.handle, ctypes.byref(t), tissue.voxels, states, dirs, k, int(with_m0),
+        _native.LAYOUT_COMPLEX_IJ, sig.data_ptr(), None, jac.data_ptr(), None,
+        trajectory.data_ptr(), workspace.data_ptr(), _native.launch_shape(launch), _stream()))
+    return sig, jac, trajectory, workspace
+
+
+def second_reverse(program: Program, tissue: TissueMaps, states: int,
+                   directions: Sequence[dict[str, torch.Tensor]], seed_derivatives: torch.Tensor,
+                   trajectory: torch.Tensor, workspace: torch.Tensor, *,
+                   seed_signal: torch.Tensor | None = None, with_m0: bool = False,
+                   curvature: dict[str, torch.Tensor] | None = None,
+                   values: Sequence[dict[str, torch.Tensor]] | None = None, launch=None) -> None:
+    """Reverse sweep of :func:`second_forward` for
+    ``L = <seed_signal, s> + sum_k <seed_derivatives[:, k], J d_k>`` (complex64
+    cotangents of the arrays :func:`second_forward` returned). Adds dL/d(inputs)
+    into ``curvature`` and dL/d(direction k) into ``values[k]`` (dicts keyed as
+    :data:`GRAD_NAMES`; absent keys are not computed)."""
+    k = len(directions)
+    seed_derivatives = seed_derivatives.to(torch.complex64).contiguous()
+    if seed_signal is not None:
+        seed_signal = seed_signal.to(torch.complex64).contiguous()
+    c = _native.Gradients(*[curvature[n].data_ptr() if curvature and curvature.get(n) is not None
+                            else None for n in GRAD_NAMES])
+    vals = (_native.Gradients * max(k, 1))()
+    for i in range(k):
+        d = values[i] if values is not None and i < len(values) else {}
+        for n in GRAD_NAMES:
+            setattr(vals[i], n, d[n].data_ptr() if d.get(n) is not None else None)
+    t = tissue.struct()
+    dirs = _direction_structs(directions)
+    _native.check(_native.library().tsg_epg_second_reverse(
+        program.handle, ctypes.byref(t), tissue.voxels, states, dirs, k, int(with_m0),
+        None if seed_signal is None else seed_signal.data_ptr(), seed_derivatives.data_ptr(),
+        _native.LAYOUT_COMPLEX_IJ, trajectory.data_ptr(), ctypes.byref(c), vals,
+        workspace.data_ptr(), workspace.numel(), _native.launch_shape(launch), _stream()))
+
+
+# Public property name -> its key in a direction; M0 is the free column.
+DIRECTION_OF = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1", "inv_efficiency": "inversion"}
+
+
+class JacobianFunction(torch.autograd.Function):
+    """Signal and Jacobian columns whose backward is the second-order sweep.
+
+    ``names`` are property names of :data:`DIFFERENTIABLE`; every column but
+    M0 carries a tangent state (at most three), M0's is F+[0] itself. The
+    backward of both outputs is ONE reverse sweep
+    (``tsg_epg_second_reverse``): the first-order adjoint of the signal's
+    cotangent plus the second-order term of the Jacobian's. The reference
+    pays one forward-over-reverse call per column
+    (sequence/_accelerators.py:1780-1800)."""
+
+    @staticmethod
+    def forward(ctx, program, states, names, launch, t1, t2, m0, b1, inv, flip_events,
+                duration_events):
+        tissue = TissueMaps(t1.detach(), t2.detach(), None if m0 is None else m0.detach(),
+                            None if b1 is None else b1.detach(),
+                            None if inv is None else inv.detach())
+        ones = torch.ones(tissue.voxels, dtype=torch.float32, device=t1.device)
+        stateful = [n for n in names if n != "M0"]
+        if not stateful or len(stateful) > MAX_SECOND_DIRECTIONS:
+            raise NotImplementedError(
+                "a differentiable Jacobian takes one to three of T1, T2, B1, inv_efficiency "
+                "(plus M0)")
+        directions = [{DIRECTION_OF[n]: ones} for n in stateful]
+        with_m0 = "M0" in names
+        sig, jac, traj, ws = second_forward(program, tissue, states, directions, with_m0=with_m0,
+                                            launch=launch)
+        # Columns in the caller's order.
+        order = [stateful.index(n) if n != "M0" else len(stateful) for n in names]
+        if order != list(range(len(names))):
+            jac = jac[:, order]
+        ctx.program, ctx.states, ctx.launch = program, states, launch
+        ctx.tissue, ctx.directions, ctx.with_m0, ctx.order = tissue, directions, with_m0, order
+        ctx.ones = ones
+        ctx.save_for_backward(traj, ws)
+        ctx.present = (m0 is not None, b1 is not None, inv is not None)
+        return sig, jac
+
+    @staticmethod
+    def backward(ctx, grad_sig, grad_jac):
+        traj, ws = ctx.saved_tensors
+        tissue, program = ctx.tissue, ctx.program
+        need = ctx.needs_input_grad
+        dev = traj.device
+        V = tissue.voxels
+        rows = program.trains * V
+        kk = len(ctx.order)
+        if grad_jac is None:
+            grad_jac = torch.zeros((rows, kk, program.outputs), dtype=torch.complex64, device=dev)
+        # Back to the kernel's column order.
+        seed = torch.empty_like(grad_jac)
+        seed[:, ctx.order] = grad_jac
+        curvature: dict[str, torch.Tensor] = {}
+        names = ("t1_ms", "t2_ms", "m0", "b1", "inversion")
+        for i, name in enumerate(names):
+            if need[4 + i]:
+                curvature[name] = torch.zeros(V, dtype=torch.float32, device=dev)
+        ev_shape = (program.trains, program.events.events)
+        if need[9]:
+            curvature["flip_rad"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
+        if need[10]:
+            curvature["duration_s"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
+        second_reverse(program, tissue, ctx.states, ctx.directions, seed, traj, ws,
+                       seed_signal=grad_sig, with_m0=ctx.with_m0, curvature=curvature,
+                       launch=ctx.launch)
+        out = [None, None, None, None]
+        out += [curvature.get(n) for n in names]
+        out += [curvature.get("flip_rad"), curvature.get("duration_s")]
+        return tuple(out)
+
+
 class EpgFunction(torch.autograd.Function):
     """Forward sweep whose backward is the adjoint kernel (trajectory mode
     when it fits in memory, else checkpointed).

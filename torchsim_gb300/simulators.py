@@ -198,7 +198,10 @@ class _EpgSimulator:
                 f"{type(self).__name__}: gradients w.r.t. its sequence arguments are not built")
         return flip_ev, dur_ev
 
-    def _run_differentiable(self, values: dict[str, Any]) -> torch.Tensor:
+    def _run_differentiable(self, values: dict[str, Any], names: Sequence[str] | None = None):
+        """The signal (or, with ``names``, the signal and Jacobian) on the
+        autograd route: the first-order adjoint kernel behind the signal, the
+        second-order sweep behind a Jacobian."""
         held, protocol, states, device, repetitions = self._split(values)
         home = _home(values)
         dev = engine.require_cuda(torch.device(device) if device is not None else
@@ -223,17 +226,34 @@ class _EpgSimulator:
             t = t.expand(batch).reshape(-1) if batch else t.reshape(1)
             return t.clamp_min(engine.MINIMUM_RELAXATION_TIME_MS) if clamp else t
 
+        if names:
+            for name in names:
+                if name not in held:
+                    raise ValueError(
+                        f"{name!r} is not among the properties this call gave "
+                        f"{type(self).__name__}: {sorted(held)}")
         with torch.cuda.device(dev):
             program = program_for(events, dev)
             flip_ev = torch.from_numpy(events.flip).to(dev)
             dur_ev = torch.from_numpy(events.duration).to(dev)
             flip_ev, dur_ev = self._event_gradients(protocol, events, flip_ev, dur_ev, repetitions)
-            signal = engine.EpgFunction.apply(
-                program, states, None, flat(maps["T1"], True, False), flat(maps["T2"], True, False),
-                flat(maps["M0"]), flat(maps["B1"]), flat(maps["inv"]), flip_ev, dur_ev)
-            signal, _ = self._post(signal, None, None, held, plain, dev)
+            tissue = (flat(maps["T1"], True, False), flat(maps["T2"], True, False),
+                      flat(maps["M0"]), flat(maps["B1"]), flat(maps["inv"]))
+            jac = None
+            if names:
+                kernel = tuple(self._kernel_names(names))
+                signal, jac = engine.JacobianFunction.apply(program, states, kernel, None, *tissue,
+                                                            flip_ev, dur_ev)
+            else:
+                signal = engine.EpgFunction.apply(program, states, None, *tissue, flip_ev, dur_ev)
+            signal, jac = self._post(signal, jac, names, held, plain, dev)
         signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
-        return signal.to(home) if home.type != "cuda" else signal
+        if jac is not None:
+            jac = jac.reshape(*batch, *jac.shape[-2:]) if batch else jac.reshape(jac.shape[-2:])
+        if home.type != "cuda":
+            signal = signal.to(home)
+            jac = None if jac is None else jac.to(home)
+        return signal if names is None else (signal, jac)
 
     def jacobian(self, diff: str | Sequence[str], **values: Any):
         """Return ``(signal, jacobian)``; the Jacobian is ``(*voxels, k, samples)``
@@ -242,10 +262,11 @@ class _EpgSimulator:
         if torch.is_grad_enabled() and any(
                 isinstance(v, torch.Tensor) and v.requires_grad
                 for v in {**self.protocol, **values}.values()):
-            raise NotImplementedError(
-                "the Jacobian is not differentiable here: second-order (forward-over-reverse) "
-                "derivatives are not built")
-        signal, jac = self._run(values, names)
+            # Differentiable: a cost of the Jacobian (a Cramer-Rao bound)
+            # backs through the second-order sweep.
+            signal, jac = self._run_differentiable(values, names)
+        else:
+            signal, jac = self._run(values, names)
         if isinstance(diff, str):
             jac = jac[..., 0, :]
         return signal, jac
