@@ -353,6 +353,8 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     }
     if not args.skip_adjoint:
         line["adjoint"] = adjoint_section(torch, device)
+    if not args.skip_second:
+        line["second_order"] = second_order_section(torch, device)
     if not args.skip_batched:
         line["batched"] = batched_section(torch, device, sequences=args.batch_sequences,
                                           shape=args.batch_shape)
@@ -460,6 +462,135 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
         "gradient_definition": "forward with checkpoints + backward, over a plain forward (the "
                                "reference's benchmarks/anatomy.py measure: 8.4x CUDA, 4.6x CPU)",
         "forward_updates_per_s": V * n * S / (fwd * 1e-3),
+        "timing": "best of 5 after 3 warm-up runs, CUDA events",
+    }
+
+
+# ---- second order: Cramer-Rao design gradient ---------------------------------
+
+
+def second_order_section(torch, device, voxels: int = 16384, repeats: int = 5) -> dict:
+    """Gradient of a Cramer-Rao design cost, sum over voxels of the bounds of
+    (T1, T2, B1, M0) relative to their squares, with respect to 600 flips and
+    600 TRs (nstates 20, 16,384 tissues drawn as the adjoint workload's): the
+    Jacobian forward that stores the trajectory plus ONE reverse sweep over
+    the three tangent directions and the M0 column, against the fused forward
+    Jacobian alone and against one forward-over-reverse pass per column (the
+    reference's route, sequence/_accelerators.py:1780-1800)."""
+    from torchsim_gb300 import MRFSimulator, crlb, engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    rng = np.random.default_rng(0)
+    V, n, S = voxels, 600, 20
+    t1 = np.exp(rng.uniform(np.log(100), np.log(3000), V)).astype(np.float32)
+    t2 = np.minimum(np.exp(rng.uniform(np.log(10), np.log(300), V)), 0.999 * t1).astype(np.float32)
+    b1 = rng.uniform(0.8, 1.2, V).astype(np.float32)
+    m0 = rng.uniform(0.5, 1.5, V).astype(np.float32)
+    flips = rng.uniform(5, 70, n).astype(np.float32)
+    trs = rng.uniform(8, 15, n).astype(np.float32)
+    ev = mrf_events(flips, trs)
+    prog = program_for(ev, device)
+    tissue = engine.tissue_maps(device, V, torch.from_numpy(t1), torch.from_numpy(t2),
+                                torch.from_numpy(m0), torch.from_numpy(b1), None)
+    names = ("T1", "T2", "B1")
+    mask = sum(engine.DESIGN_BITS[k] for k in names)
+    seed = torch.randn((V, len(names) + 1, n), dtype=torch.complex64, device=device)
+    curvature = {"flip_rad": torch.zeros((1, ev.events), device=device),
+                 "duration_s": torch.zeros((1, ev.events), device=device)}
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(repeats):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e))
+        return best
+
+    jac_ms = timed(lambda: engine.forward_tangents(prog, tissue, S, (*names, "M0")))
+    # Launch shape (lanes per voxel, orders per lane): forward + reverse timed
+    # once each per candidate, the fastest kept.
+    tuning = {}
+    for shape in ((5, 4, 0), (10, 2, 0), (8, 4, 0), (16, 2, 0)):
+        tb, wb = engine.design_plan(prog, V, S, mask, launch=shape)
+        traj = torch.empty(tb, dtype=torch.uint8, device=device)
+        work = torch.empty(wb, dtype=torch.uint8, device=device)
+
+        def pair():
+            engine.design_forward(prog, tissue, S, mask, with_m0=True, trajectory=traj,
+                                  launch=shape)
+            engine.design_reverse(prog, tissue, S, mask, seed, traj, work, with_m0=True,
+                                  curvature=curvature, launch=shape)
+
+        tuning[shape] = timed(pair)
+        del traj, work
+    shape = min(tuning, key=tuning.get)
+    tb, wb = engine.design_plan(prog, V, S, mask, launch=shape)
+    traj = torch.empty(tb, dtype=torch.uint8, device=device)
+    work = torch.empty(wb, dtype=torch.uint8, device=device)
+    fwd_ms = timed(lambda: engine.design_forward(prog, tissue, S, mask, with_m0=True,
+                                                 trajectory=traj, launch=shape))
+    engine.design_forward(prog, tissue, S, mask, with_m0=True, trajectory=traj, launch=shape)
+    rev_ms = timed(lambda: engine.design_reverse(prog, tissue, S, mask, seed, traj, work,
+                                                 with_m0=True, curvature=curvature, launch=shape))
+    # One forward-over-reverse pass per column, as the reference pays.
+    tb1, wb1 = engine.design_plan(prog, V, S, engine.DESIGN_BITS["T1"], launch=shape)
+    traj1 = torch.empty(tb1, dtype=torch.uint8, device=device)
+    work1 = torch.empty(wb1, dtype=torch.uint8, device=device)
+    seeds1 = [seed[:, k:k + 1].contiguous() for k in range(len(names))]
+
+    def per_column():
+        for k, name in enumerate(names):
+            bit = engine.DESIGN_BITS[name]
+            engine.design_forward(prog, tissue, S, bit, trajectory=traj1, launch=shape)
+            engine.design_reverse(prog, tissue, S, bit, seeds1[k], traj1, work1,
+                                  curvature=curvature, launch=shape)
+
+    per_col_ms = timed(per_column)
+    del traj1, work1
+    # The public route: Jacobian, Cramer-Rao cost and backward per design step.
+    theta = torch.tensor(flips, device=device, requires_grad=True)
+    tau = torch.tensor(trs, device=device, requires_grad=True)
+    tis = {"T1": torch.from_numpy(t1).to(device), "T2": torch.from_numpy(t2).to(device),
+           "B1": torch.from_numpy(b1).to(device), "M0": torch.from_numpy(m0).to(device)}
+    scale = torch.stack([tis[k] for k in ("T1", "T2", "B1", "M0")], dim=-1)
+
+    def design_step():
+        theta.grad = None
+        tau.grad = None
+        _, jac = MRFSimulator(flip=theta, TR=tau, states=S).jacobian(
+            ("T1", "T2", "B1", "M0"), **tis)
+        (crlb(jac) / scale.square()).sum().backward()
+
+    step_ms = timed(design_step)
+    state_bytes = V * prog.ops * (len(names) + 1) * 3 * S * 4
+    rec_bytes = V * ev.outputs * (len(names) + 1) * 4
+    seed_bytes = V * (len(names) + 1) * n * 8
+    rev_bytes = state_bytes + rec_bytes + seed_bytes
+    fwd_bytes = state_bytes + rec_bytes + V * (len(names) + 2) * n * 8
+    return {
+        "workload": f"Cramer-Rao design gradient: {V} tissues, 600-pulse MRF (flip U(5,70) deg, "
+                    "TR U(8,15) ms), nstates 20, Jacobian (T1, T2, B1, M0), cost sum CRLB/theta^2",
+        "forward_jacobian_ms": jac_ms,
+        "forward_with_trajectory_ms": fwd_ms,
+        "reverse_ms": rev_ms,
+        "gradient_over_forward_jacobian": (fwd_ms + rev_ms) / jac_ms,
+        "per_column_ms": per_col_ms,
+        "per_column_form": "one forward-with-trajectory + reverse pass per tangent column (the "
+                           "reference's one forward-over-reverse call per column)",
+        "fused_speedup_over_per_column": per_col_ms / (fwd_ms + rev_ms),
+        "design_step_ms": step_ms,
+        "design_step_form": "MRFSimulator.jacobian + torchsim_gb300.crlb + backward (public API)",
+        "launch_shape": {"lanes_per_voxel": shape[0], "orders_per_lane": shape[1]},
+        "tuning_ms": {f"{k[0]}x{k[1]}": v for k, v in tuning.items()},
+        "trajectory_bytes": tb,
+        "reverse_hbm": {"algorithmic_bytes": rev_bytes, "achieved_gbs": rev_bytes / rev_ms / 1e6},
+        "forward_hbm": {"algorithmic_bytes": fwd_bytes, "achieved_gbs": fwd_bytes / fwd_ms / 1e6},
         "timing": "best of 5 after 3 warm-up runs, CUDA events",
     }
 
@@ -878,6 +1009,7 @@ def main() -> None:
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--skip-second", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-gn", action="store_true")
     ap.add_argument("--skip-match", action="store_true")

@@ -330,6 +330,26 @@ int tsg_epg_second_reverse(const tsg_program* program, const tsg_tissue* tissue,
                            void* workspace, int64_t workspace_bytes, const tsg_launch* launch,
                            void* stream);
 
+/* The same two sweeps for a design cost: the directions are the unit
+ * tangents of the properties in tangent_mask (TSG_TANGENT_T1 | T2 | B1, in
+ * that order; the Jacobian columns a Cramer-Rao bound differentiates), so
+ * the kernels carry no per-voxel or per-event direction and leave the terms
+ * those directions zero out. The reverse writes the curvature only. */
+int tsg_epg_design_plan(const tsg_program* program, int64_t atom_count, int64_t state_count,
+                        unsigned tangent_mask, const tsg_launch* launch,
+                        int64_t* trajectory_bytes, int64_t* workspace_bytes);
+int tsg_epg_design_forward(const tsg_program* program, const tsg_tissue* tissue,
+                           int64_t atom_count, int64_t state_count, unsigned tangent_mask,
+                           int with_m0, int layout, float* sig_a, float* sig_b, float* jac_a,
+                           float* jac_b, void* trajectory, const tsg_launch* launch,
+                           void* stream);
+int tsg_epg_design_reverse(const tsg_program* program, const tsg_tissue* tissue,
+                           int64_t atom_count, int64_t state_count, unsigned tangent_mask,
+                           int with_m0, const float* seed_signal, const float* seed_derivatives,
+                           int seed_layout, const void* trajectory,
+                           const tsg_gradients* curvature, void* workspace,
+                           int64_t workspace_bytes, const tsg_launch* launch, void* stream);
+
 /* ---- many sequences in one persistent launch ---------------------------- */
 
 /* One sequence of a batch. Its ops are op_count consecutive entries of the

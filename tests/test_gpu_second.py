@@ -81,9 +81,11 @@ def _case(seed, voxels, pulses, states, ti=12.0):
     return rng, flips, trs, ev, t1, t2, b1, m0
 
 
-@pytest.mark.parametrize("names,states", [(("T1",), 8), (("T1", "T2"), 12),
-                                          (("T1", "T2", "B1"), 20), (("T2", "B1"), 33)])
-def test_fused_directions_match_the_oracle(cuda, names, states):
+@pytest.mark.parametrize("names,states,shape", [
+    (("T1",), 8, None), (("T1", "T2"), 12, None), (("T1", "T2", "B1"), 20, None),
+    (("T2", "B1"), 33, None), (("T1", "T2", "B1"), 20, (10, 2, 0)), (("T1", "T2"), 12, (10, 2, 0)),
+    (("B1",), 7, (4, 2, 0)), (("T1", "T2", "B1"), 20, (8, 4, 0))])
+def test_fused_directions_match_the_oracle(cuda, names, states, shape):
     """One reverse sweep over K one-hot directions (and the signal's own
     cotangent) against the FP64 oracle: the first-order adjoint of the signal
     seed plus, per direction, the forward-over-reverse call with its seed."""
@@ -96,7 +98,7 @@ def test_fused_directions_match_the_oracle(cuda, names, states):
     tissue = engine.tissue_maps(cuda, V, t1, t2, m0, b1, None)
     ones = torch.ones(V, device=cuda)
     directions = [{engine.DIRECTION_OF[n]: ones} for n in names]
-    sig, jac, traj, ws = engine.second_forward(prog, tissue, states, directions)
+    sig, jac, traj, ws = engine.second_forward(prog, tissue, states, directions, launch=shape)
     p = packed_from_events(ev, t1, t2, states, m0=m0, b1=b1)
     key = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1"}
     # Forward: signal and derivatives (1j * values).
@@ -115,7 +117,7 @@ def test_fused_directions_match_the_oracle(cuda, names, states):
     values = [{n: torch.zeros(V, device=cuda) for n in ("t1_ms", "t2_ms", "m0", "b1")}
               for _ in names]
     engine.second_reverse(prog, tissue, states, directions, seed_jac, traj, ws,
-                          seed_signal=seed_sig, curvature=curvature, values=values)
+                          seed_signal=seed_sig, curvature=curvature, values=values, launch=shape)
     want = O.adjoint(p, s0, "f64")
     want_values = []
     for k, n in enumerate(names):
@@ -134,6 +136,50 @@ def test_fused_directions_match_the_oracle(cuda, names, states):
     for k, n in enumerate(names):
         for g in ("t1_ms", "t2_ms", "m0", "b1"):
             assert max_rel(values[k][g].cpu().numpy(), want_values[k][g]) <= GRAD_TOL, (n, g)
+
+
+@pytest.mark.parametrize("names,states,shape", [
+    (("T1",), 8, None), (("T2", "B1"), 12, None), (("T1", "T2", "B1"), 20, None),
+    (("T1", "T2", "B1"), 20, (5, 4, 0)), (("T1", "B1"), 33, (32, 2, 0)), (("T1", "T2"), 6, (2, 4, 0))])
+def test_design_sweep_matches_the_oracle(cuda, names, states, shape):
+    """The one-hot design sweeps (no per-voxel or per-event directions): the
+    curvature of the signal seed plus the derivatives' seeds, and an M0
+    column, against the FP64 oracle."""
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import program_for
+
+    rng, flips, trs, ev, t1, t2, b1, m0 = _case(43, 29, 50, states)
+    V = t1.size
+    prog = program_for(ev, cuda)
+    tissue = engine.tissue_maps(cuda, V, t1, t2, m0, b1, None)
+    mask = sum(engine.DESIGN_BITS[n] for n in names)
+    sig, jac, traj = engine.design_forward(prog, tissue, states, mask, with_m0=True, launch=shape)
+    p = packed_from_events(ev, t1, t2, states, m0=m0, b1=b1)
+    key = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1"}
+    assert max_rel(sig.real.cpu().numpy(), -O.forward(p, "f64")) <= 1e-5
+    for k, n in enumerate(names):
+        assert max_rel(jac[:, k].real.cpu().numpy(), -O.tangent(p, "f64", **{key[n]: 1.0})) <= \
+            GRAD_TOL, n
+    p0 = O.forward(p, "f64") / m0[:, None]
+    assert max_rel(jac[:, -1].real.cpu().numpy(), -p0) <= 1e-5
+    s0 = rng.standard_normal((V, ev.outputs)).astype(np.float32)
+    sk = rng.standard_normal((V, len(names) + 1, ev.outputs)).astype(np.float32)
+    curvature = {n: torch.zeros(V, device=cuda) for n in ("t1_ms", "t2_ms", "m0", "b1")}
+    curvature["flip_rad"] = torch.zeros((1, ev.events), device=cuda)
+    engine.design_reverse(prog, tissue, states, mask,
+                          torch.from_numpy((-sk).astype(np.complex64)).to(cuda), traj,
+                          seed_signal=torch.from_numpy((-s0).astype(np.complex64)).to(cuda),
+                          with_m0=True, curvature=curvature, launch=shape)
+    # The M0 column's seed acts on F+[0] = signal / m0.
+    want = O.adjoint(p, s0 + sk[:, -1] / m0[:, None], "f64")
+    want["m0"] = want["m0"] - (sk[:, -1] * p0).sum(1) / m0
+    for k, n in enumerate(names):
+        _, c = O.second(p, sk[:, k], "f64", **{key[n]: 1.0})
+        for g in want:
+            want[g] = want[g] + c[g]
+    for g in ("t1_ms", "t2_ms", "m0", "b1", "flip_rad"):
+        got = curvature[g].cpu().numpy().reshape(want[g].shape)
+        assert max_rel(got, want[g]) <= GRAD_TOL, g
 
 
 def test_m0_column_and_order(cuda):

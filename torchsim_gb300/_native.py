@@ -153,6 +153,14 @@ SIGNATURES: dict[str, tuple] = {
                                       ctypes.POINTER(Direction), _int, _int, _int, _vp, _vp, _vp,
                                       _vp,
                                       _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_design_plan": (_int, [_vp, _i64, _i64, ctypes.c_uint, ctypes.POINTER(Launch),
+                                   ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "tsg_epg_design_forward": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.c_uint,
+                                      _int, _int, _vp, _vp, _vp, _vp, _vp,
+                                      ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_design_reverse": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.c_uint,
+                                      _int, _vp, _vp, _int, _vp, ctypes.POINTER(Gradients), _vp,
+                                      _i64, ctypes.POINTER(Launch), _vp]),
     "tsg_epg_second_reverse": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64,
                                       ctypes.POINTER(Direction), _int, _int, _vp, _vp, _int, _vp,
                                       ctypes.POINTER(Gradients), ctypes.POINTER(Gradients), _vp,

@@ -20,14 +20,43 @@ extern const SecondEntry kSecondK2[];
 extern const int kSecondK2Count;
 extern const SecondEntry kSecondK3[];
 extern const int kSecondK3Count;
+extern const SecondEntry kSecondHotT1[];
+extern const int kSecondHotT1Count;
+extern const SecondEntry kSecondHotT2[];
+extern const int kSecondHotT2Count;
+extern const SecondEntry kSecondHotB1[];
+extern const int kSecondHotB1Count;
+extern const SecondEntry kSecondHotT1T2[];
+extern const int kSecondHotT1T2Count;
+extern const SecondEntry kSecondHotT1B1[];
+extern const int kSecondHotT1B1Count;
+extern const SecondEntry kSecondHotT2B1[];
+extern const int kSecondHotT2B1Count;
+extern const SecondEntry kSecondHotT1T2B1[];
+extern const int kSecondHotT1T2B1Count;
 
-const SecondEntry* second_table(int k, int* count) {
-    switch (k) {
-        case 1: *count = kSecondK1Count; return kSecondK1;
-        case 2: *count = kSecondK2Count; return kSecondK2;
-        case 3: *count = kSecondK3Count; return kSecondK3;
-        default: *count = 0; return nullptr;
+const SecondEntry* second_table(int k, int hot, int* count) {
+    if (hot == 0) {
+        switch (k) {
+            case 1: *count = kSecondK1Count; return kSecondK1;
+            case 2: *count = kSecondK2Count; return kSecondK2;
+            case 3: *count = kSecondK3Count; return kSecondK3;
+            default: break;
+        }
+    } else {
+        switch (hot) {
+            case 1: *count = kSecondHotT1Count; return kSecondHotT1;
+            case 2: *count = kSecondHotT2Count; return kSecondHotT2;
+            case 3: *count = kSecondHotB1Count; return kSecondHotB1;
+            case 1 | 2 << 2: *count = kSecondHotT1T2Count; return kSecondHotT1T2;
+            case 1 | 3 << 2: *count = kSecondHotT1B1Count; return kSecondHotT1B1;
+            case 2 | 3 << 2: *count = kSecondHotT2B1Count; return kSecondHotT2B1;
+            case 1 | 2 << 2 | 3 << 4: *count = kSecondHotT1T2B1Count; return kSecondHotT1T2B1;
+            default: break;
+        }
     }
+    *count = 0;
+    return nullptr;
 }
 
 namespace {
@@ -48,8 +77,8 @@ __global__ void gather_second_directions(const OpSource* src, int64_t ops, int64
 }
 
 // Sums the per-warp event partials in warp order and scatters them to the
-// events the ops came from (adding): curvature into curve_*, for one
-// direction also the values into value_*.
+// events the ops came from (adding): curvature into curve_*, with two pairs
+// also the values into value_*.
 __global__ void reduce_second_events(const float2* partial, int64_t warps, int64_t n_ops,
                                      int64_t trains, int64_t events, int pairs,
                                      const OpSource* src, float* curve_flip, float* curve_dt,
@@ -87,11 +116,10 @@ struct TissueSlots {
     float* slot[1 + kSecondMaxK][5];
 };
 
-__global__ void reduce_second_tissue(const float* partial, int64_t atoms, int64_t trains, int k,
+__global__ void reduce_second_tissue(const float* partial, int64_t atoms, int64_t trains, int nv,
                                      TissueSlots out) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= atoms) return;
-    const int nv = 5 * (1 + k);
     for (int j = 0; j < nv; ++j) {
         float sum = 0.f;
         for (int64_t t = 0; t < trains; ++t) sum += partial[(t * atoms + i) * nv + j];
@@ -100,15 +128,8 @@ __global__ void reduce_second_tissue(const float* partial, int64_t atoms, int64_
     }
 }
 
-int sm_count_second() {
-    static int count = [] {
-        int dev = 0, n = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        return n > 0 ? n : 152;
-    }();
-    return count;
-}
+int event_pairs(int k, int hot) { return (k == 1 && hot == 0) ? 2 : 1; }
+int tissue_values(int k, int hot) { return hot ? 5 : 5 * (1 + k); }
 
 struct SecondPlan {
     const SecondEntry* entry = nullptr;
@@ -122,22 +143,31 @@ struct SecondPlan {
     size_t smem = 0;
 };
 
-int second_plan(const tsg_program* prog, int64_t atoms, int64_t states, int k,
+// The kernel pair and buffer sizes. Without a requested shape: two orders
+// per lane (the fewest registers, so the most resident warps), on the fewest
+// lanes that hold the states; four orders where two would need more than 32
+// lanes.
+int second_plan(const tsg_program* prog, int64_t atoms, int64_t states, int k, int hot,
                 const tsg_launch* want, bool event_directions, SecondPlan* plan) {
     if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
     if (atoms < 0 || states < 1) return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
     if (k < 1 || k > kSecondMaxK) return fail(TSG_ERR_ARGUMENT, "1 to 3 directions");
     if (states > 64) return fail(TSG_ERR_CAPACITY, "second order takes at most 64 states");
     int count = 0;
-    const SecondEntry* table = second_table(k, &count);
+    const SecondEntry* table = second_table(k, hot, &count);
+    if (!table) return fail(TSG_ERR_ARGUMENT, "unknown direction set");
     const SecondEntry* best = nullptr;
+    auto better = [](const SecondEntry& e, const SecondEntry* b) {
+        if (!b) return true;
+        if (e.orders_per_lane != b->orders_per_lane) return e.orders_per_lane < b->orders_per_lane;
+        return e.lanes_per_voxel < b->lanes_per_voxel;
+    };
     for (int i = 0; i < count; ++i) {
         const SecondEntry& e = table[i];
         if (want && want->lanes_per_voxel > 0 && e.lanes_per_voxel != want->lanes_per_voxel) continue;
         if (want && want->orders_per_lane > 0 && e.orders_per_lane != want->orders_per_lane) continue;
         if (e.lanes_per_voxel * e.orders_per_lane < states) continue;
-        // The fewest lanes that hold the orders.
-        if (!best || e.lanes_per_voxel < best->lanes_per_voxel) best = &e;
+        if (better(e, best)) best = &e;
     }
     if (!best) return fail(TSG_ERR_UNSUPPORTED, "no second-order kernel for this state count / launch shape");
     plan->entry = best;
@@ -146,20 +176,23 @@ int second_plan(const tsg_program* prog, int64_t atoms, int64_t states, int k,
     const int vpb = kSecondWarps * (32 / best->lanes_per_voxel);
     plan->blocks = (atoms + vpb - 1) / vpb;
     plan->warps_per_train = plan->blocks * kSecondWarps;
-    plan->state_bytes = second_trajectory_floats(trains, atoms, ops, int(states), k) * 4;
+    plan->state_bytes = second_trajectory_floats(trains, atoms, ops, best->lanes_per_voxel,
+                                                 best->orders_per_lane, k) * 4;
     plan->trajectory_bytes =
         align256(plan->state_bytes) + second_record_floats(trains, atoms, prog->host.outputs, k) * 4;
     plan->dir_bytes = event_directions ? align256(int64_t(k) * trains * ops * 8) : 0;
-    plan->event_bytes =
-        align256(trains * plan->warps_per_train * ops * second_event_pairs(k) * 8);
-    plan->workspace_bytes =
-        plan->dir_bytes + plan->event_bytes + trains * atoms * 5 * (1 + k) * int64_t(sizeof(float));
+    plan->event_bytes = align256(trains * plan->warps_per_train * ops * event_pairs(k, hot) * 8);
+    plan->workspace_bytes = plan->dir_bytes + plan->event_bytes +
+                            trains * atoms * tissue_values(k, hot) * int64_t(sizeof(float));
+    // The reverse sweep's rings (states per lane; transcendentals, seeds and
+    // records per voxel slot), its ops and op directions.
     const int T = 32 * kSecondWarps;
     const int RP = best->orders_per_lane / 2;
-    plan->smem = size_t(kSecondRing) * T *
-                     (sizeof(float4) + sizeof(float2) * size_t((k + 1) * 3 * RP) +
-                      sizeof(float2) * size_t(k + 1) + sizeof(float)) +
-                 sizeof(float2) * size_t(second_event_pairs(k)) * T * (kSecondGroup + 1) +
+    const size_t slots = size_t(vpb), slots4 = (slots + 3) & ~size_t(3);
+    plan->smem = size_t(kSecondRing) *
+                     (sizeof(float2) * size_t((k + 1) * 3 * RP) * T +
+                      sizeof(float2) * size_t(k + 1) * slots + sizeof(float) * slots4) +
+                 sizeof(float4) * slots * size_t(best->lanes_per_voxel) +
                  sizeof(Op) * size_t(ops) + (event_directions ? sizeof(float2) * size_t(k * ops) : 0);
     if (plan->smem > 220 * 1024)
         return fail(TSG_ERR_CAPACITY, "the program does not fit in shared memory for the reverse sweep");
@@ -173,18 +206,15 @@ bool has_event_directions(const tsg_direction* d, int k) {
     return false;
 }
 
-int check_second(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms,
-                 const tsg_direction* d, int k) {
+int check_common(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms) {
     if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
     if (!tissue || (atoms > 0 && (!tissue->t1_ms || !tissue->t2_ms)))
         return fail(TSG_ERR_ARGUMENT, "t1 and t2 are required");
-    if (k < 1 || k > kSecondMaxK) return fail(TSG_ERR_ARGUMENT, "1 to 3 directions");
-    if (!d) return fail(TSG_ERR_ARGUMENT, "null directions");
     return TSG_OK;
 }
 
-SecondArgs second_args(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms,
-                       int64_t states, const tsg_direction* d, int k) {
+SecondArgs base_second_args(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms,
+                            int64_t states) {
     SecondArgs a{};
     a.ops = prog->d_ops;
     a.n_ops = int(prog->host.ops);
@@ -196,6 +226,10 @@ SecondArgs second_args(const tsg_program* prog, const tsg_tissue* tissue, int64_
     a.m0 = tissue->m0;
     a.b1 = tissue->b1;
     a.inv = tissue->inversion;
+    return a;
+}
+
+void set_directions(SecondArgs& a, const tsg_direction* d, int k) {
     for (int i = 0; i < k; ++i) {
         a.dir[i][0] = d[i].t1_ms;
         a.dir[i][1] = d[i].t2_ms;
@@ -203,7 +237,6 @@ SecondArgs second_args(const tsg_program* prog, const tsg_tissue* tissue, int64_
         a.dir[i][3] = d[i].b1;
         a.dir[i][4] = d[i].inversion;
     }
-    return a;
 }
 
 // Fills the per-op directions of the K directions into `dirs`.
@@ -220,99 +253,50 @@ int gather_all(const tsg_program* prog, const tsg_direction* d, int k, float2* d
     return TSG_OK;
 }
 
-}  // namespace
-
-}  // namespace tsg
-
-using namespace tsg;
-
-extern "C" int tsg_epg_second_plan(const tsg_program* program, int64_t atom_count,
-                                   int64_t state_count, int direction_count,
-                                   int event_directions, const tsg_launch* launch,
-                                   int64_t* trajectory_bytes, int64_t* workspace_bytes) {
-    SecondPlan plan;
-    int rc = second_plan(program, atom_count, state_count, direction_count, launch,
-                         event_directions != 0, &plan);
-    if (rc) return rc;
-    if (trajectory_bytes) *trajectory_bytes = plan.trajectory_bytes;
-    if (workspace_bytes) *workspace_bytes = plan.workspace_bytes;
-    return TSG_OK;
+// The one-hot direction code of a TSG_TANGENT_T1 | T2 | B1 mask (those
+// properties' unit tangents, in that order), and its direction count.
+int hot_code(unsigned mask, int* k) {
+    int code = 0, n = 0;
+    const unsigned bits[3] = {TSG_TANGENT_T1, TSG_TANGENT_T2, TSG_TANGENT_B1};
+    for (int p = 0; p < 3; ++p)
+        if (mask & bits[p]) code |= (p + 1) << (2 * n++);
+    *k = n;
+    return code;
 }
 
-extern "C" int tsg_epg_second_forward(const tsg_program* program, const tsg_tissue* tissue,
-                                      int64_t atom_count, int64_t state_count,
-                                      const tsg_direction* directions, int direction_count,
-                                      int with_m0, int layout, float* sig_a, float* sig_b,
-                                      float* jac_a, float* jac_b, void* trajectory,
-                                      void* workspace, const tsg_launch* launch, void* stream) {
-    int rc = check_second(program, tissue, atom_count, directions, direction_count);
-    if (rc) return rc;
-    const int k = direction_count;
-    const bool evdir = has_event_directions(directions, k);
-    SecondPlan plan;
-    rc = second_plan(program, atom_count, state_count, k, launch, evdir, &plan);
-    if (rc) return rc;
-    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+int run_forward(const tsg_program* program, const SecondPlan& plan, SecondArgs a, int with_m0,
+                int layout, float* sig_a, float* sig_b, float* jac_a, float* jac_b,
+                void* trajectory, cudaStream_t s) {
     if (!trajectory) return fail(TSG_ERR_ARGUMENT, "null trajectory");
-    if (evdir && !workspace) return fail(TSG_ERR_ARGUMENT, "null workspace");
     if (layout != TSG_LAYOUT_PLANES && layout != TSG_LAYOUT_COMPLEX_IJ && layout != TSG_LAYOUT_COMPLEX)
         return fail(TSG_ERR_ARGUMENT, "unknown layout");
     if (layout == TSG_LAYOUT_PLANES && ((sig_a && !sig_b) || (jac_a && !jac_b)))
         return fail(TSG_ERR_ARGUMENT, "the planes layout writes the imaginary plane");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    SecondArgs a = second_args(program, tissue, atom_count, state_count, directions, k);
-    if (evdir) {
-        a.op_dir = static_cast<const float2*>(workspace);
-        rc = gather_all(program, directions, k, static_cast<float2*>(workspace), s);
-        if (rc) return rc;
-    }
     a.layout = layout;
     a.with_m0 = with_m0 ? 1 : 0;
     a.sig_a = sig_a;
     a.sig_b = layout == TSG_LAYOUT_PLANES ? sig_b : nullptr;
-    if (layout != TSG_LAYOUT_PLANES && !sig_a) a.sig_a = nullptr;
     a.jac_a = jac_a;
     a.jac_b = layout == TSG_LAYOUT_PLANES ? jac_b : nullptr;
     a.traj = static_cast<float2*>(trajectory);
     a.traj_rec = reinterpret_cast<float*>(static_cast<char*>(trajectory) + align256(plan.state_bytes));
     const int vpb = 4 * (32 / plan.entry->lanes_per_voxel);
-    const int64_t blocks = (atom_count + vpb - 1) / vpb;
+    const int64_t blocks = (a.atoms + vpb - 1) / vpb;
     if (blocks > 0x7fffffffLL) return fail(TSG_ERR_CAPACITY, "too many voxels for one launch");
     plan.entry->forward(a, dim3(unsigned(blocks), unsigned(program->host.trains)), dim3(128), 0, s);
     TSG_CUDA(cudaGetLastError());
     return TSG_OK;
 }
 
-extern "C" int tsg_epg_second_reverse(const tsg_program* program, const tsg_tissue* tissue,
-                                      int64_t atom_count, int64_t state_count,
-                                      const tsg_direction* directions, int direction_count,
-                                      int with_m0, const float* seed_signal,
-                                      const float* seed_derivatives, int seed_layout,
-                                      const void* trajectory,
-                                      const tsg_gradients* curvature, const tsg_gradients* values,
-                                      void* workspace, int64_t workspace_bytes,
-                                      const tsg_launch* launch, void* stream) {
-    int rc = check_second(program, tissue, atom_count, directions, direction_count);
-    if (rc) return rc;
-    const int k = direction_count;
-    const bool evdir = has_event_directions(directions, k);
-    SecondPlan plan;
-    rc = second_plan(program, atom_count, state_count, k, launch, evdir, &plan);
-    if (rc) return rc;
-    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
-    if (!trajectory || !workspace || !seed_derivatives)
+int run_reverse(const tsg_program* program, const SecondPlan& plan, SecondArgs a, int k, int hot,
+                int with_m0, const float* seed_signal, const float* seed_derivatives,
+                int seed_layout, const void* trajectory, const tsg_gradients* curvature,
+                const tsg_gradients* values, char* ws, int64_t workspace_bytes, cudaStream_t s) {
+    if (!trajectory || !ws || !seed_derivatives)
         return fail(TSG_ERR_ARGUMENT, "null trajectory, workspace or seed");
     if (workspace_bytes < plan.workspace_bytes) return fail(TSG_ERR_ARGUMENT, "workspace too small");
     if (seed_layout != TSG_LAYOUT_PLANES && seed_layout != TSG_LAYOUT_COMPLEX_IJ)
         return fail(TSG_ERR_ARGUMENT, "unknown seed layout");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    SecondArgs a = second_args(program, tissue, atom_count, state_count, directions, k);
-    char* ws = static_cast<char*>(workspace);
-    if (evdir) {
-        a.op_dir = reinterpret_cast<const float2*>(ws);
-        rc = gather_all(program, directions, k, reinterpret_cast<float2*>(ws), s);
-        if (rc) return rc;
-    }
     a.traj = const_cast<float2*>(static_cast<const float2*>(trajectory));
     a.traj_rec = reinterpret_cast<float*>(const_cast<char*>(static_cast<const char*>(trajectory)) +
                                           align256(plan.state_bytes));
@@ -331,12 +315,13 @@ extern "C" int tsg_epg_second_reverse(const tsg_program* program, const tsg_tiss
     TSG_CUDA(cudaGetLastError());
     const int64_t ops = program->host.ops;
     const int64_t n_ev = ops * program->host.trains;
-    const bool one = k == 1;
+    const int pairs = event_pairs(k, hot);
     reduce_second_events<<<unsigned((n_ev + 127) / 128), 128, 0, s>>>(
         a.event_partial, plan.warps_per_train, ops, program->host.trains, program->host.events,
-        second_event_pairs(k), program->d_src, curvature ? curvature->flip_rad : nullptr,
-        curvature ? curvature->duration_s : nullptr, one && values ? values->flip_rad : nullptr,
-        one && values ? values->duration_s : nullptr);
+        pairs, program->d_src, curvature ? curvature->flip_rad : nullptr,
+        curvature ? curvature->duration_s : nullptr,
+        pairs == 2 && values ? values->flip_rad : nullptr,
+        pairs == 2 && values ? values->duration_s : nullptr);
     TSG_CUDA(cudaGetLastError());
     TissueSlots slots{};
     if (curvature) {
@@ -346,7 +331,7 @@ extern "C" int tsg_epg_second_reverse(const tsg_program* program, const tsg_tiss
         slots.slot[0][3] = curvature->b1;
         slots.slot[0][4] = curvature->inversion;
     }
-    if (values)
+    if (values && hot == 0)
         for (int i = 0; i < k; ++i) {
             slots.slot[1 + i][0] = values[i].t1_ms;
             slots.slot[1 + i][1] = values[i].t2_ms;
@@ -354,10 +339,146 @@ extern "C" int tsg_epg_second_reverse(const tsg_program* program, const tsg_tiss
             slots.slot[1 + i][3] = values[i].b1;
             slots.slot[1 + i][4] = values[i].inversion;
         }
-    reduce_second_tissue<<<unsigned((atom_count + 127) / 128), 128, 0, s>>>(
-        a.tissue_partial, atom_count, program->host.trains, k, slots);
+    reduce_second_tissue<<<unsigned((a.atoms + 127) / 128), 128, 0, s>>>(
+        a.tissue_partial, a.atoms, program->host.trains, tissue_values(k, hot), slots);
     TSG_CUDA(cudaGetLastError());
     return TSG_OK;
+}
+
+}  // namespace
+
+}  // namespace tsg
+
+using namespace tsg;
+
+extern "C" int tsg_epg_second_plan(const tsg_program* program, int64_t atom_count,
+                                   int64_t state_count, int direction_count,
+                                   int event_directions, const tsg_launch* launch,
+                                   int64_t* trajectory_bytes, int64_t* workspace_bytes) {
+    SecondPlan plan;
+    int rc = second_plan(program, atom_count, state_count, direction_count, 0, launch,
+                         event_directions != 0, &plan);
+    if (rc) return rc;
+    if (trajectory_bytes) *trajectory_bytes = plan.trajectory_bytes;
+    if (workspace_bytes) *workspace_bytes = plan.workspace_bytes;
+    return TSG_OK;
+}
+
+extern "C" int tsg_epg_second_forward(const tsg_program* program, const tsg_tissue* tissue,
+                                      int64_t atom_count, int64_t state_count,
+                                      const tsg_direction* directions, int direction_count,
+                                      int with_m0, int layout, float* sig_a, float* sig_b,
+                                      float* jac_a, float* jac_b, void* trajectory,
+                                      void* workspace, const tsg_launch* launch, void* stream) {
+    int rc = check_common(program, tissue, atom_count);
+    if (rc) return rc;
+    const int k = direction_count;
+    if (!directions) return fail(TSG_ERR_ARGUMENT, "null directions");
+    if (k < 1 || k > kSecondMaxK) return fail(TSG_ERR_ARGUMENT, "1 to 3 directions");
+    const bool evdir = has_event_directions(directions, k);
+    SecondPlan plan;
+    rc = second_plan(program, atom_count, state_count, k, 0, launch, evdir, &plan);
+    if (rc) return rc;
+    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+    if (evdir && !workspace) return fail(TSG_ERR_ARGUMENT, "null workspace");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    SecondArgs a = base_second_args(program, tissue, atom_count, state_count);
+    set_directions(a, directions, k);
+    if (evdir) {
+        a.op_dir = static_cast<const float2*>(workspace);
+        rc = gather_all(program, directions, k, static_cast<float2*>(workspace), s);
+        if (rc) return rc;
+    }
+    return run_forward(program, plan, a, with_m0, layout, sig_a, sig_b, jac_a, jac_b, trajectory, s);
+}
+
+extern "C" int tsg_epg_second_reverse(const tsg_program* program, const tsg_tissue* tissue,
+                                      int64_t atom_count, int64_t state_count,
+                                      const tsg_direction* directions, int direction_count,
+                                      int with_m0, const float* seed_signal,
+                                      const float* seed_derivatives, int seed_layout,
+                                      const void* trajectory,
+                                      const tsg_gradients* curvature, const tsg_gradients* values,
+                                      void* workspace, int64_t workspace_bytes,
+                                      const tsg_launch* launch, void* stream) {
+    int rc = check_common(program, tissue, atom_count);
+    if (rc) return rc;
+    const int k = direction_count;
+    if (!directions) return fail(TSG_ERR_ARGUMENT, "null directions");
+    if (k < 1 || k > kSecondMaxK) return fail(TSG_ERR_ARGUMENT, "1 to 3 directions");
+    const bool evdir = has_event_directions(directions, k);
+    SecondPlan plan;
+    rc = second_plan(program, atom_count, state_count, k, 0, launch, evdir, &plan);
+    if (rc) return rc;
+    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    SecondArgs a = base_second_args(program, tissue, atom_count, state_count);
+    set_directions(a, directions, k);
+    char* ws = static_cast<char*>(workspace);
+    if (evdir && ws) {
+        a.op_dir = reinterpret_cast<const float2*>(ws);
+        rc = gather_all(program, directions, k, reinterpret_cast<float2*>(ws), s);
+        if (rc) return rc;
+    }
+    return run_reverse(program, plan, a, k, 0, with_m0, seed_signal, seed_derivatives, seed_layout,
+                       trajectory, curvature, values, ws, workspace_bytes, s);
+}
+
+extern "C" int tsg_epg_design_plan(const tsg_program* program, int64_t atom_count,
+                                   int64_t state_count, unsigned tangent_mask,
+                                   const tsg_launch* launch, int64_t* trajectory_bytes,
+                                   int64_t* workspace_bytes) {
+    int k = 0;
+    const int hot = hot_code(tangent_mask, &k);
+    if (k == 0 || (tangent_mask & ~7u)) return fail(TSG_ERR_ARGUMENT, "tangent_mask takes T1, T2, B1");
+    SecondPlan plan;
+    int rc = second_plan(program, atom_count, state_count, k, hot, launch, false, &plan);
+    if (rc) return rc;
+    if (trajectory_bytes) *trajectory_bytes = plan.trajectory_bytes;
+    if (workspace_bytes) *workspace_bytes = plan.workspace_bytes;
+    return TSG_OK;
+}
+
+extern "C" int tsg_epg_design_forward(const tsg_program* program, const tsg_tissue* tissue,
+                                      int64_t atom_count, int64_t state_count,
+                                      unsigned tangent_mask, int with_m0, int layout,
+                                      float* sig_a, float* sig_b, float* jac_a, float* jac_b,
+                                      void* trajectory, const tsg_launch* launch, void* stream) {
+    int rc = check_common(program, tissue, atom_count);
+    if (rc) return rc;
+    int k = 0;
+    const int hot = hot_code(tangent_mask, &k);
+    if (k == 0 || (tangent_mask & ~7u)) return fail(TSG_ERR_ARGUMENT, "tangent_mask takes T1, T2, B1");
+    SecondPlan plan;
+    rc = second_plan(program, atom_count, state_count, k, hot, launch, false, &plan);
+    if (rc) return rc;
+    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+    SecondArgs a = base_second_args(program, tissue, atom_count, state_count);
+    return run_forward(program, plan, a, with_m0, layout, sig_a, sig_b, jac_a, jac_b, trajectory,
+                       static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tsg_epg_design_reverse(const tsg_program* program, const tsg_tissue* tissue,
+                                      int64_t atom_count, int64_t state_count,
+                                      unsigned tangent_mask, int with_m0,
+                                      const float* seed_signal, const float* seed_derivatives,
+                                      int seed_layout, const void* trajectory,
+                                      const tsg_gradients* curvature, void* workspace,
+                                      int64_t workspace_bytes, const tsg_launch* launch,
+                                      void* stream) {
+    int rc = check_common(program, tissue, atom_count);
+    if (rc) return rc;
+    int k = 0;
+    const int hot = hot_code(tangent_mask, &k);
+    if (k == 0 || (tangent_mask & ~7u)) return fail(TSG_ERR_ARGUMENT, "tangent_mask takes T1, T2, B1");
+    SecondPlan plan;
+    rc = second_plan(program, atom_count, state_count, k, hot, launch, false, &plan);
+    if (rc) return rc;
+    if (atom_count == 0 || program->host.ops == 0) return TSG_OK;
+    SecondArgs a = base_second_args(program, tissue, atom_count, state_count);
+    return run_reverse(program, plan, a, k, hot, with_m0, seed_signal, seed_derivatives,
+                       seed_layout, trajectory, curvature, nullptr, static_cast<char*>(workspace),
+                       workspace_bytes, static_cast<cudaStream_t>(stream));
 }
 
 // ---- the host-buffer drop-in -------------------------------------------------

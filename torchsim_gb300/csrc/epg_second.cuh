@@ -32,20 +32,21 @@
 //   recovery e0 at order 0), and r = 1000/T, r' = -1000 T'/T^2 chain to T.
 //
 // The forward stores every op's entry state of x and of each t_k (the
-// trajectory, in tiles of 32 atoms) and every recorded F+[0]; the reverse
+// trajectory, one tile per warp: per op, state and plane the warp's 32 lanes'
+// order pairs are 32 * RP consecutive float2, so every store and every load
+// is a whole, aligned line) and every recorded F+[0]; the reverse
 // streams them back through a cp.async ring, so nothing is re-run but each
-// op's relaxation and pre-shift. Per-event partials are parked per lane in
-// shared memory and summed over the warp in a fixed order every 32 ops, as
-// in the first-order trajectory adjoint; tissue gradients are summed over a
-// voxel's lanes with shuffles. No atomics: results are deterministic.
+// op's relaxation and pre-shift. Per-event partials are summed over the warp
+// with a fixed butterfly of shuffles after each op; tissue gradients are
+// summed over a voxel's lanes with shuffles. No atomics: results are
+// deterministic.
 #pragma once
 #include "epg_adjoint.cuh"
 
 namespace tsg {
 
 constexpr int kSecondMaxK = 3;
-constexpr int kSecondRing = 4;
-constexpr int kSecondGroup = 32;
+constexpr int kSecondRing = 2;
 constexpr int kSecondWarps = 2;
 
 struct SecondArgs {
@@ -71,9 +72,9 @@ struct SecondArgs {
     float* sig_b;
     float* jac_a;
     float* jac_b;
-    // Trajectory: [train][atom / 32][op][state][plane][pair][atom % 32]
-    // float2 (state 0 = x, k + 1 = t_k), and the recorded F+[0] of each
-    // state, [train][output][state][atom].
+    // Trajectory: [train][warp][op][state][plane][lane][RP] float2 (state
+    // 0 = x, k + 1 = t_k; warp = atom / (32 / lanes_per_voxel)), and the
+    // recorded F+[0] of each state, [train][output][state][atom].
     float2* traj;
     float* traj_rec;
     // Reverse: cotangents of the signal (nullable) and of the derivatives
@@ -90,13 +91,16 @@ struct SecondArgs {
     int64_t warps_per_train;
 };
 
-__host__ __device__ inline int second_event_pairs(int k) { return k == 1 ? 2 : 1; }
+// Warps (trajectory tiles) per train for lanes_per_voxel lanes a voxel.
+inline int64_t second_warps(int64_t atoms, int lanes_per_voxel) {
+    const int64_t vpw = 32 / lanes_per_voxel;
+    return (atoms + vpw - 1) / vpw;
+}
 
-inline int64_t second_trajectory_floats(int64_t trains, int64_t atoms, int64_t ops, int states,
-                                        int k) {
-    const int64_t np = (states + 1) / 2;
-    const int64_t tiles = (atoms + 31) / 32;
-    return trains * tiles * ops * (k + 1) * 3 * np * 32 * 2;
+inline int64_t second_trajectory_floats(int64_t trains, int64_t atoms, int64_t ops,
+                                        int lanes_per_voxel, int orders_per_lane, int k) {
+    return trains * second_warps(atoms, lanes_per_voxel) * ops * (k + 1) * 3 * 32 *
+           int64_t(orders_per_lane);
 }
 
 inline int64_t second_record_floats(int64_t trains, int64_t atoms, int64_t outputs, int k) {
@@ -117,6 +121,12 @@ __device__ __forceinline__ void store_sample(int layout, float* a, float* b, int
     }
 }
 
+// A one-hot direction set (HOT != 0): direction k is the unit tangent of
+// one property, (HOT >> 2k) & 3 = 1 T1, 2 T2, 3 B1, with no event
+// directions; its zero terms are left out at compile time. HOT == 0: general
+// directions.
+__host__ __device__ constexpr int hot_dir(int hot, int k) { return (hot >> (2 * k)) & 3; }
+
 // The voxel constants both sweeps use.
 template <int K>
 struct Voxel {
@@ -124,7 +134,7 @@ struct Voxel {
     float dt1[K], dt2[K], dm0[K], db1[K], deff[K];
 };
 
-template <int K>
+template <int K, int HOT>
 __device__ __forceinline__ Voxel<K> load_voxel(const SecondArgs& a, int64_t ac) {
     Voxel<K> v;
     v.t1 = a.t1[ac];
@@ -138,6 +148,13 @@ __device__ __forceinline__ Voxel<K> load_voxel(const SecondArgs& a, int64_t ac) 
     v.w2 = 1000.f / (v.t2 * v.t2);
 #pragma unroll
     for (int k = 0; k < K; ++k) {
+        if (HOT) {
+            v.dt1[k] = hot_dir(HOT, k) == 1 ? 1.f : 0.f;
+            v.dt2[k] = hot_dir(HOT, k) == 2 ? 1.f : 0.f;
+            v.db1[k] = hot_dir(HOT, k) == 3 ? 1.f : 0.f;
+            v.dm0[k] = v.deff[k] = 0.f;
+            continue;
+        }
         v.dt1[k] = a.dir[k][0] ? a.dir[k][0][ac] : 0.f;
         v.dt2[k] = a.dir[k][1] ? a.dir[k][1][ac] : 0.f;
         // m0, b1 and the inversion efficiency carry a direction only where
@@ -152,7 +169,7 @@ __device__ __forceinline__ Voxel<K> load_voxel(const SecondArgs& a, int64_t ac) 
 // Relaxation of x and the tangents over one op: t_k <- E (t_k + eps_k (x -
 // e0)), x <- E x + (1 - E1) e0, e0 the recovery target (Z at order 0, held
 // by lane 0's first slot).
-template <int RP, int K>
+template <int RP, int K, int HOT>
 __device__ __forceinline__ void relax_all(float2 (&P)[K + 1][RP], float2 (&M)[K + 1][RP],
                                           float2 (&Z)[K + 1][RP], float e1, float e2,
                                           const float (&eps1)[K], const float (&eps2)[K], int q) {
@@ -161,13 +178,24 @@ __device__ __forceinline__ void relax_all(float2 (&P)[K + 1][RP], float2 (&M)[K 
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const float2 a1 = dup(eps1[k]), a2 = dup(eps2[k]);
+        const bool e2k = !HOT || hot_dir(HOT, k) == 2;
+        const bool e1k = !HOT || hot_dir(HOT, k) == 1;
 #pragma unroll
         for (int kk = 0; kk < RP; ++kk) {
-            P[k + 1][kk] = mul2(E2, fma2(a2, P[0][kk], P[k + 1][kk]));
-            M[k + 1][kk] = mul2(E2, fma2(a2, M[0][kk], M[k + 1][kk]));
-            float2 zx = Z[0][kk];
-            if (kk == 0) zx.x = z0;
-            Z[k + 1][kk] = mul2(E1, fma2(a1, zx, Z[k + 1][kk]));
+            if (e2k) {
+                P[k + 1][kk] = mul2(E2, fma2(a2, P[0][kk], P[k + 1][kk]));
+                M[k + 1][kk] = mul2(E2, fma2(a2, M[0][kk], M[k + 1][kk]));
+            } else {
+                P[k + 1][kk] = mul2(E2, P[k + 1][kk]);
+                M[k + 1][kk] = mul2(E2, M[k + 1][kk]);
+            }
+            if (e1k) {
+                float2 zx = Z[0][kk];
+                if (kk == 0) zx.x = z0;
+                Z[k + 1][kk] = mul2(E1, fma2(a1, zx, Z[k + 1][kk]));
+            } else {
+                Z[k + 1][kk] = mul2(E1, Z[k + 1][kk]);
+            }
         }
     }
 #pragma unroll
@@ -203,13 +231,20 @@ __device__ __forceinline__ void spoil_all(float2 (&P)[K + 1][RP], float2 (&M)[K 
 
 // One op's per-direction scalars: eps1_k, eps2_k (relaxation) and a'_k
 // (rotation); ddt_k and dflip_k from the op's directions.
-template <int K>
+template <int K, int HOT>
 __device__ __forceinline__ void op_directions(const SecondArgs& a, const float2* dirs, int64_t n,
                                               int o, const Op& op, const Voxel<K>& v,
                                               float (&ddt)[K], float (&eps1)[K], float (&eps2)[K],
                                               float (&dal)[K], float (&dfl)[K]) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
+        if (HOT) {
+            ddt[k] = dfl[k] = 0.f;
+            eps1[k] = hot_dir(HOT, k) == 1 ? v.w1 * op.dt : 0.f;
+            eps2[k] = hot_dir(HOT, k) == 2 ? v.w2 * op.dt : 0.f;
+            dal[k] = hot_dir(HOT, k) == 3 ? op.flip : 0.f;
+            continue;
+        }
         const float2 d = dirs ? dirs[k * n + o] : make_float2(0.f, 0.f);
         ddt[k] = d.x;
         dfl[k] = d.y;
@@ -227,7 +262,7 @@ using namespace second_detail;
 
 // Static shared memory: a chunk of ops and of each direction's per-op
 // (d dt, d flip).
-template <int RP, int L, int K>
+template <int RP, int L, int K, int HOT>
 __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a) {
     constexpr int R = 2 * RP;
     constexpr int VPW = 32 / L;
@@ -243,10 +278,9 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
     const bool active = slot < VPW && atom < a.atoms;
     const int64_t ac = active ? atom : 0;
     const int S = a.states;
-    const int NP = (S + 1) >> 1;
     const bool kill = L * R > S;
     const int kill_r = S - q * R;
-    const Voxel<K> v = load_voxel<K>(a, ac);
+    const Voxel<K> v = load_voxel<K, HOT>(a, ac);
 
     float2 P[NS][RP], M[NS][RP], Z[NS][RP];
 #pragma unroll
@@ -259,11 +293,14 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
     const int64_t n_all = int64_t(gridDim.y) * a.n_ops;  // ops of all trains, per direction
     const float2* dirs = a.op_dir ? a.op_dir + train * a.n_ops : nullptr;
     const int64_t row = train * a.atoms + atom;
-    const int64_t tiles = (a.atoms + 31) >> 5;
-    const int64_t op_stride = int64_t(NS) * 3 * NP * 32;
-    float2* lane_traj = a.traj ? a.traj + (train * tiles + (ac >> 5)) * a.n_ops * op_stride +
-                                     (ac & 31) + q * RP * 32
-                               : nullptr;
+    // This warp's tile; lanes of a warp past the last voxel store nothing.
+    const int64_t n_warps = (a.atoms + VPW - 1) / VPW;
+    const int64_t warp_global = int64_t(blockIdx.x) * (blockDim.x >> 5) + warp;
+    const int64_t op_stride = int64_t(NS) * 3 * 32 * RP;
+    float2* lane_traj = (a.traj && warp_global < n_warps)
+                            ? a.traj + (train * n_warps + warp_global) * a.n_ops * op_stride +
+                                  lane * RP
+                            : nullptr;
     const bool lane0 = active && q == 0;
 
     for (int base = 0; base < a.n_ops; base += kOpChunk) {
@@ -279,34 +316,23 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
         for (int i = 0; i < count; ++i) {
             const Op op = s_ops[i];
             const uint32_t code = op.code;
-            if (lane_traj && active) {
+            if (lane_traj) {
                 float2* dst = lane_traj + int64_t(base + i) * op_stride;
 #pragma unroll
                 for (int s = 0; s < NS; ++s)
 #pragma unroll
                     for (int kk = 0; kk < RP; ++kk) {
-                        if (q * RP + kk < NP) {
-                            dst[((s * 3 + 0) * NP + kk) * 32] = P[s][kk];
-                            dst[((s * 3 + 1) * NP + kk) * 32] = M[s][kk];
-                            dst[((s * 3 + 2) * NP + kk) * 32] = Z[s][kk];
-                        }
+                        dst[(s * 3 + 0) * 32 * RP + kk] = P[s][kk];
+                        dst[(s * 3 + 1) * 32 * RP + kk] = M[s][kk];
+                        dst[(s * 3 + 2) * 32 * RP + kk] = Z[s][kk];
                     }
             }
-            float ddt[K], dfl[K];
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                ddt[k] = s_dir[k][i].x;
-                dfl[k] = s_dir[k][i].y;
-            }
-            if (code & OP_RELAX) {
-                float eps1[K], eps2[K];
-#pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    eps1[k] = v.w1 * v.dt1[k] * op.dt - v.r1 * ddt[k];
-                    eps2[k] = v.w2 * v.dt2[k] * op.dt - v.r2 * ddt[k];
-                }
-                relax_all<RP, K>(P, M, Z, expf(-v.r1 * op.dt), expf(-v.r2 * op.dt), eps1, eps2, q);
-            }
+            float ddt[K], eps1[K], eps2[K], dal[K], dfl[K];
+            op_directions<K, HOT>(a, HOT ? nullptr : &s_dir[0][0], kOpChunk, i, op, v, ddt, eps1,
+                                  eps2, dal, dfl);
+            if (code & OP_RELAX)
+                relax_all<RP, K, HOT>(P, M, Z, expf(-v.r1 * op.dt), expf(-v.r2 * op.dt), eps1,
+                                      eps2, q);
             for (int s = 0; s < op_shift1(code); ++s) shift_all<RP, L, K>(P, M, q, kill, kill_r);
             const int rf = op_rf(code);
             if (rf == RF_ROTATE) {
@@ -325,11 +351,18 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
                     const float2 dZ = fma2(hc, w, mul2(nsi2, z));
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        const float2 al = dup(op.flip * v.db1[k] + dfl[k] * v.b1);
                         const float2 tp = P[k + 1][kk], tm = M[k + 1][kk], tz = Z[k + 1][kk];
-                        P[k + 1][kk] = fma2(ch, tp, fma2(sh, tm, fma2(nsi2, tz, mul2(neg1, mul2(al, dM)))));
-                        M[k + 1][kk] = fma2(sh, tp, fma2(ch, tm, fma2(si2, tz, mul2(al, dM))));
-                        Z[k + 1][kk] = fma2(hs, tp, fma2(nhs, tm, fma2(co2, tz, mul2(al, dZ))));
+                        if (!HOT || hot_dir(HOT, k) == 3) {
+                            const float2 al = dup(dal[k]);
+                            const float2 aM = mul2(al, dM);
+                            P[k + 1][kk] = fma2(ch, tp, fma2(sh, tm, fma2(nsi2, tz, mul2(neg1, aM))));
+                            M[k + 1][kk] = fma2(sh, tp, fma2(ch, tm, fma2(si2, tz, aM)));
+                            Z[k + 1][kk] = fma2(hs, tp, fma2(nhs, tm, fma2(co2, tz, mul2(al, dZ))));
+                        } else {
+                            P[k + 1][kk] = fma2(ch, tp, fma2(sh, tm, mul2(nsi2, tz)));
+                            M[k + 1][kk] = fma2(sh, tp, fma2(ch, tm, mul2(si2, tz)));
+                            Z[k + 1][kk] = fma2(hs, tp, fma2(nhs, tm, mul2(co2, tz)));
+                        }
                     }
                     P[0][kk] = fma2(ch, p, fma2(sh, m, mul2(nsi2, z)));
                     M[0][kk] = fma2(sh, p, fma2(ch, m, mul2(si2, z)));
@@ -341,7 +374,8 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
                 for (int kk = 0; kk < RP; ++kk) {
 #pragma unroll
                     for (int k = 0; k < K; ++k)
-                        Z[k + 1][kk] = fma2(f, Z[k + 1][kk], mul2(dup(-v.deff[k]), Z[0][kk]));
+                        Z[k + 1][kk] = HOT ? mul2(f, Z[k + 1][kk])
+                                           : fma2(f, Z[k + 1][kk], mul2(dup(-v.deff[k]), Z[0][kk]));
                     Z[0][kk] = mul2(Z[0][kk], f);
                 }
             }
@@ -357,7 +391,8 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
 #pragma unroll
                     for (int k = 0; k < K; ++k)
                         store_sample(a.layout, a.jac_a, a.jac_b, (row * jc + k) * a.outputs + rec,
-                                     fmaf(v.m0, P[k + 1][0].x, v.dm0[k] * p0));
+                                     HOT ? v.m0 * P[k + 1][0].x
+                                         : fmaf(v.m0, P[k + 1][0].x, v.dm0[k] * p0));
                     if (a.with_m0)
                         store_sample(a.layout, a.jac_a, a.jac_b, (row * jc + K) * a.outputs + rec, p0);
                 }
@@ -377,10 +412,9 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
 
 // Dynamic shared memory: transcendentals [D][T] float4, entry states
 // [D][NS][3][RP][T] float2, (seed, recorded F+[0]) [D][NS][T] float2, the
-// M0 derivative's seed [D][T] float, event partials [NE2][T][G + 1] float2,
-// ops [n_ops], per-direction op directions [K][n_ops] float2 (only with
-// event directions).
-template <int RP, int L, int K>
+// M0 derivative's seed [D][T] float, ops [n_ops], per-direction op
+// directions [K][n_ops] float2 (only with event directions).
+template <int RP, int L, int K, int HOT>
 __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const SecondArgs a) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     constexpr int W = kSecondWarps;
@@ -389,8 +423,7 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
     constexpr int VPW = 32 / L;
     constexpr int NS = K + 1;
     constexpr int D = kSecondRing;
-    constexpr int G = kSecondGroup;
-    constexpr int NE2 = K == 1 ? 2 : 1;
+    constexpr int NE2 = (K == 1 && !HOT) ? 2 : 1;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int q = lane % L;
@@ -401,27 +434,30 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
     const bool active = slot < VPW && atom < a.atoms;
     const int64_t ac = active ? atom : 0;
     const int S = a.states;
-    const int NP = (S + 1) >> 1;
     const int n_ops = a.n_ops;
     const bool kill = L * R > S;
     const int kill_r = S - q * R;
     const bool lane0 = active && q == 0;
     const int64_t n = a.atoms;
     const int64_t row = train * n + atom;
+    const int vslot = warp * VPW + (slot < VPW ? slot : VPW - 1);
 
-    float4* s_tring = reinterpret_cast<float4*>(s_raw);                   // [D][T]
-    float2* s_ring = reinterpret_cast<float2*>(s_tring + D * T);          // [D][NS*3*RP][T]
-    float2* s_sring = s_ring + D * NS * 3 * RP * T;                        // [D][NS][T]
-    float* s_mring = reinterpret_cast<float*>(s_sring + D * NS * T);      // [D][T]
-    float2* s_ev = reinterpret_cast<float2*>(s_mring + D * T);             // [NE2][T][G+1]
-    Op* s_ops = reinterpret_cast<Op*>(s_ev + NE2 * T * (G + 1));          // [n_ops]
+    // Per voxel slot (not per lane): the transcendentals, seeds and
+    // recorded F+[0] one lane of the voxel fetches.
+    constexpr int VPB = W * VPW;
+    constexpr int VPB4 = (VPB + 3) & ~3;
+    float2* s_ring = reinterpret_cast<float2*>(s_raw);                    // [D][NS*3][T][RP]
+    float4* s_tring = reinterpret_cast<float4*>(s_ring + D * NS * 3 * RP * T);  // [L][VPB]
+    float2* s_sring = reinterpret_cast<float2*>(s_tring + L * VPB);       // [D][NS][VPB]
+    float* s_mring = reinterpret_cast<float*>(s_sring + D * NS * VPB);    // [D][VPB4]
+    Op* s_ops = reinterpret_cast<Op*>(s_mring + D * VPB4);                 // [n_ops]
     float2* s_dir = reinterpret_cast<float2*>(s_ops + n_ops);              // [K][n_ops]
 
-    const Voxel<K> v = load_voxel<K>(a, ac);
+    const Voxel<K> v = load_voxel<K, HOT>(a, ac);
     {
         const Op* ops = a.ops + train * n_ops;
         for (int i = threadIdx.x; i < n_ops; i += T) s_ops[i] = ops[i];
-        if (a.op_dir) {
+        if (!HOT && a.op_dir) {
             const int64_t n_all = int64_t(gridDim.y) * n_ops;
             for (int i = threadIdx.x; i < K * n_ops; i += T) {
                 const int k = i / n_ops, o = i - k * n_ops;
@@ -454,15 +490,17 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
     const float* seed_row = a.seed + (active ? row : 0) * jc * a.outputs * seed_stride;
     const float* rec_col = a.traj_rec + train * a.outputs * NS * n + ac;
 
-    const int64_t tiles = (n + 31) >> 5;
-    const int64_t op_stride = int64_t(NS) * 3 * NP * 32;
+    // This warp's tile (a warp past the last voxel reads tile 0 and keeps
+    // nothing of it).
+    const int64_t n_warps = (n + VPW - 1) / VPW;
+    const int64_t op_stride = int64_t(NS) * 3 * 32 * RP;
     const float2* lane_traj =
-        a.traj + (train * tiles + (ac >> 5)) * n_ops * op_stride + (ac & 31) + q * RP * 32;
-    const unsigned ring_base = static_cast<unsigned>(__cvta_generic_to_shared(s_ring + threadIdx.x));
-    const unsigned sring_base =
-        static_cast<unsigned>(__cvta_generic_to_shared(s_sring + threadIdx.x));
-    const unsigned mring_base =
-        static_cast<unsigned>(__cvta_generic_to_shared(s_mring + threadIdx.x));
+        a.traj + (train * n_warps + (warp_global < n_warps ? warp_global : 0)) * n_ops * op_stride +
+        lane * RP;
+    const unsigned ring_base =
+        static_cast<unsigned>(__cvta_generic_to_shared(s_ring + threadIdx.x * RP));
+    const unsigned sring_base = static_cast<unsigned>(__cvta_generic_to_shared(s_sring + vslot));
+    const unsigned mring_base = static_cast<unsigned>(__cvta_generic_to_shared(s_mring + vslot));
 
     // Op o into ring slot rs: entry-state pairs of every state (zero past the
     // last pair), the seeds and recorded F+[0] (zero unless this lane
@@ -472,46 +510,49 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
         const unsigned dst_op = ring_base + unsigned(rs * NS * 3 * RP * T) * 8u;
 #pragma unroll
         for (int sp = 0; sp < NS * 3; ++sp) {
-            const float2* src = src_op + sp * NP * 32;
-#pragma unroll
-            for (int kk = 0; kk < RP; ++kk) {
-                const bool ok = q * RP + kk < NP;
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(
-                                 dst_op + unsigned((sp * RP + kk) * T) * 8u),
-                             "l"(ok ? src + kk * 32 : a.traj), "r"(ok ? 8 : 0)
+            const float2* src = src_op + sp * 32 * RP;
+            const unsigned dst = dst_op + unsigned(sp * T * RP) * 8u;
+            if constexpr (RP == 2) {
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src)
                              : "memory");
+            } else {
+#pragma unroll
+                for (int kk = 0; kk < RP; ++kk)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst + 8u * kk),
+                                 "l"(src + kk)
+                                 : "memory");
             }
         }
         const Op op = s_ops[o];
-        const bool rec = lane0 && (op.code & OP_RECORD);
-        const int64_t r = rec ? op.record : 0;
-        const unsigned sdst = sring_base + unsigned(rs * NS * T) * 8u;
-        const bool have0 = rec && seed0_row != nullptr;
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sdst),
-                     "l"(have0 ? seed0_row + r * seed_stride : a.seed), "r"(have0 ? 4 : 0)
-                     : "memory");
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
-                             sdst + unsigned((k + 1) * T) * 8u),
-                         "l"(seed_row + (k * a.outputs + r) * seed_stride), "r"(rec ? 4 : 0)
+        // Seeds and recorded F+[0]: lane 0 of each voxel slot copies them
+        // (zeros unless the voxel is live and the op records).
+        if (q == 0 && slot < VPW) {
+            const bool rec = lane0 && (op.code & OP_RECORD);
+            const int64_t r = rec ? op.record : 0;
+            const unsigned sdst = sring_base + unsigned(rs * NS * VPB) * 8u;
+            const bool have0 = rec && seed0_row != nullptr;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sdst),
+                         "l"(have0 ? seed0_row + r * seed_stride : a.seed), "r"(have0 ? 4 : 0)
                          : "memory");
 #pragma unroll
-        for (int s = 0; s < NS; ++s)
+            for (int k = 0; k < K; ++k)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
+                                 sdst + unsigned((k + 1) * VPB) * 8u),
+                             "l"(seed_row + (k * a.outputs + r) * seed_stride), "r"(rec ? 4 : 0)
+                             : "memory");
+#pragma unroll
+            for (int s = 0; s < NS; ++s)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
+                                 sdst + unsigned(s * VPB) * 8u + 4u),
+                             "l"(rec_col + (r * NS + s) * n), "r"(rec ? 4 : 0)
+                             : "memory");
+            const bool have_m = rec && a.with_m0;
             asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
-                             sdst + unsigned(s * T) * 8u + 4u),
-                         "l"(rec_col + (r * NS + s) * n), "r"(rec ? 4 : 0)
+                             mring_base + unsigned(rs * VPB4) * 4u),
+                         "l"(have_m ? seed_row + (K * a.outputs + r) * seed_stride : a.seed),
+                         "r"(have_m ? 4 : 0)
                          : "memory");
-        const bool have_m = rec && a.with_m0;
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
-                         mring_base + unsigned(rs * T) * 4u),
-                     "l"(have_m ? seed_row + (K * a.outputs + r) * seed_stride : a.seed),
-                     "r"(have_m ? 4 : 0)
-                     : "memory");
-        float si = 0.f, co = 1.f;
-        if (op_rf(op.code) == RF_ROTATE) sincosf(op.flip * v.b1, &si, &co);
-        s_tring[rs * T + threadIdx.x] =
-            make_float4(si, co, expf(-v.r1 * op.dt), expf(-v.r2 * op.dt));
+        }
     };
 
 #pragma unroll
@@ -519,26 +560,41 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
         if (n_ops - j >= 0) fetch(n_ops - j, j - 1);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
-    float2* my_ev = s_ev + threadIdx.x * (G + 1);
-    const float2* warp_ev = s_ev + warp * 32 * (G + 1);
     float2* event_out =
         a.event_partial + (train * a.warps_per_train + warp_global) * int64_t(n_ops) * NE2;
     const float2* dirs = a.op_dir ? s_dir : nullptr;
-    int use_slot = 0, fill_slot = D - 1, group = 0;
+    int use_slot = 0, fill_slot = D - 1;
     const float2 neg1 = dup(-1.f);
 
     for (int o = n_ops - 1; o >= 0; --o) {
+        if ((n_ops - 1 - o) % L == 0) {
+            // Every L ops, the transcendentals of the next L: lane q of a
+            // voxel evaluates op o - q, so one pass of the warp covers them
+            // (slot (op % L) of each voxel; the slots' last readers are done).
+            __syncwarp();
+            const int oq = o - q;
+            if (slot < VPW && oq >= 0) {
+                const Op opq = s_ops[oq];
+                float si = 0.f, co = 1.f;
+                if (op_rf(opq.code) == RF_ROTATE) sincosf(opq.flip * v.b1, &si, &co);
+                s_tring[(oq % L) * VPB + vslot] =
+                    make_float4(si, co, expf(-v.r1 * opq.dt), expf(-v.r2 * opq.dt));
+            }
+        }
+        // Orders the lanes' reads of the slot this fetch refills (used last
+        // iteration) and the transcendentals written above.
+        __syncwarp();
         if (o - (D - 1) >= 0) fetch(o - (D - 1), fill_slot);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
         fill_slot = fill_slot + 1 == D ? 0 : fill_slot + 1;
         const Op op = s_ops[o];
         const uint32_t code = op.code;
         asm volatile("cp.async.wait_group %0;\n" ::"n"(D - 1) : "memory");
-        const float4 tr = s_tring[use_slot * T + threadIdx.x];
-        const float2* ring = s_ring + use_slot * (NS * 3 * RP * T) + threadIdx.x;
-        const float2* sr = s_sring + use_slot * (NS * T) + threadIdx.x;
-        const float g_m0col = s_mring[use_slot * T + threadIdx.x];
+        const int cur = use_slot;
         use_slot = use_slot + 1 == D ? 0 : use_slot + 1;
+        const float4 tr = s_tring[(o % L) * VPB + vslot];
+        const float2* ring = s_ring + cur * (NS * 3 * RP * T) + threadIdx.x * RP;
+        const float2* sr = s_sring + cur * (NS * VPB) + vslot;
 
         // The pre-RF states: entry states relaxed and pre-shifted.
         float2 P[NS][RP], M[NS][RP], Z[NS][RP];
@@ -546,14 +602,14 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
         for (int s = 0; s < NS; ++s)
 #pragma unroll
             for (int kk = 0; kk < RP; ++kk) {
-                P[s][kk] = ring[((s * 3 + 0) * RP + kk) * T];
-                M[s][kk] = ring[((s * 3 + 1) * RP + kk) * T];
-                Z[s][kk] = ring[((s * 3 + 2) * RP + kk) * T];
+                P[s][kk] = ring[(s * 3 + 0) * T * RP + kk];
+                M[s][kk] = ring[(s * 3 + 1) * T * RP + kk];
+                Z[s][kk] = ring[(s * 3 + 2) * T * RP + kk];
             }
         float ddt[K], eps1[K], eps2[K], dal[K], dfl[K];
-        op_directions<K>(a, dirs, n_ops, o, op, v, ddt, eps1, eps2, dal, dfl);
+        op_directions<K, HOT>(a, dirs, n_ops, o, op, v, ddt, eps1, eps2, dal, dfl);
         const bool relax = (code & OP_RELAX) != 0;
-        if (relax) relax_all<RP, K>(P, M, Z, tr.z, tr.w, eps1, eps2, q);
+        if (relax) relax_all<RP, K, HOT>(P, M, Z, tr.z, tr.w, eps1, eps2, q);
         for (int s = 0; s < op_shift1(code); ++s) shift_all<RP, L, K>(P, M, q, kill, kill_r);
 
         // Reverse of the op's micro-steps after the pulse.
@@ -563,16 +619,17 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
             const float g0 = seed_sign * sr[0].x;
             const float x0 = sr[0].y;
             // The M0 derivative is F+[0] itself: its seed acts unscaled.
+            const float g_m0col = s_mring[cur * VPB4 + vslot];
             float add0 = fmaf(g0, v.m0, seed_sign * g_m0col);
             c_m0 = fmaf(g0, x0, c_m0);
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                const float gk = seed_sign * sr[(k + 1) * T].x;
-                const float tk0 = sr[(k + 1) * T].y;
-                add0 = fmaf(gk, v.dm0[k], add0);
+                const float gk = seed_sign * sr[(k + 1) * VPB].x;
+                const float tk0 = sr[(k + 1) * VPB].y;
+                if (!HOT) add0 = fmaf(gk, v.dm0[k], add0);
                 pb[k + 1][0].x = fmaf(gk, v.m0, pb[k + 1][0].x);
                 c_m0 = fmaf(gk, tk0, c_m0);
-                v_m0[k] = fmaf(gk, x0, v_m0[k]);
+                if (!HOT) v_m0[k] = fmaf(gk, x0, v_m0[k]);
             }
             pb[0][0].x += add0;
         }
@@ -614,12 +671,14 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
                     // G_k = d.ax + zb.bx; H_k = d.at + zb.bt;
                     // I_k = d.(hc w - si z) + zb.(-hs w - co z) = d.bx + zb.ex.
                     gk[k] = fma2(d, ax, fma2(zbk, bx, gk[k]));
-                    const float2 al = dup(dal[k]);
                     ga = fma2(d, at, fma2(zbk, bt, ga));
-                    ga = fma2(al, fma2(d, bx, mul2(zbk, ex)), ga);
-                    // (R'^T mu_k): P (hs d + hc zb), M -(..), Z (co d - si zb).
-                    U = fma2(al, fma2(hs, d, mul2(hc, zbk)), U);
-                    V = fma2(al, fma2(co2, d, mul2(nsi2, zbk)), V);
+                    if (!HOT || hot_dir(HOT, k) == 3) {
+                        const float2 al = dup(dal[k]);
+                        ga = fma2(al, fma2(d, bx, mul2(zbk, ex)), ga);
+                        // (R'^T mu_k): P (hs d + hc zb), M -(..), Z (co d - si zb).
+                        U = fma2(al, fma2(hs, d, mul2(hc, zbk)), U);
+                        V = fma2(al, fma2(co2, d, mul2(nsi2, zbk)), V);
+                    }
                     // mu_k <- R^T mu_k.
                     const float2 p_ = pb[k + 1][kk], m_ = mb[k + 1][kk];
                     pb[k + 1][kk] = fma2(ch, p_, fma2(sh, m_, mul2(hs, zbk)));
@@ -636,6 +695,10 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const float g = gk[k].x + gk[k].y;
+                if (HOT) {
+                    if (hot_dir(HOT, k) == 3) gf += g;
+                    continue;
+                }
                 gf = fmaf(g, v.db1[k], gf);
                 gb = fmaf(g, dfl[k], gb);
                 v_b1[k] = fmaf(g, op.flip, v_b1[k]);
@@ -657,15 +720,18 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
                 for (int k = 0; k < K; ++k) {
                     const float2 zbk = zb[k + 1][kk];
                     acc = fma2(zbk, Z[k + 1][kk], acc);
-                    vk[k] = fma2(zbk, Z[0][kk], vk[k]);
-                    nz = fma2(dup(-v.deff[k]), zbk, nz);
+                    if (!HOT) {
+                        vk[k] = fma2(zbk, Z[0][kk], vk[k]);
+                        nz = fma2(dup(-v.deff[k]), zbk, nz);
+                    }
                     zb[k + 1][kk] = mul2(zbk, f);
                 }
                 zb[0][kk] = nz;
             }
             c_inv -= acc.x + acc.y;
+            if (!HOT)
 #pragma unroll
-            for (int k = 0; k < K; ++k) v_inv[k] -= vk[k].x + vk[k].y;
+                for (int k = 0; k < K; ++k) v_inv[k] -= vk[k].x + vk[k].y;
         }
         if (relax) {
             // Q2, Q1 and C2_k, C1_k at the pre-RF point.
@@ -681,18 +747,33 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
             float dtc = 0.f;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
+                // C2_k and C1_k: a one-hot direction needs only its own.
+                const bool n2 = !HOT || hot_dir(HOT, k) == 2;
+                const bool n1 = !HOT || hot_dir(HOT, k) == 1;
                 float2 c2 = dup(0.f), c1 = dup(0.f), t2 = dup(0.f), t1 = dup(0.f);
 #pragma unroll
                 for (int kk = 0; kk < RP; ++kk) {
-                    c2 = fma2(pb[k + 1][kk], P[0][kk], fma2(mb[k + 1][kk], M[0][kk], c2));
-                    c1 = fma2(zb[k + 1][kk], Z[0][kk], c1);
+                    if (n2) c2 = fma2(pb[k + 1][kk], P[0][kk], fma2(mb[k + 1][kk], M[0][kk], c2));
+                    if (n1) c1 = fma2(zb[k + 1][kk], Z[0][kk], c1);
                     t2 = fma2(pb[k + 1][kk], P[k + 1][kk], fma2(mb[k + 1][kk], M[k + 1][kk], t2));
                     t1 = fma2(zb[k + 1][kk], Z[k + 1][kk], t1);
                 }
-                const float C2 = c2.x + c2.y;
-                const float C1 = c1.x + c1.y - (q == 0 ? zb[k + 1][0].x : 0.f);
                 Q2 += t2.x + t2.y;
                 Q1 += t1.x + t1.y;
+                const float C2 = n2 ? c2.x + c2.y : 0.f;
+                const float C1 = n1 ? c1.x + c1.y - (q == 0 ? zb[k + 1][0].x : 0.f) : 0.f;
+                if (HOT) {
+                    // r'_k = -w for the unit tangent of T1 (or T2).
+                    if (n2) {
+                        g_rd2[k] = fmaf(-op.dt, C2, g_rd2[k]);
+                        dtc = fmaf(C2, v.w2, dtc);
+                    }
+                    if (n1) {
+                        g_rd1[k] = fmaf(-op.dt, C1, g_rd1[k]);
+                        dtc = fmaf(C1, v.w1, dtc);
+                    }
+                    continue;
+                }
                 g_r2 = fmaf(-C2, ddt[k], g_r2);
                 g_r1 = fmaf(-C1, ddt[k], g_r1);
                 g_rd2[k] = fmaf(-op.dt, C2, g_rd2[k]);
@@ -716,44 +797,49 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
                     pb[k + 1][kk] = mul2(pb[k + 1][kk], E2);
                     mb[k + 1][kk] = mul2(mb[k + 1][kk], E2);
                     zb[k + 1][kk] = mul2(zb[k + 1][kk], E1);
-                    lp = fma2(dup(eps2[k]), pb[k + 1][kk], lp);
-                    lm = fma2(dup(eps2[k]), mb[k + 1][kk], lm);
-                    lz = fma2(dup(eps1[k]), zb[k + 1][kk], lz);
+                    if (!HOT || hot_dir(HOT, k) == 2) {
+                        lp = fma2(dup(eps2[k]), pb[k + 1][kk], lp);
+                        lm = fma2(dup(eps2[k]), mb[k + 1][kk], lm);
+                    }
+                    if (!HOT || hot_dir(HOT, k) == 1) lz = fma2(dup(eps1[k]), zb[k + 1][kk], lz);
                 }
                 pb[0][kk] = lp;
                 mb[0][kk] = lm;
                 zb[0][kk] = lz;
             }
         }
-        my_ev[group] = active ? make_float2(e_flip, e_dt) : dup(0.f);
-        if (NE2 == 2) my_ev[T * (G + 1) + group] = active ? make_float2(ev_flip, ev_dt) : dup(0.f);
-        if (++group == G || o == 0) {
-            __syncwarp();
+        // The op's event partials summed over the warp (a fixed butterfly;
+        // nothing on the state recursion waits for it).
+        float ev[2 * NE2] = {active ? e_flip : 0.f, active ? e_dt : 0.f};
+        if constexpr (NE2 == 2) {
+            ev[2] = active ? ev_flip : 0.f;
+            ev[3] = active ? ev_dt : 0.f;
+        }
 #pragma unroll
-            for (int e = 0; e < NE2; ++e) {
-                const float2* src = warp_ev + e * T * (G + 1);
-                for (int j = lane; j < group; j += 32) {
-                    float2 acc[4] = {dup(0.f), dup(0.f), dup(0.f), dup(0.f)};
+        for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-                    for (int l = 0; l < 32; ++l)
-                        acc[l & 3] = __fadd2_rn(acc[l & 3], src[l * (G + 1) + j]);
-                    event_out[int64_t(o + group - 1 - j) * NE2 + e] =
-                        __fadd2_rn(__fadd2_rn(acc[0], acc[1]), __fadd2_rn(acc[2], acc[3]));
-                }
-            }
-            __syncwarp();
-            group = 0;
+            for (int e = 0; e < 2 * NE2; ++e) ev[e] += __shfl_xor_sync(0xffffffffu, ev[e], off);
+        if (lane == 0) {
+#pragma unroll
+            for (int e = 0; e < NE2; ++e)
+                event_out[int64_t(o) * NE2 + e] = make_float2(ev[2 * e], ev[2 * e + 1]);
         }
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 
     // Tissue: r = 1000/T, r'_k = -1000 T'_k/T^2, summed over the voxel's lanes.
-    constexpr int NV = 5 * (1 + K);
+    // One-hot directions write the curvature only.
+    constexpr int NV = HOT ? 5 : 5 * (1 + K);
     float out[NV];
     {
         float gt1 = -v.w1 * g_r1, gt2 = -v.w2 * g_r2;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
+            if (HOT) {
+                if (hot_dir(HOT, k) == 1) gt1 = fmaf(g_rd1[k], 2.f * v.w1 / v.t1, gt1);
+                if (hot_dir(HOT, k) == 2) gt2 = fmaf(g_rd2[k], 2.f * v.w2 / v.t2, gt2);
+                continue;
+            }
             gt1 = fmaf(g_rd1[k], 2.f * v.w1 * v.dt1[k] / v.t1, gt1);
             gt2 = fmaf(g_rd2[k], 2.f * v.w2 * v.dt2[k] / v.t2, gt2);
         }
@@ -762,13 +848,15 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
         out[2] = c_m0;
         out[3] = c_b1;
         out[4] = c_inv;
+        if constexpr (!HOT) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            out[5 + 5 * k + 0] = -v.w1 * g_rd1[k];
-            out[5 + 5 * k + 1] = -v.w2 * g_rd2[k];
-            out[5 + 5 * k + 2] = v_m0[k];
-            out[5 + 5 * k + 3] = v_b1[k];
-            out[5 + 5 * k + 4] = v_inv[k];
+            for (int k = 0; k < K; ++k) {
+                out[5 + 5 * k + 0] = -v.w1 * g_rd1[k];
+                out[5 + 5 * k + 1] = -v.w2 * g_rd2[k];
+                out[5 + 5 * k + 2] = v_m0[k];
+                out[5 + 5 * k + 3] = v_b1[k];
+                out[5 + 5 * k + 4] = v_inv[k];
+            }
         }
     }
 #pragma unroll
@@ -786,32 +874,50 @@ __global__ void __launch_bounds__(32 * kSecondWarps) second_reverse_kernel(const
     }
 }
 
-template <int RP, int L, int K>
+template <int RP, int L, int K, int HOT>
 void launch_second_forward(const SecondArgs& a, dim3 grid, dim3 block, size_t smem,
                            cudaStream_t s) {
-    second_forward_kernel<RP, L, K><<<grid, block, smem, s>>>(a);
+    second_forward_kernel<RP, L, K, HOT><<<grid, block, smem, s>>>(a);
 }
 
-template <int RP, int L, int K>
+template <int RP, int L, int K, int HOT>
 void launch_second_reverse(const SecondArgs& a, dim3 grid, dim3 block, size_t smem,
                            cudaStream_t s) {
-    second_reverse_kernel<RP, L, K><<<grid, block, smem, s>>>(a);
+    second_reverse_kernel<RP, L, K, HOT><<<grid, block, smem, s>>>(a);
 }
 
-// One (orders per lane, lanes per voxel) shape for K directions.
+// One (orders per lane, lanes per voxel) shape for K directions, general
+// (hot == 0) or one-hot (the direction code of hot_dir).
 struct SecondEntry {
     int orders_per_lane;
     int lanes_per_voxel;
     int directions;
+    int hot;
     void (*forward)(const SecondArgs&, dim3, dim3, size_t, cudaStream_t);
     void (*reverse)(const SecondArgs&, dim3, dim3, size_t, cudaStream_t);
     const void* reverse_fn;
 };
 
-#define TSG_SECOND_ENTRY(R, L, K)                                                      \
-    {R, L, K, &launch_second_forward<(R) / 2, L, K>, &launch_second_reverse<(R) / 2, L, K>, \
-     reinterpret_cast<const void*>(&second_reverse_kernel<(R) / 2, L, K>)}
+#define TSG_SECOND_ENTRY(R, L, K, HOT)                                                  \
+    {R,                                                                                 \
+     L,                                                                                 \
+     K,                                                                                 \
+     HOT,                                                                               \
+     &launch_second_forward<(R) / 2, L, K, HOT>,                                        \
+     &launch_second_reverse<(R) / 2, L, K, HOT>,                                        \
+     reinterpret_cast<const void*>(&second_reverse_kernel<(R) / 2, L, K, HOT>)}
 
-const SecondEntry* second_table(int k, int* count);
+// The shapes instantiated per direction set: general directions take every
+// shape, one-hot sets the ones measured useful.
+#define TSG_SECOND_SHAPES_HOT(K, HOT)                                                     \
+    TSG_SECOND_ENTRY(2, 4, K, HOT), TSG_SECOND_ENTRY(2, 5, K, HOT),                       \
+        TSG_SECOND_ENTRY(2, 8, K, HOT), TSG_SECOND_ENTRY(2, 10, K, HOT),                  \
+        TSG_SECOND_ENTRY(2, 16, K, HOT), TSG_SECOND_ENTRY(2, 32, K, HOT),                 \
+        TSG_SECOND_ENTRY(4, 1, K, HOT), TSG_SECOND_ENTRY(4, 2, K, HOT),                   \
+        TSG_SECOND_ENTRY(4, 4, K, HOT), TSG_SECOND_ENTRY(4, 5, K, HOT),                   \
+        TSG_SECOND_ENTRY(4, 8, K, HOT)
+
+// Every table of one translation unit.
+const SecondEntry* second_table(int k, int hot, int* count);
 
 }  // namespace tsg

@@ -1,5 +1,5 @@
-// Second-order kernels for 2 direction(s) at once (epg_second.cuh), one
-// translation unit per direction count so they compile in parallel.
+// Second-order kernels for 2 general direction(s) at once (epg_second.cuh);
+// one translation unit per table so they compile in parallel.
 #include "epg_second.cuh"
 
 namespace tsg {
@@ -8,9 +8,15 @@ extern const SecondEntry kSecondK2[];
 extern const int kSecondK2Count;
 
 const SecondEntry kSecondK2[] = {
-    TSG_SECOND_ENTRY(4, 1, 2), TSG_SECOND_ENTRY(4, 2, 2), TSG_SECOND_ENTRY(4, 3, 2),
-    TSG_SECOND_ENTRY(4, 4, 2), TSG_SECOND_ENTRY(4, 5, 2), TSG_SECOND_ENTRY(4, 8, 2),
-    TSG_SECOND_ENTRY(4, 16, 2),
+    TSG_SECOND_ENTRY(4, 1, 2, 0),
+    TSG_SECOND_ENTRY(4, 2, 2, 0),
+    TSG_SECOND_ENTRY(4, 4, 2, 0),
+    TSG_SECOND_ENTRY(4, 5, 2, 0),
+    TSG_SECOND_ENTRY(4, 8, 2, 0),
+    TSG_SECOND_ENTRY(2, 5, 2, 0),
+    TSG_SECOND_ENTRY(2, 10, 2, 0),
+    TSG_SECOND_ENTRY(2, 16, 2, 0),
+    TSG_SECOND_ENTRY(2, 32, 2, 0),
 };
 const int kSecondK2Count = int(sizeof(kSecondK2) / sizeof(kSecondK2[0]));
 

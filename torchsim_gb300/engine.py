@@ -480,6 +480,67 @@ def second_reverse(program: Program, tissue: TissueMaps, states: int,
 
 # Public property name -> its key in a direction; M0 is the free column.
 DIRECTION_OF = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1", "inv_efficiency": "inversion"}
+# The one-hot direction sets of the design sweeps, in their column order.
+DESIGN_BITS = {"T1": _native.TANGENT_T1, "T2": _native.TANGENT_T2, "B1": _native.TANGENT_B1}
+
+
+def design_plan(program: Program, voxels: int, states: int, mask: int,
+                launch=None) -> tuple[int, int]:
+    """(trajectory bytes, workspace bytes) of the design sweeps."""
+    tb = ctypes.c_int64()
+    wb = ctypes.c_int64()
+    _native.check(_native.library().tsg_epg_design_plan(
+        program.handle, voxels, states, int(mask), _native.launch_shape(launch), ctypes.byref(tb),
+        ctypes.byref(wb)))
+    return tb.value, wb.value
+
+
+def design_forward(program: Program, tissue: TissueMaps, states: int, mask: int, *,
+                   with_m0: bool = False, trajectory: torch.Tensor | None = None, launch=None):
+    """Signal and its derivatives along the unit tangents of the properties in
+    ``mask`` (``TANGENT_T1 | T2 | B1``, columns in that order; with
+    ``with_m0`` a last M0 column) in ONE pass storing the trajectory.
+    Returns ``(signal, derivatives, trajectory)`` (complex64, as
+    :func:`second_forward`)."""
+    k = bin(int(mask) & 7).count("1")
+    rows = program.trains * tissue.voxels
+    device = tissue.t1.device
+    tb, _ = design_plan(program, tissue.voxels, states, mask, launch)
+    if trajectory is None or trajectory.numel() < tb:
+        trajectory = torch.empty(max(tb, 4), dtype=torch.uint8, device=device)
+    sig = torch.empty((rows, program.outputs), dtype=torch.complex64, device=device)
+    jac = torch.empty((rows, k + int(with_m0), program.outputs), dtype=torch.complex64,
+                      device=device)
+    t = tissue.struct()
+    _native.check(_native.library().tsg_epg_design_forward(
+        program.handle, ctypes.byref(t), tissue.voxels, states, int(mask), int(with_m0),
+        _native.LAYOUT_COMPLEX_IJ, sig.data_ptr(), None, jac.data_ptr(), None,
+        trajectory.data_ptr(), _native.launch_shape(launch), _stream()))
+    return sig, jac, trajectory
+
+
+def design_reverse(program: Program, tissue: TissueMaps, states: int, mask: int,
+                   seed_derivatives: torch.Tensor, trajectory: torch.Tensor,
+                   workspace: torch.Tensor | None = None, *,
+                   seed_signal: torch.Tensor | None = None, with_m0: bool = False,
+                   curvature: dict[str, torch.Tensor] | None = None, launch=None) -> None:
+    """Reverse sweep of :func:`design_forward`: adds the gradient of
+    ``<seed_signal, s> + sum_k <seed_derivatives[:, k], J e_k>`` with respect
+    to the inputs into ``curvature`` (keyed as :data:`GRAD_NAMES`)."""
+    _, wb = design_plan(program, tissue.voxels, states, mask, launch)
+    if workspace is None or workspace.numel() < wb:
+        workspace = torch.empty(max(wb, 4), dtype=torch.uint8, device=trajectory.device)
+    seed_derivatives = seed_derivatives.to(torch.complex64).contiguous()
+    if seed_signal is not None:
+        seed_signal = seed_signal.to(torch.complex64).contiguous()
+    c = _native.Gradients(*[curvature[n].data_ptr() if curvature and curvature.get(n) is not None
+                            else None for n in GRAD_NAMES])
+    t = tissue.struct()
+    _native.check(_native.library().tsg_epg_design_reverse(
+        program.handle, ctypes.byref(t), tissue.voxels, states, int(mask), int(with_m0),
+        None if seed_signal is None else seed_signal.data_ptr(), seed_derivatives.data_ptr(),
+        _native.LAYOUT_COMPLEX_IJ, trajectory.data_ptr(), ctypes.byref(c), workspace.data_ptr(),
+        workspace.numel(), _native.launch_shape(launch), _stream()))
 
 
 class JacobianFunction(torch.autograd.Function):
@@ -499,23 +560,34 @@ class JacobianFunction(torch.autograd.Function):
         tissue = TissueMaps(t1.detach(), t2.detach(), None if m0 is None else m0.detach(),
                             None if b1 is None else b1.detach(),
                             None if inv is None else inv.detach())
-        ones = torch.ones(tissue.voxels, dtype=torch.float32, device=t1.device)
         stateful = [n for n in names if n != "M0"]
         if not stateful or len(stateful) > MAX_SECOND_DIRECTIONS:
             raise NotImplementedError(
                 "a differentiable Jacobian takes one to three of T1, T2, B1, inv_efficiency "
                 "(plus M0)")
-        directions = [{DIRECTION_OF[n]: ones} for n in stateful]
         with_m0 = "M0" in names
-        sig, jac, traj, ws = second_forward(program, tissue, states, directions, with_m0=with_m0,
+        ctx.mask = 0
+        ctx.directions = None
+        if all(n in DESIGN_BITS for n in stateful):
+            # Unit tangents of T1, T2, B1: the design sweeps, columns in that
+            # order.
+            stateful = [n for n in DESIGN_BITS if n in stateful]
+            ctx.mask = sum(DESIGN_BITS[n] for n in stateful)
+            sig, jac, traj = design_forward(program, tissue, states, ctx.mask, with_m0=with_m0,
                                             launch=launch)
+            ws = torch.empty(0, dtype=torch.uint8, device=t1.device)
+        else:
+            ones = torch.ones(tissue.voxels, dtype=torch.float32, device=t1.device)
+            ctx.directions = [{DIRECTION_OF[n]: ones} for n in stateful]
+            ctx.ones = ones
+            sig, jac, traj, ws = second_forward(program, tissue, states, ctx.directions,
+                                                with_m0=with_m0, launch=launch)
         # Columns in the caller's order.
         order = [stateful.index(n) if n != "M0" else len(stateful) for n in names]
         if order != list(range(len(names))):
             jac = jac[:, order]
         ctx.program, ctx.states, ctx.launch = program, states, launch
-        ctx.tissue, ctx.directions, ctx.with_m0, ctx.order = tissue, directions, with_m0, order
-        ctx.ones = ones
+        ctx.tissue, ctx.with_m0, ctx.order = tissue, with_m0, order
         ctx.save_for_backward(traj, ws)
         ctx.present = (m0 is not None, b1 is not None, inv is not None)
         return sig, jac
@@ -544,9 +616,14 @@ class JacobianFunction(torch.autograd.Function):
             curvature["flip_rad"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
         if need[10]:
             curvature["duration_s"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
-        second_reverse(program, tissue, ctx.states, ctx.directions, seed, traj, ws,
-                       seed_signal=grad_sig, with_m0=ctx.with_m0, curvature=curvature,
-                       launch=ctx.launch)
+        if ctx.mask:
+            design_reverse(program, tissue, ctx.states, ctx.mask, seed, traj,
+                           seed_signal=grad_sig, with_m0=ctx.with_m0, curvature=curvature,
+                           launch=ctx.launch)
+        else:
+            second_reverse(program, tissue, ctx.states, ctx.directions, seed, traj, ws,
+                           seed_signal=grad_sig, with_m0=ctx.with_m0, curvature=curvature,
+                           launch=ctx.launch)
         out = [None, None, None, None]
         out += [curvature.get(n) for n in names]
         out += [curvature.get("flip_rad"), curvature.get("duration_s")]
