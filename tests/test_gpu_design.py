@@ -40,11 +40,25 @@ def test_mrf_design_fits_a_target_inside_its_limits(cuda):
     assert float(tr.min()) >= 8.0 and float(tr.max()) <= 15.0
 
 
-def test_jacobian_of_a_design_variable_is_refused(cuda):
-    from torchsim_gb300 import mrf_sim
+def test_a_cramer_rao_design_lowers_its_bound(cuda):
+    """A design cost that differentiates a Jacobian (the Cramer-Rao bound of
+    T1 and T2, relative to their squares) backs through the second-order
+    sweep; minimising it over the flip angles lowers the bound and keeps the
+    limits (the reference's optim/_design.py with crlb)."""
+    from torchsim_gb300 import Bounded, SequenceDesign, crlb, mrf_sim
 
-    flip = torch.full((8,), 20.0, device=cuda, requires_grad=True)
-    T1 = torch.full((4,), 800.0, device=cuda)
-    T2 = torch.full((4,), 60.0, device=cuda)
-    with pytest.raises(NotImplementedError):
-        mrf_sim(flip, 10.0, T1, T2, diff=("T1", "T2"))
+    T1 = torch.tensor([800.0, 1300.0, 400.0, 2000.0], device=cuda)
+    T2 = torch.tensor([60.0, 110.0, 40.0, 150.0], device=cuda)
+    scale = torch.stack((T1, T2), dim=-1)
+
+    def cost(flip):
+        _, jac = mrf_sim(flip, 12.0, T1, T2, diff=("T1", "T2"), states=12)
+        return (crlb(jac) / scale.square()).sum()
+
+    design = SequenceDesign(cost, flip=Bounded(torch.full((24,), 30.0, device=cuda), 5.0, 70.0))
+    result = design.minimize(iterations=30, learning_rate=0.1)
+    loss = result.loss.cpu().numpy()
+    assert np.all(np.isfinite(loss))
+    assert loss[-1] < 0.8 * loss[0]
+    flip = result.parameters["flip"]
+    assert float(flip.min()) >= 5.0 and float(flip.max()) <= 70.0

@@ -199,10 +199,12 @@ int run_adjoint(const tsg_program* prog, const tsg_tissue* tissue, int64_t atoms
     plan.entry->launch(a, dim3(unsigned(plan.blocks), unsigned(prog->host.trains)),
                        dim3(32 * plan.warps), plan.smem, stream);
     TSG_CUDA(cudaGetLastError());
-    const int64_t n_ev = ops * prog->host.trains;
-    reduce_event_gradients<<<unsigned((n_ev + 127) / 128), 128, 0, stream>>>(
-        a.event_partial, plan.warps_per_train, ops, prog->host.trains, prog->host.events,
-        prog->d_src, grads ? grads->flip_rad : nullptr, grads ? grads->duration_s : nullptr);
+    if (grads && (grads->flip_rad || grads->duration_s)) {
+        reduce_event_gradients<<<dim3(unsigned(ops), unsigned(prog->host.trains)),
+                                 kEventReduceThreads, 0, stream>>>(
+            a.event_partial, plan.warps_per_train, ops, prog->host.trains, prog->host.events,
+            prog->d_src, grads->flip_rad, grads->duration_s);
+    }
     TSG_CUDA(cudaGetLastError());
     reduce_tissue_gradients<<<unsigned((atoms + 127) / 128), 128, 0, stream>>>(
         a.tissue_partial, atoms, prog->host.trains, grads ? grads->t1_ms : nullptr,

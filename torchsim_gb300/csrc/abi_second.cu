@@ -76,37 +76,53 @@ __global__ void gather_second_directions(const OpSource* src, int64_t ops, int64
     out[i] = make_float2(a, b);
 }
 
-// Sums the per-warp event partials in warp order and scatters them to the
-// events the ops came from (adding): curvature into curve_*, with two pairs
-// also the values into value_*.
-__global__ void reduce_second_events(const float2* partial, int64_t warps, int64_t n_ops,
-                                     int64_t trains, int64_t events, int pairs,
-                                     const OpSource* src, float* curve_flip, float* curve_dt,
-                                     float* value_flip, float* value_dt) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n_ops * trains) return;
-    const int64_t t = i / n_ops;
-    const int64_t op = i % n_ops;
-    float2 c = make_float2(0.f, 0.f), v = make_float2(0.f, 0.f);
+// Sums the per-warp event partials and scatters them to the events the ops
+// came from (adding): curvature into curve_*, with two pairs also the values
+// into value_*. One block per (op, train): each thread sums a fixed stride of
+// warps, then a fixed tree over the threads (deterministic).
+__global__ void __launch_bounds__(kEventReduceThreads)
+    reduce_second_events(const float2* partial, int64_t warps, int64_t n_ops, int64_t trains,
+                         int64_t events, int pairs, const OpSource* src, float* curve_flip,
+                         float* curve_dt, float* value_flip, float* value_dt) {
+    __shared__ float4 s_sum[kEventReduceThreads];
+    const int64_t op = blockIdx.x;
+    const int64_t t = blockIdx.y;
     const float2* p = partial + (t * warps * n_ops + op) * pairs;
-    for (int64_t w = 0; w < warps; ++w) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t w = threadIdx.x; w < warps; w += kEventReduceThreads) {
         const float2 x = p[w * n_ops * pairs];
-        c.x += x.x;
-        c.y += x.y;
+        acc.x += x.x;
+        acc.y += x.y;
         if (pairs == 2) {
             const float2 y = p[w * n_ops * pairs + 1];
-            v.x += y.x;
-            v.y += y.y;
+            acc.z += y.x;
+            acc.w += y.y;
         }
     }
-    const OpSource s = src[i];
-    if (s.rf_event >= 0) {
-        if (curve_flip) curve_flip[t * events + s.rf_event] += c.x;
-        if (value_flip) value_flip[t * events + s.rf_event] += v.x;
+    s_sum[threadIdx.x] = acc;
+    __syncthreads();
+    for (int half = kEventReduceThreads / 2; half > 0; half >>= 1) {
+        if (threadIdx.x < half) {
+            float4& d = s_sum[threadIdx.x];
+            const float4 e = s_sum[threadIdx.x + half];
+            d.x += e.x;
+            d.y += e.y;
+            d.z += e.z;
+            d.w += e.w;
+        }
+        __syncthreads();
     }
-    if (s.dt_event >= 0) {
-        if (curve_dt) curve_dt[t * events + s.dt_event] += c.y;
-        if (value_dt) value_dt[t * events + s.dt_event] += v.y;
+    if (threadIdx.x == 0) {
+        const float4 c = s_sum[0];
+        const OpSource s = src[t * n_ops + op];
+        if (s.rf_event >= 0) {
+            if (curve_flip) curve_flip[t * events + s.rf_event] += c.x;
+            if (value_flip) value_flip[t * events + s.rf_event] += c.z;
+        }
+        if (s.dt_event >= 0) {
+            if (curve_dt) curve_dt[t * events + s.dt_event] += c.y;
+            if (value_dt) value_dt[t * events + s.dt_event] += c.w;
+        }
     }
 }
 
@@ -314,9 +330,9 @@ int run_reverse(const tsg_program* program, const SecondPlan& plan, SecondArgs a
                         dim3(32 * kSecondWarps), plan.smem, s);
     TSG_CUDA(cudaGetLastError());
     const int64_t ops = program->host.ops;
-    const int64_t n_ev = ops * program->host.trains;
     const int pairs = event_pairs(k, hot);
-    reduce_second_events<<<unsigned((n_ev + 127) / 128), 128, 0, s>>>(
+    reduce_second_events<<<dim3(unsigned(ops), unsigned(program->host.trains)),
+                           kEventReduceThreads, 0, s>>>(
         a.event_partial, plan.warps_per_train, ops, program->host.trains, program->host.events,
         pairs, program->d_src, curvature ? curvature->flip_rad : nullptr,
         curvature ? curvature->duration_s : nullptr,

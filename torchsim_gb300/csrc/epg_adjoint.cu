@@ -28,25 +28,38 @@ const AdjointEntry* adjoint_table(int warps, bool trajectory, int* count) {
     return nullptr;
 }
 
-// Sums the per-warp event partials in warp order and scatters them to the
-// events the ops came from; adds into the outputs.
-__global__ void reduce_event_gradients(const float2* partial, int64_t warps, int64_t n_ops,
-                                       int64_t trains, int64_t events, const OpSource* src,
-                                       float* grad_flip, float* grad_duration) {
-    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n_ops * trains) return;
-    const int64_t t = i / n_ops;
-    const int64_t op = i % n_ops;
-    float f = 0.f, d = 0.f;
+// Sums the per-warp event partials and scatters them to the events the ops
+// came from; adds into the outputs. One block per (op, train): each thread
+// sums a fixed stride of warps, then a fixed tree over the threads, so the
+// sum does not depend on scheduling.
+__global__ void __launch_bounds__(kEventReduceThreads)
+    reduce_event_gradients(const float2* partial, int64_t warps, int64_t n_ops, int64_t trains,
+                           int64_t events, const OpSource* src, float* grad_flip,
+                           float* grad_duration) {
+    __shared__ float2 s_sum[kEventReduceThreads];
+    const int64_t op = blockIdx.x;
+    const int64_t t = blockIdx.y;
     const float2* p = partial + t * warps * n_ops + op;
-    for (int64_t w = 0; w < warps; ++w) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int64_t w = threadIdx.x; w < warps; w += kEventReduceThreads) {
         const float2 v = p[w * n_ops];
-        f += v.x;
-        d += v.y;
+        acc.x += v.x;
+        acc.y += v.y;
     }
-    const OpSource s = src[i];
-    if (grad_flip && s.rf_event >= 0) grad_flip[t * events + s.rf_event] += f;
-    if (grad_duration && s.dt_event >= 0) grad_duration[t * events + s.dt_event] += d;
+    s_sum[threadIdx.x] = acc;
+    __syncthreads();
+    for (int half = kEventReduceThreads / 2; half > 0; half >>= 1) {
+        if (threadIdx.x < half) {
+            s_sum[threadIdx.x].x += s_sum[threadIdx.x + half].x;
+            s_sum[threadIdx.x].y += s_sum[threadIdx.x + half].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const OpSource s = src[t * n_ops + op];
+        if (grad_flip && s.rf_event >= 0) grad_flip[t * events + s.rf_event] += s_sum[0].x;
+        if (grad_duration && s.dt_event >= 0) grad_duration[t * events + s.dt_event] += s_sum[0].y;
+    }
 }
 
 // Sums the per-train tissue partials in train order; adds into the outputs.

@@ -220,6 +220,8 @@ const AdjointEntry* adjoint_table(int warps, bool trajectory, int* count);
 // Trajectory-mode reverse sweep: ops per event-gradient reduction, ops in
 // flight per lane (ring slots in shared memory), and the longest program it
 // keeps in shared memory.
+// Threads of the event-gradient reductions (one block per op and train).
+constexpr int kEventReduceThreads = 128;
 constexpr int kTrajChunk = 32;
 constexpr int kTrajRing = 4;
 constexpr int kTrajMaxOps = 2048;

@@ -9,11 +9,14 @@ the optimiser moves an unconstrained variable ``u`` and the cost sees
 ``lower + (upper - lower) * sigmoid(u)`` (``optim/_design.py:263-278``).
 
 The gradient of a cost that simulates through :func:`torchsim_gb300.mrf_sim`
-or a simulator's ``simulate`` comes from the checkpointed adjoint kernel
-(``engine.EpgFunction``): one forward sweep that stores a checkpoint every few
-pulses, one reverse sweep. Costs that differentiate a Jacobian (a Cramer-Rao
-bound from :func:`crlb`) need second-order derivatives, which this package
-does not build; such a cost raises ``NotImplementedError`` in ``jacobian``.
+or a simulator's ``simulate`` comes from the adjoint kernel
+(``engine.EpgFunction``): one forward sweep that stores the trajectory (or a
+checkpoint every few pulses), one reverse sweep. A cost that differentiates a
+Jacobian (a Cramer-Rao bound from :func:`crlb`) backs through the
+second-order sweep (``engine.JacobianFunction``): one forward of the signal
+and its tangents that stores their trajectory, one reverse sweep over all the
+Jacobian's columns, where the reference pays one forward-over-reverse pass per
+column (``sequence/_accelerators.py:1780-1800``).
 """
 
 from __future__ import annotations
