@@ -24,6 +24,7 @@
  *                         (dual arithmetic 346-365, 407-418, 768-775, 6964-6967)
  *   run_forward_complex   simulate_range<INSTANT, ONE>     4216-4566
  *                         with shift 2164-2174, rotate 2176-2208
+ *   run_adjoint_complex   simulate_vjp_range<INSTANT, ONE> 4840-5985
  * Action bits are the packed action word (_epg_cpu.cpp:36-41,
  * sequence/_accelerators.py:77-84). Event kinds: 0 wait, 1 RF, 2 ADC
  * (sequence/_description.py:31-36). The work range enumerates (train, atom)
@@ -739,6 +740,82 @@ static void rotate_complex(cplx* plus, cplx* minus, cplx* lon, int64_t states, R
     }
 }
 
+/* Transpose of shift_complex: F+ cotangents move one order down, F-
+ * cotangents one order up, and F+[0] = conj(F-[0]) returns conj(pb[0]) to
+ * the F-[1] that became F-[0]. */
+static void shift_complex_adjoint(cplx* pb, cplx* mb, int64_t states) {
+    const cplx carry = cconj(pb[0]);
+    const cplx zero = {LIT(0.0), LIT(0.0)};
+    for (int64_t s = 0; s + 1 < states; ++s) pb[s] = pb[s + 1];
+    pb[states - 1] = zero;
+    for (int64_t s = states - 1; s > 0; --s) mb[s] = mb[s - 1];
+    mb[0] = zero;
+    if (states > 1) mb[1] = cadd(mb[1], carry);
+}
+
+/* Transpose (conjugate) of rotate_complex applied to the cotangents, and the
+ * gradients Re(conj(y_bar) dT/dalpha x), Re(conj(y_bar) dT/dphi x) added
+ * into ga, gp, with x the pre-pulse state (p, m, z). */
+static void rotate_complex_adjoint(cplx* pb, cplx* mb, cplx* zb, const cplx* p, const cplx* m,
+                                   const cplx* z, int64_t states, REAL alpha, REAL phi, REAL* ga,
+                                   REAL* gp) {
+    const REAL co = COS(alpha), si = SIN(alpha);
+    const REAL chs = LIT(0.5) * (LIT(1.0) + co), shs = LIT(0.5) * (LIT(1.0) - co);
+    const cplx one = cpolar(LIT(1.0), phi), two = cmul(one, one);
+    const cplx i1 = {LIT(0.0), LIT(1.0)};
+    /* T and dT/dalpha, dT/dphi, entry by entry. */
+    cplx t[3][3], ta[3][3], tp[3][3];
+    t[0][0] = (cplx){chs, LIT(0.0)};
+    t[0][1] = cscale(shs, two);
+    t[0][2] = cmul((cplx){LIT(0.0), -si}, one);
+    t[1][0] = cconj(t[0][1]);
+    t[1][1] = t[0][0];
+    t[1][2] = cmul((cplx){LIT(0.0), si}, cconj(one));
+    t[2][0] = cmul((cplx){LIT(0.0), -LIT(0.5) * si}, cconj(one));
+    t[2][1] = cmul((cplx){LIT(0.0), LIT(0.5) * si}, one);
+    t[2][2] = (cplx){co, LIT(0.0)};
+    ta[0][0] = (cplx){-LIT(0.5) * si, LIT(0.0)};
+    ta[0][1] = cscale(LIT(0.5) * si, two);
+    ta[0][2] = cmul((cplx){LIT(0.0), -co}, one);
+    ta[1][0] = cconj(ta[0][1]);
+    ta[1][1] = ta[0][0];
+    ta[1][2] = cmul((cplx){LIT(0.0), co}, cconj(one));
+    ta[2][0] = cmul((cplx){LIT(0.0), -LIT(0.5) * co}, cconj(one));
+    ta[2][1] = cmul((cplx){LIT(0.0), LIT(0.5) * co}, one);
+    ta[2][2] = (cplx){-si, LIT(0.0)};
+    /* d/dphi: one -> i one, two -> 2i two, conj(one) -> -i conj(one). */
+    tp[0][0] = (cplx){LIT(0.0), LIT(0.0)};
+    tp[0][1] = cmul(cscale(LIT(2.0), i1), t[0][1]);
+    tp[0][2] = cmul(i1, t[0][2]);
+    tp[1][0] = cmul(cscale(-LIT(2.0), i1), t[1][0]);
+    tp[1][1] = tp[0][0];
+    tp[1][2] = cmul(cscale(-LIT(1.0), i1), t[1][2]);
+    tp[2][0] = cmul(cscale(-LIT(1.0), i1), t[2][0]);
+    tp[2][1] = cmul(i1, t[2][1]);
+    tp[2][2] = tp[0][0];
+    for (int64_t s = 0; s < states; ++s) {
+        const cplx x[3] = {p[s], m[s], z[s]};
+        const cplx y[3] = {pb[s], mb[s], zb[s]};
+        for (int r = 0; r < 3; ++r) {
+            cplx da = {LIT(0.0), LIT(0.0)}, dp = {LIT(0.0), LIT(0.0)};
+            for (int k = 0; k < 3; ++k) {
+                da = cadd(da, cmul(ta[r][k], x[k]));
+                dp = cadd(dp, cmul(tp[r][k], x[k]));
+            }
+            *ga += y[r].re * da.re + y[r].im * da.im;
+            *gp += y[r].re * dp.re + y[r].im * dp.im;
+        }
+        cplx nx[3];
+        for (int k = 0; k < 3; ++k) {
+            nx[k] = (cplx){LIT(0.0), LIT(0.0)};
+            for (int r = 0; r < 3; ++r) nx[k] = cadd(nx[k], cmul(cconj(t[r][k]), y[r]));
+        }
+        pb[s] = nx[0];
+        mb[s] = nx[1];
+        zb[s] = nx[2];
+    }
+}
+
 /* Complex forward over work items [begin, end): both output planes are the
  * recorded m0 * F+[0] demodulated by the receiver phase. */
 static void run_forward_complex(const oracle_case* c, const oracle_offaxis* o, int64_t begin,
@@ -811,6 +888,160 @@ static void run_forward_complex(const oracle_case* c, const oracle_offaxis* o, i
         }
     }
     free(plus);
+}
+
+/* First-order adjoint of the complex path (the single-pool instant-RF case
+ * of simulate_vjp_range, _epg_cpu.cpp:4840-5985), restated in this file's
+ * complex arithmetic: the entry state of every event is recorded, then the
+ * events are swept backwards replaying each event's stages from its entry
+ * state. The seed is complex (real plane + i imaginary plane): the loss is
+ * sum Re(conj(seed) * sample). For y = a x the cotangent is x_bar = conj(a)
+ * y_bar; a parameter's gradient is Re(conj(y_bar) * (da/dp) x).
+ * Gradients add into g[10]: per atom t1, t2, m0, b1, inversion, b1 phase,
+ * b0; per (train, event) flip, duration, phase. */
+static void run_adjoint_complex(const oracle_case* c, const oracle_offaxis* o,
+                                const float* seed_real, const float* seed_imag, int64_t begin,
+                                int64_t end, REAL* const* g) {
+    const int64_t S = c->state_count;
+    const int64_t E = c->event_count;
+    const cplx zero = {LIT(0.0), LIT(0.0)};
+    cplx* traj = (cplx*)malloc(sizeof(cplx) * (size_t)(E > 0 ? E : 1) * (size_t)(3 * S));
+    cplx* buf = (cplx*)calloc((size_t)(9 * S), sizeof(cplx));
+    cplx *plus = buf, *minus = buf + S, *lon = buf + 2 * S;
+    cplx *pb = buf + 3 * S, *mb = buf + 4 * S, *zb = buf + 5 * S;
+    cplx *ps = buf + 6 * S, *ms = buf + 7 * S, *zs = buf + 8 * S;
+#if defined(REAL_IS_FLOAT)
+    const REAL pi = 3.14159265358979323846F;
+#else
+    const REAL pi = 3.14159265358979323846;
+#endif
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / c->atom_count;
+        const int64_t atom = work % c->atom_count;
+        const int64_t ebase = train * E;
+        const float* duration = c->duration_s + ebase;
+        const float* flip = c->flip_rad + ebase;
+        const float* phase = o->phase_rad ? o->phase_rad + ebase : NULL;
+        const int64_t out_base = (train * c->atom_count + atom) * c->output_count;
+        const REAL t1 = (REAL)c->t1_ms[atom];
+        const REAL t2 = (REAL)c->t2_ms[atom];
+        const REAL r1 = LIT(1000.0) / t1;
+        const REAL r2 = LIT(1000.0) / t2;
+        const REAL m0 = tissue(c->m0, atom, LIT(1.0));
+        const REAL b1 = tissue(c->b1, atom, LIT(1.0));
+        const REAL eff = tissue(c->inversion, atom, LIT(1.0));
+        const REAL b1_phase = tissue(o->b1_phase_rad, atom, LIT(0.0));
+        const REAL b0 = tissue(o->b0_hz, atom, LIT(0.0));
+        for (int64_t s = 0; s < 9 * S; ++s) buf[s] = zero;
+        lon[0].re = LIT(1.0);
+        /* The forward, as run_forward_complex, recording entry states. */
+        for (int64_t e = 0; e < E; ++e) {
+            memcpy(traj + e * 3 * S, plus, sizeof(cplx) * (size_t)(3 * S));
+            const REAL dt = (REAL)duration[e];
+            const REAL e1 = EXP(-r1 * dt);
+            const cplx tr = cpolar(EXP(-r2 * dt), -LIT(2.0) * pi * b0 * dt);
+            for (int64_t s = 0; s < S; ++s) {
+                plus[s] = cmul(plus[s], tr);
+                minus[s] = cmul(minus[s], cconj(tr));
+                lon[s] = cscale(e1, lon[s]);
+            }
+            lon[0].re += LIT(1.0) - e1;
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) shift_complex(plus, minus, S);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    for (int64_t s = 0; s < S; ++s) lon[s] = cscale(-eff, lon[s]);
+                } else {
+                    const REAL phi = (phase ? (REAL)phase[e] : LIT(0.0)) + b1_phase;
+                    rotate_complex(plus, minus, lon, S, (REAL)flip[e] * b1, phi);
+                }
+            }
+            if (a & A_POST_SHIFT) shift_complex(plus, minus, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) plus[s] = minus[s] = zero;
+            } else if (a & A_SHIFT_AFTER) {
+                shift_complex(plus, minus, S);
+            }
+        }
+        for (int64_t s = 0; s < 3 * S; ++s) pb[s] = zero;
+        REAL gt1 = 0, gt2 = 0, gm0 = 0, gb1 = 0, ginv = 0, gb1p = 0, gb0 = 0;
+        for (int64_t e = E - 1; e >= 0; --e) {
+            const cplx* slot = traj + e * 3 * S;
+            const uint8_t a = c->action[e];
+            const REAL dt = (REAL)duration[e];
+            const REAL e1 = EXP(-r1 * dt);
+            const cplx tr = cpolar(EXP(-r2 * dt), -LIT(2.0) * pi * b0 * dt);
+            for (int64_t s = 0; s < S; ++s) {
+                ps[s] = cmul(slot[s], tr);
+                ms[s] = cmul(slot[S + s], cconj(tr));
+                zs[s] = cscale(e1, slot[2 * S + s]);
+            }
+            zs[0].re += LIT(1.0) - e1;
+            if (a & A_PRE_SHIFT) shift_complex(ps, ms, S);
+            if (a & A_SPOIL_AFTER) {
+                for (int64_t s = 0; s < S; ++s) pb[s] = mb[s] = zero;
+            } else if (a & A_SHIFT_AFTER) {
+                shift_complex_adjoint(pb, mb, S);
+            }
+            if (a & A_POST_SHIFT) shift_complex_adjoint(pb, mb, S);
+            const REAL ph = phase ? (REAL)phase[e] : LIT(0.0);
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    for (int64_t s = 0; s < S; ++s) {
+                        ginv -= zb[s].re * zs[s].re + zb[s].im * zs[s].im;
+                        zb[s] = cscale(-eff, zb[s]);
+                    }
+                } else {
+                    REAL ga = 0, gp = 0;
+                    rotate_complex_adjoint(pb, mb, zb, ps, ms, zs, S, (REAL)flip[e] * b1,
+                                           ph + b1_phase, &ga, &gp);
+                    g[7][ebase + e] += ga * b1;
+                    gb1 += ga * (REAL)flip[e];
+                    g[9][ebase + e] += gp;
+                    gb1p += gp;
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                const int64_t idx = out_base + c->output_index[e];
+                const cplx sd = {(REAL)seed_real[idx], (REAL)seed_imag[idx]};
+                const cplx d = cpolar(LIT(1.0), -ph);
+                const cplx v = cmul(cscale(m0, ps[0]), d);
+                const cplx fd = cmul(ps[0], d);
+                gm0 += sd.re * fd.re + sd.im * fd.im;
+                /* dv/dph = -i v. */
+                g[9][ebase + e] += sd.re * v.im - sd.im * v.re;
+                pb[0] = cadd(pb[0], cscale(m0, cmul(cconj(d), sd)));
+            }
+            if (a & A_PRE_SHIFT) shift_complex_adjoint(pb, mb, S);
+            /* Relaxation and turn: y = T x on F+, conj(T) x on F-, e1 x + (1 - e1)
+             * on Z. With A+ = sum conj(pb) slot+, A- = sum conj(mb) slot-:
+             * dL/dlog(e2) = Re(A+ T) + Re(A- conj T), dL/doff = -Im(A+ T) +
+             * Im(A- conj T), dL/dlog(e1) = e1 (Re sum conj(zb) slotz - Re zb0). */
+            cplx ap = zero, am = zero;
+            REAL az = LIT(0.0);
+            for (int64_t s = 0; s < S; ++s) {
+                ap = cadd(ap, cmul(cconj(pb[s]), slot[s]));
+                am = cadd(am, cmul(cconj(mb[s]), slot[S + s]));
+                az += zb[s].re * slot[2 * S + s].re + zb[s].im * slot[2 * S + s].im;
+            }
+            const cplx apt = cmul(ap, tr), amt = cmul(am, cconj(tr));
+            const REAL g2 = apt.re + amt.re;
+            const REAL goff = -apt.im + amt.im;
+            const REAL g1 = e1 * (az - zb[0].re);
+            gt2 += g2 * dt * (LIT(1000.0) / (t2 * t2));
+            gt1 += g1 * dt * (LIT(1000.0) / (t1 * t1));
+            gb0 += goff * (-LIT(2.0) * pi * dt);
+            g[8][ebase + e] += -r2 * g2 - r1 * g1 + goff * (-LIT(2.0) * pi * b0);
+            for (int64_t s = 0; s < S; ++s) {
+                pb[s] = cmul(pb[s], cconj(tr));
+                mb[s] = cmul(mb[s], tr);
+                zb[s] = cscale(e1, zb[s]);
+            }
+        }
+        const REAL tissue_g[7] = {gt1, gt2, gm0, gb1, ginv, gb1p, gb0};
+        for (int k = 0; k < 7; ++k) g[k][atom] += tissue_g[k];
+    }
+    free(buf);
+    free(traj);
 }
 
 /* ---- threaded drivers -------------------------------------------------- */
@@ -899,6 +1130,15 @@ void NAME(oracle_forward_complex)(const oracle_case* c, const oracle_offaxis* o,
 void NAME(oracle_second)(const oracle_case* c, const oracle_direction* d, const float* seed_imag,
                          REAL* const* value, REAL* const* curve) {
     run_second(c, d, seed_imag, 0, c->atom_count * c->train_count, value, curve);
+}
+
+/* Single-threaded complex adjoint; g[10] (t1, t2, m0, b1, inversion, b1
+ * phase, b0 per atom; flip, duration, phase per train and event) must be
+ * zeroed by the caller. */
+void NAME(oracle_adjoint_complex)(const oracle_case* c, const oracle_offaxis* o,
+                                  const float* seed_real, const float* seed_imag,
+                                  REAL* const* g) {
+    run_adjoint_complex(c, o, seed_real, seed_imag, 0, c->atom_count * c->train_count, g);
 }
 
 /* Single-threaded adjoint; gradient arrays must be zeroed by the caller. */

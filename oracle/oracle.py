@@ -266,6 +266,44 @@ def adjoint(p: Packed, seed_imag: np.ndarray, precision: str = "f64") -> dict[st
     return grads
 
 
+COMPLEX_GRADIENTS = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "b1_phase_rad", "b0_hz",
+                     "flip_rad", "duration_s", "phase_rad")
+
+
+def adjoint_complex(p: Packed, seed: np.ndarray, precision: str = "f64") -> dict[str, np.ndarray]:
+    """First-order adjoint of the complex path for a complex seed (the
+    cotangent of both output planes): gradients keyed as
+    :data:`COMPLEX_GRADIENTS`, per atom or per (train, event). Follows the
+    single-pool instant-RF case of ``simulate_vjp_range``
+    (src/torchsim/_epg_cpu.cpp:4840-5985)."""
+    dtype, _ = _dtype(precision)
+    keep: list = []
+    c = _case(p, keep)
+    arrays = {
+        "phase_rad": None if p.phase_rad is None else _f32(
+            np.broadcast_to(p.phase_rad, (p.train_count, p.event_count))),
+        "b1_phase_rad": _f32(p.b1_phase_rad),
+        "b0_hz": _f32(p.b0_hz),
+    }
+    keep.append(arrays)
+    o = _Offaxis()
+    for name, value in arrays.items():
+        setattr(o, name, _ptr(value))
+    sd = np.broadcast_to(np.asarray(seed, np.complex64), _shape(p))
+    sr, si = _f32(sd.real), _f32(sd.imag)
+    g = {n: np.zeros(p.atom_count, dtype=dtype) for n in COMPLEX_GRADIENTS[:7]}
+    for n in COMPLEX_GRADIENTS[7:]:
+        g[n] = np.zeros((p.train_count, p.event_count), dtype=dtype)
+    ptrs = (ctypes.c_void_p * 10)(*[g[n].ctypes.data for n in COMPLEX_GRADIENTS])
+    fn = getattr(_library(), f"oracle_adjoint_complex_{precision}")
+    fn(ctypes.byref(c), ctypes.byref(o), ctypes.c_void_p(sr.ctypes.data),
+       ctypes.c_void_p(si.ctypes.data), ptrs)
+    if p.train_count == 1:
+        for n in COMPLEX_GRADIENTS[7:]:
+            g[n] = g[n][0]
+    return g
+
+
 def _direction(p: Packed, direction: dict, keep: list) -> _Direction:
     d = _Direction()
     shape = (p.train_count, p.event_count)

@@ -332,6 +332,77 @@ def case_adjoint(ts, rec) -> dict:
     return out
 
 
+def _vjp_record(rec, prefix: str) -> dict:
+    """The packed buffers, seed and gradients of the first recorded
+    ``_run_packed_vjp`` call."""
+    out = {}
+    vjp = [c for c in rec.calls if c["route"] == "_run_packed_vjp"]
+    call = vjp[0]
+    out.update(_packed(call, prefix))
+    out[prefix + "seed"] = _np(call["args"][2])
+    names = (*TISSUE_NAMES, "duration", "flip", "phase")
+    for name, value in zip(names, call["result"], strict=True):
+        if value is not None:
+            out[f"{prefix}grad_{name}"] = _np(value)
+    return out
+
+
+def case_complex_adjoint(ts, rec) -> dict:
+    """Gradients on the complex path: an off-axis MRF (B0, B1phase, M0 maps)
+    with every tissue map, flip and TR a leaf, and a default-phase CPMG with
+    its refocusing flips and tissue as leaves; loss sum |s - target|^2."""
+    import torch
+    from torchsim.simulators import FSESimulator, MRFSimulator
+
+    rng = np.random.default_rng(8)
+    n, pulses = 5, 30
+    t1, t2, b1 = draw_tissue(rng, n)
+    b0 = rng.uniform(-40, 40, n).astype(np.float32)
+    b1p = rng.uniform(-0.5, 0.5, n).astype(np.float32)
+    m0 = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    target = (rng.standard_normal((n, pulses)) + 1j * rng.standard_normal((n, pulses)))
+    target = (0.05 * target).astype(np.complex64)
+    leaves = {k: torch.from_numpy(v).clone().requires_grad_(True) for k, v in
+              (("T1", t1), ("T2", t2), ("B1", b1), ("B0", b0), ("B1phase", b1p), ("M0", m0))}
+    theta = torch.from_numpy(flip).clone().requires_grad_(True)
+    tau = torch.from_numpy(tr).clone().requires_grad_(True)
+    rec.clear()
+    sig = MRFSimulator(flip=theta, TR=tau, TI=15.0, states=10).simulate(**leaves)
+    loss = (sig - torch.from_numpy(target)).abs().square().sum()
+    loss.backward()
+    out = {"mrf_flip_deg": flip, "mrf_tr_ms": tr, "mrf_t1": t1, "mrf_t2": t2, "mrf_b1": b1,
+           "mrf_b0": b0, "mrf_b1_phase": b1p, "mrf_m0": m0, "mrf_states": np.int64(10),
+           "mrf_target": target, "mrf_signal": _np(sig), "mrf_loss": _np(loss),
+           "mrf_grad_flip_deg": _np(theta.grad), "mrf_grad_tr_ms": _np(tau.grad)}
+    for k, v in leaves.items():
+        out[f"mrf_grad_{k}"] = _np(v.grad)
+    out.update(_vjp_record(rec, "mrf_vjp_"))
+    # Default-phase CPMG.
+    etl = 8
+    t1f = rng.uniform(300, 3000, 4).astype(np.float32)
+    t2f = rng.uniform(10, 300, 4).astype(np.float32)
+    b1f = rng.uniform(0.7, 1.3, 4).astype(np.float32)
+    refoc = rng.uniform(100, 180, etl).astype(np.float32)
+    ftarget = (0.05 * rng.standard_normal((4, etl))).astype(np.complex64)
+    fleaves = {k: torch.from_numpy(v).clone().requires_grad_(True) for k, v in
+               (("T1", t1f), ("T2", t2f), ("B1", b1f))}
+    phi = torch.from_numpy(refoc).clone().requires_grad_(True)
+    rec.clear()
+    fsig = FSESimulator(flip=phi, ESP=9.0, states=2 * etl).simulate(**fleaves)
+    floss = (fsig - torch.from_numpy(ftarget)).abs().square().sum()
+    floss.backward()
+    out.update({"fse_flip_deg": refoc, "fse_esp_ms": np.float32(9.0), "fse_t1": t1f,
+                "fse_t2": t2f, "fse_b1": b1f, "fse_states": np.int64(2 * etl),
+                "fse_target": ftarget, "fse_signal": _np(fsig), "fse_loss": _np(floss),
+                "fse_grad_flip_deg": _np(phi.grad)})
+    for k, v in fleaves.items():
+        out[f"fse_grad_{k}"] = _np(v.grad)
+    out.update(_vjp_record(rec, "fse_vjp_"))
+    return out
+
+
 def case_second(ts, rec) -> dict:
     """Second order. A Cramer-Rao cost of the (T1, T2) Jacobian differentiated
     with respect to the flip angles and TRs: the reference's design route
@@ -445,7 +516,7 @@ def case_gn(ts, rec) -> dict:
 
 
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
-         "mrf_second")
+         "mrf_second", "complex_adjoint")
 
 
 def main() -> None:
@@ -467,7 +538,7 @@ def main() -> None:
     for name, fn in (("mrf880", case_mrf880), ("mrf_prep", case_mrf_prep),
                      ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn),
                      ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
-                     ("mrf_second", case_second)):
+                     ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

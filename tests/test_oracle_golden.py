@@ -196,3 +196,63 @@ def test_oracle_second_order_planted_mistake_is_caught(golden):
     direction.pop("duration_s")
     _, curvature = O.second(p, seed, "f64", **direction)
     assert max_rel(curvature["flip_rad"], d["direct_curvature_flip"]) > 1e-3
+
+
+# ---- gradients on the complex path ------------------------------------------
+
+COMPLEX_GRADS = {"t1_ms": "t1_ms", "t2_ms": "t2_ms", "m0": "m0", "b1": "b1",
+                 "inversion": "inversion_efficiency", "b1_phase_rad": "b1_phase_rad",
+                 "b0_hz": "b0_hz", "flip_rad": "flip", "duration_s": "duration",
+                 "phase_rad": "phase"}
+
+
+def complex_adjoint_case(d, prefix: str):
+    fields = {k: d[k] for k in d.files}
+    fields["states"] = d[prefix.split("_")[0] + "_states"]
+    return packed_complex_from_golden(fields, prefix + "vjp_")
+
+
+@pytest.mark.parametrize("prefix", ["mrf", "fse"])
+def test_oracle_complex_adjoint_matches_reference(golden, prefix):
+    """Every gradient slot of the reference's complex first-order adjoint (an
+    off-axis MRF with B0, B1phase and M0 maps; a default-phase CPMG) against
+    the FP64 restatement. Gradients the reference forms as rounding noise
+    (B0 and B1phase of the on-resonance CPMG) are compared absolutely."""
+    d = golden("complex_adjoint")
+    p = complex_adjoint_case(d, prefix + "_")
+    g = O.adjoint_complex(p, d[f"{prefix}_vjp_seed"], "f64")
+    scale = max(float(np.abs(d[f"{prefix}_vjp_grad_{v}"]).max()) for v in COMPLEX_GRADS.values())
+    for mine, ref in COMPLEX_GRADS.items():
+        want = d[f"{prefix}_vjp_grad_{ref}"]
+        if np.abs(want).max() < 1e-6 * scale:
+            assert np.abs(g[mine]).max() <= 1e-6 * scale, mine
+        else:
+            assert max_rel(g[mine], want) <= 5e-6, mine
+
+
+def test_oracle_complex_adjoint_is_the_gradient_of_the_forward(golden):
+    """Central differences of the FP64 complex forward along random
+    directions of the tissue, flip, duration and phase buffers."""
+    d = golden("complex_adjoint")
+    p = complex_adjoint_case(d, "mrf_")
+    seed = d["mrf_vjp_seed"]
+    g = O.adjoint_complex(p, seed, "f64")
+    rng = np.random.default_rng(11)
+    # The packed inputs are FP32: the step must stay well above their
+    # rounding, which bounds the agreement at about 1e-3.
+    h = 1e-3
+    for name, attr in (("t1_ms", "t1_ms"), ("t2_ms", "t2_ms"), ("b1", "b1"), ("b0_hz", "b0_hz"),
+                       ("b1_phase_rad", "b1_phase_rad"), ("flip_rad", "flip_rad"),
+                       ("duration_s", "duration_s"), ("phase_rad", "phase_rad")):
+        base = np.asarray(getattr(p, attr), np.float64)
+        v = rng.standard_normal(base.shape) * np.maximum(np.abs(base), 1e-3)
+
+        def loss(sign):
+            q = complex_adjoint_case(d, "mrf_")
+            setattr(q, attr, base + sign * h * v)
+            out = O.forward_complex(q, "f64")
+            return float((seed.real * out.real + seed.imag * out.imag).sum())
+
+        fd = (loss(1.0) - loss(-1.0)) / (2 * h)
+        got = float((g[name].reshape(v.shape) * v).sum())
+        assert abs(got - fd) <= 2e-3 * max(abs(fd), 1e-9), (name, got, fd)
