@@ -91,6 +91,15 @@ typedef struct {
     const float* flip_rad;
 } tsg_direction;
 
+/* The complex path's further gradients (DEVICE pointers, nullable): per
+ * atom the transmit phase and off-resonance, per (train, event) the phase
+ * (of a pulse, or of an ADC's receiver). */
+typedef struct {
+    float* b1_phase_rad;
+    float* b0_hz;
+    float* phase_rad;
+} tsg_offaxis_gradients;
+
 /* Gradients the adjoint adds into (DEVICE pointers, nullable). Per atom:
  * t1/t2/m0/b1/inversion; per (train, event): flip and duration. The slots
  * simulate_real_vjp_range fills (_epg_cpu.cpp:6223-6231, 6180, 6217). */
@@ -284,6 +293,37 @@ int tsg_epg_adjoint_noalloc(const tsg_program* program, const tsg_tissue* tissue
                             const tsg_launch* launch, void* stream);
 /* TSG_STATIC_SCRATCH_BYTES, as built into the library. */
 int64_t tsg_static_scratch_bytes(void);
+
+/* ---- the complex path's first-order adjoint ----------------------------- */
+
+/* Sizes of the complex adjoint's trajectory (every op's entry state: six
+ * real planes; and every recorded F+[0]) and workspace. */
+int tsg_epg_complex_adjoint_plan(const tsg_program* program, int64_t atom_count,
+                                 int64_t state_count, const tsg_launch* launch,
+                                 int64_t* trajectory_bytes, int64_t* workspace_bytes);
+
+/* The complex forward (as tsg_epg_forward_complex; the output nullable) that
+ * also stores the trajectory tsg_epg_adjoint_complex reads. The program is
+ * built with event phases (tsg_program_create_phased). */
+int tsg_epg_forward_complex_trajectory(const tsg_program* program, const tsg_tissue* tissue,
+                                       const tsg_offaxis* offaxis, int64_t atom_count,
+                                       int64_t state_count, int layout, float* out_a,
+                                       float* out_b, void* trajectory, const tsg_launch* launch,
+                                       void* stream);
+
+/* First-order adjoint of the complex path (the reference's complex
+ * simulate_vjp_range, _epg_cpu.cpp:4840-5985): `seed` is the complex
+ * cotangent of the samples, two planes (TSG_LAYOUT_PLANES: seed_a real,
+ * seed_b imaginary) or interleaved complex64 (TSG_LAYOUT_COMPLEX). Adds the
+ * gradients of T1, T2, M0, B1, the inversion efficiency, flip and duration
+ * into `gradients`, and of B1phase, B0 and the event phases into
+ * `offaxis_gradients` (each nullable). Deterministic. */
+int tsg_epg_adjoint_complex(const tsg_program* program, const tsg_tissue* tissue,
+                            const tsg_offaxis* offaxis, int64_t atom_count, int64_t state_count,
+                            const float* seed_a, const float* seed_b, int seed_layout,
+                            const void* trajectory, const tsg_gradients* gradients,
+                            const tsg_offaxis_gradients* offaxis_gradients, void* workspace,
+                            int64_t workspace_bytes, const tsg_launch* launch, void* stream);
 
 /* ---- second order: the adjoint of the tangent sweep --------------------- */
 
@@ -506,8 +546,10 @@ int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count, int64_t a
  * buffers, two seed planes, 20 gradient slots (17 tissue, then flip, phase,
  * duration, the order of :11243-11253), 13 tail slots (61). The program is
  * compiled unmerged so that every event's duration gradient is formed.
- * Gradients are written (not accumulated); phase and the tissue directions
- * the real subspace divides out are written as zero. Synchronous. */
+ * Gradients are written (not accumulated). real_axis == 1 runs the real
+ * subspace (only the imaginary seed plane acts; phase, B1phase and B0 are
+ * written as zero); any other value the complex adjoint (both seed planes;
+ * phase, B1phase and B0 gradients formed). Synchronous. */
 int tsg_epg_simulate_vjp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
                          int64_t train_count, int64_t event_count, int64_t state_count,
                          int64_t output_count, int real_axis, int features);

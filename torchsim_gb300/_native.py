@@ -44,6 +44,10 @@ class Offaxis(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("b1_phase_rad", "b0_hz")]
 
 
+class OffaxisGradients(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("b1_phase_rad", "b0_hz", "phase_rad")]
+
+
 class Direction(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in
                 ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s", "flip_rad")]
@@ -153,6 +157,15 @@ SIGNATURES: dict[str, tuple] = {
                                       ctypes.POINTER(Direction), _int, _int, _int, _vp, _vp, _vp,
                                       _vp,
                                       _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_complex_adjoint_plan": (_int, [_vp, _i64, _i64, ctypes.POINTER(Launch),
+                                            ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "tsg_epg_forward_complex_trajectory": (_int, [_vp, ctypes.POINTER(Tissue),
+                                                  ctypes.POINTER(Offaxis), _i64, _i64, _int, _vp,
+                                                  _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_adjoint_complex": (_int, [_vp, ctypes.POINTER(Tissue), ctypes.POINTER(Offaxis), _i64,
+                                       _i64, _vp, _vp, _int, _vp, ctypes.POINTER(Gradients),
+                                       ctypes.POINTER(OffaxisGradients), _vp, _i64,
+                                       ctypes.POINTER(Launch), _vp]),
     "tsg_epg_design_plan": (_int, [_vp, _i64, _i64, ctypes.c_uint, ctypes.POINTER(Launch),
                                    ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "tsg_epg_design_forward": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.c_uint,

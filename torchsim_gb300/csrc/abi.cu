@@ -166,7 +166,7 @@ using namespace tsg;
 
 extern "C" int tsg_version(void) { return 1; }
 
-namespace {
+namespace tsg {
 
 int create_program(const float* duration_s, const int32_t* kind, const float* flip_rad,
                    const float* phase_rad, const uint8_t* action, const int32_t* output_index,
@@ -219,7 +219,7 @@ int create_program(const float* duration_s, const int32_t* kind, const float* fl
     return TSG_OK;
 }
 
-}  // namespace
+}  // namespace tsg
 
 extern "C" int tsg_program_create(const float* duration_s, const int32_t* kind,
                                   const float* flip_rad, const uint8_t* action,

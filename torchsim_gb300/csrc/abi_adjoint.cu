@@ -259,6 +259,132 @@ constexpr int TISSUE = 17, PACKED = 26, FLOATS = 20, TAIL = 13;
 }  // namespace
 }  // namespace tsg
 
+namespace tsg {
+namespace {
+
+// The complex path of the drop-in (the reference's complex simulate_vjp_range
+// single-pool instant case): a phased program compiled unmerged, so every
+// event's duration and phase gradient is formed; both seed planes act.
+int simulate_vjp_complex(void* const* pointers, int64_t atom_count, int64_t train_count,
+                         int64_t event_count, int64_t state_count, int64_t output_count,
+                         int features) {
+    if (features & 2) return fail(TSG_ERR_UNSUPPORTED, "flow is not built");
+    for (int idx : {7, 9, 12}) {
+        const float* v = static_cast<const float*>(pointers[idx]);
+        if (v && (idx != 7 || (features & 4)))
+            for (int64_t i = 0; i < atom_count; ++i)
+                if (v[i] != 0.f) return fail(TSG_ERR_UNSUPPORTED, "diffusion and second pools are not built");
+    }
+    std::lock_guard<std::mutex> guard(g_vjp_mutex);
+    cudaStream_t s = nullptr;
+    const float* duration = static_cast<const float*>(pointers[TISSUE + 0]);
+    const int32_t* kind = static_cast<const int32_t*>(pointers[TISSUE + 1]);
+    const float* flip = static_cast<const float*>(pointers[TISSUE + 2]);
+    const float* phase = static_cast<const float*>(pointers[TISSUE + 3]);
+    const uint8_t* action = static_cast<const uint8_t*>(pointers[TISSUE + 4]);
+    const int32_t* oindex = static_cast<const int32_t*>(pointers[TISSUE + 5]);
+    if (!phase && event_count > 0) return fail(TSG_ERR_ARGUMENT, "null phase buffer");
+    tsg_program* prog = nullptr;
+    int rc = create_program(duration, kind, flip, phase, action, oindex, train_count, event_count, 1,
+                            nullptr, &prog);
+    if (rc) return rc;
+    if (prog->host.outputs > output_count) {
+        tsg_program_destroy(prog);
+        return fail(TSG_ERR_ARGUMENT, "output index beyond output_count");
+    }
+    prog->host.outputs = output_count;
+    std::vector<void*> owned;
+    auto dev = [&](size_t bytes, void** out) -> int {
+        *out = nullptr;
+        cudaError_t e = cudaMallocAsync(out, bytes ? bytes : 4, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync");
+        owned.push_back(*out);
+        return TSG_OK;
+    };
+    auto up = [&](const void* host, size_t bytes, void** out) -> int {
+        *out = nullptr;
+        if (!host || bytes == 0) return TSG_OK;
+        int r = dev(bytes, out);
+        if (r) return r;
+        cudaError_t e = cudaMemcpyAsync(*out, host, bytes, cudaMemcpyHostToDevice, s);
+        return e == cudaSuccess ? TSG_OK : cuda_fail(e, "cudaMemcpyAsync(H2D)");
+    };
+    const size_t ab = size_t(atom_count) * 4;
+    const size_t eb = size_t(train_count) * size_t(event_count) * 4;
+    const size_t ob = size_t(train_count) * size_t(atom_count) * size_t(output_count) * 4;
+    void *t1 = nullptr, *t2 = nullptr, *m0 = nullptr, *b1 = nullptr, *inv = nullptr;
+    void *b1p = nullptr, *b0 = nullptr, *sr = nullptr, *si = nullptr, *traj = nullptr,
+         *work = nullptr, *g = nullptr;
+    int64_t traj_bytes = 0, work_bytes = 0;
+    if (!rc) rc = up(pointers[0], ab, &t1);
+    if (!rc) rc = up(pointers[1], ab, &t2);
+    if (!rc && (features & 16)) rc = up(pointers[2], ab, &m0);
+    if (!rc && (features & 8)) rc = up(pointers[3], ab, &b1);
+    if (!rc && (features & 32)) rc = up(pointers[6], ab, &inv);
+    if (!rc && (features & 1)) rc = up(pointers[4], ab, &b1p);
+    if (!rc && (features & 1)) rc = up(pointers[5], ab, &b0);
+    if (!rc) rc = up(pointers[PACKED + 0], ob, &sr);
+    if (!rc) rc = up(pointers[PACKED + 1], ob, &si);
+    if (!rc) rc = tsg_epg_complex_adjoint_plan(prog, atom_count, state_count, nullptr, &traj_bytes,
+                                               &work_bytes);
+    if (!rc && atom_count > 0) rc = dev(size_t(traj_bytes), &traj);
+    if (!rc && atom_count > 0) rc = dev(size_t(work_bytes), &work);
+    // Device gradients: 7 per-atom rows (t1, t2, m0, b1, inversion, b1 phase,
+    // b0), then flip, duration and phase rows.
+    const size_t gb = 7 * ab + 3 * eb;
+    if (!rc) rc = dev(gb, &g);
+    if (!rc) {
+        cudaMemsetAsync(g, 0, gb, s);
+        float* gf = static_cast<float*>(g);
+        float* ev = gf + 7 * atom_count;
+        const int64_t te = train_count * event_count;
+        tsg_gradients grads{gf, gf + atom_count, gf + 2 * atom_count, gf + 3 * atom_count,
+                            gf + 4 * atom_count, ev, ev + te};
+        tsg_offaxis_gradients ogr{gf + 5 * atom_count, gf + 6 * atom_count, ev + 2 * te};
+        tsg_tissue tissue{static_cast<float*>(t1), static_cast<float*>(t2), static_cast<float*>(m0),
+                          static_cast<float*>(b1), static_cast<float*>(inv)};
+        tsg_offaxis off{static_cast<float*>(b1p), static_cast<float*>(b0)};
+        if (atom_count > 0 && sr && si) {
+            rc = tsg_epg_forward_complex_trajectory(prog, &tissue, &off, atom_count, state_count,
+                                                    TSG_LAYOUT_PLANES, nullptr, nullptr, traj,
+                                                    nullptr, s);
+            if (!rc)
+                rc = tsg_epg_adjoint_complex(prog, &tissue, &off, atom_count, state_count,
+                                             static_cast<float*>(sr), static_cast<float*>(si),
+                                             TSG_LAYOUT_PLANES, traj, &grads, &ogr, work,
+                                             work_bytes, nullptr, s);
+        }
+        if (!rc) {
+            // Slots: 17 tissue, then flip, phase, duration (_epg_cpu.cpp:11243-11253).
+            void* const* slots = pointers + PACKED + 2;
+            const int tissue_slot[7] = {0, 1, 2, 3, 6, 4, 5};
+            auto down = [&](void* dst, const float* src, size_t bytes) {
+                if (!dst || rc) return;
+                cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+                if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync(D2H)");
+            };
+            for (int k = 0; k < 7; ++k) down(slots[tissue_slot[k]], gf + k * atom_count, ab);
+            down(slots[TISSUE + 0], ev, eb);
+            down(slots[TISSUE + 1], ev + 2 * te, eb);
+            down(slots[TISSUE + 2], ev + te, eb);
+        }
+    }
+    for (void* p : owned) cudaFreeAsync(p, s);
+    cudaError_t es = cudaStreamSynchronize(s);
+    if (!rc && es != cudaSuccess) rc = cuda_fail(es, "cudaStreamSynchronize");
+    if (!rc) {
+        // Directions not built carry no gradient here.
+        void* const* slots = pointers + PACKED + 2;
+        for (int k : {7, 8, 9, 10, 11, 12, 13, 14, 15, 16})
+            if (slots[k]) std::fill_n(static_cast<float*>(slots[k]), atom_count, 0.f);
+    }
+    tsg_program_destroy(prog);
+    return rc;
+}
+
+}  // namespace
+}  // namespace tsg
+
 extern "C" int tsg_epg_simulate_vjp(void* const* pointers, int64_t pointer_count,
                                     int64_t atom_count, int64_t train_count, int64_t event_count,
                                     int64_t state_count, int64_t output_count, int real_axis,
@@ -268,11 +394,12 @@ extern "C" int tsg_epg_simulate_vjp(void* const* pointers, int64_t pointer_count
         return fail(TSG_ERR_ARGUMENT, "wrong number of buffer pointers");
     if (atom_count < 0 || train_count < 1 || event_count < 0 || state_count < 1 || output_count < 0)
         return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
-    if (real_axis != 1)
-        return fail(TSG_ERR_UNSUPPORTED, "only the real-subspace path (real_axis == 1) is built");
     for (int i = 0; i < TAIL; ++i)
         if (pointers[PACKED + 2 + FLOATS + i] != nullptr && i != TAIL - 3)  // GRADIENT slot may be given
             return fail(TSG_ERR_UNSUPPORTED, "transition tables, pools and per-voxel pulses are not built");
+    if (real_axis != 1)
+        return simulate_vjp_complex(pointers, atom_count, train_count, event_count, state_count,
+                                    output_count, features);
     if (features & 2) return fail(TSG_ERR_UNSUPPORTED, "flow is not built");
     for (int idx : {7, 9, 12}) {
         const float* v = static_cast<const float*>(pointers[idx]);

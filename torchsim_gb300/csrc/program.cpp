@@ -26,7 +26,7 @@ constexpr int SLOT_RELAX = 0, SLOT_SHIFT1 = 1, SLOT_RF = 2, SLOT_SHIFT2 = 3, SLO
 
 struct Builder {
     Op op{};
-    OpSource src{-1, -1};
+    OpSource src{-1, -1, -1};
     float2 ph{0.f, 0.f};  // phase of the op's pulse, of its receiver
     std::vector<float2>* phases = nullptr;  // collected when event phases are given
     int pos = -1;  // last slot used; -1 = no op open
@@ -40,7 +40,7 @@ struct Builder {
         srcs.push_back(src);
         if (phases) phases->push_back(ph);
         op = Op{};
-        src = OpSource{-1, -1};
+        src = OpSource{-1, -1, -1};
         ph = float2{0.f, 0.f};
         pos = -1;
         n[0] = n[1] = n[2] = 0;
@@ -95,6 +95,7 @@ struct Builder {
             case SLOT_RECORD:
                 op.code |= OP_RECORD;
                 op.record = record;
+                src.rec_event = event;
                 ph.y = phase;
                 break;
             case SLOT_SPOIL1: op.code |= OP_SPOIL1; break;
@@ -175,7 +176,7 @@ int compile_program(const float* duration, const int32_t* kind, const float* fli
     out->outputs = outputs;
     out->sequential_records = sequential;
     out->op.assign(size_t(trains) * longest, Op{});
-    out->src.assign(size_t(trains) * longest, OpSource{-1, -1});
+    out->src.assign(size_t(trains) * longest, OpSource{-1, -1, -1});
     for (int64_t t = 0; t < trains; ++t) {
         std::copy(per_train[t].begin(), per_train[t].end(), out->op.begin() + t * longest);
         std::copy(per_src[t].begin(), per_src[t].end(), out->src.begin() + t * longest);

@@ -52,6 +52,7 @@ __host__ __device__ inline int op_shift3(uint32_t c) { return (c >> OP_SHIFT3_SH
 struct OpSource {
     int32_t dt_event;
     int32_t rf_event;
+    int32_t rec_event;  // the recording (ADC) event, for its phase's gradient
 };
 
 struct HostProgram {
@@ -87,6 +88,13 @@ int cuda_fail(cudaError_t err, const char* where);
         cudaError_t _e = (call);                         \
         if (_e != cudaSuccess) return ::tsg::cuda_fail(_e, #call); \
     } while (0)
+
+// Compiles an event stream and copies it to the current device (the phases
+// nullable; with them, the complex path's per-op phases).
+int create_program(const float* duration_s, const int32_t* kind, const float* flip_rad,
+                   const float* phase_rad, const uint8_t* action, const int32_t* output_index,
+                   int64_t train_count, int64_t event_count, int unmerged,
+                   const float* duration_tangent, tsg_program** out);
 
 int compile_program(const float* duration, const int32_t* kind, const float* flip,
                     const uint8_t* action, const int32_t* output_index, int64_t trains,

@@ -191,12 +191,13 @@ class _EpgSimulator:
         signal, _ = self._run(values, None)
         return signal
 
-    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions):
-        """Attach the protocol's differentiable arguments to the event buffers."""
+    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions, phase_ev=None):
+        """Attach the protocol's differentiable arguments to the event buffers
+        (flip, duration, phase; ``(trains, events)``)."""
         if any(isinstance(v, torch.Tensor) and v.requires_grad for v in protocol.values()):
             raise NotImplementedError(
                 f"{type(self).__name__}: gradients w.r.t. its sequence arguments are not built")
-        return flip_ev, dur_ev
+        return flip_ev, dur_ev, phase_ev
 
     def _run_differentiable(self, values: dict[str, Any], names: Sequence[str] | None = None):
         """The signal (or, with ``names``, the signal and Jacobian) on the
@@ -208,9 +209,11 @@ class _EpgSimulator:
                                   (home if home.type == "cuda" else None))
         plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in protocol.items()}
         events = self.events(repetitions=repetitions, **plain)
-        if _leaves_real_subspace(events, held):
+        complex_path = _leaves_real_subspace(events, held)
+        if complex_path and names:
             raise NotImplementedError(
-                "gradients on the complex path (RF phases, B0, B1phase) are not built")
+                "a differentiable Jacobian on the complex path (RF phases, B0, B1phase) is not "
+                "built; its signal is differentiable")
         batch = _batch(held)
         voxels = _numel(batch)
         maps = self._kernel_maps(held)
@@ -232,15 +235,29 @@ class _EpgSimulator:
                     raise ValueError(
                         f"{name!r} is not among the properties this call gave "
                         f"{type(self).__name__}: {sorted(held)}")
+        def turn(value):
+            # Transmit phase and off-resonance: absent (or a scalar 0) stays
+            # out of the kernel.
+            if value is None or (not _tensorish(value) and float(value) == 0.0):
+                return None
+            return flat(value, optional=False)
+
         with torch.cuda.device(dev):
-            program = program_for(events, dev)
+            program = program_for(events, dev, phased=complex_path)
             flip_ev = torch.from_numpy(events.flip).to(dev)
             dur_ev = torch.from_numpy(events.duration).to(dev)
-            flip_ev, dur_ev = self._event_gradients(protocol, events, flip_ev, dur_ev, repetitions)
+            phase_ev = torch.from_numpy(
+                np.array(np.broadcast_to(events.phase, events.duration.shape), np.float32)).to(dev)
+            flip_ev, dur_ev, phase_ev = self._event_gradients(protocol, events, flip_ev, dur_ev,
+                                                              repetitions, phase_ev)
             tissue = (flat(maps["T1"], True, False), flat(maps["T2"], True, False),
                       flat(maps["M0"]), flat(maps["B1"]), flat(maps["inv"]))
             jac = None
-            if names:
+            if complex_path:
+                signal = engine.EpgComplexFunction.apply(
+                    program, states, None, *tissue, turn(maps.get("B1phase")),
+                    turn(maps.get("B0")), flip_ev, dur_ev, phase_ev)
+            elif names:
                 kernel = tuple(self._kernel_names(names))
                 signal, jac = engine.JacobianFunction.apply(program, states, kernel, None, *tissue,
                                                             flip_ev, dur_ev)
@@ -287,7 +304,7 @@ class MRFSimulator(_EpgSimulator):
     def events(self, *, flip, TR, TI=0.0, phases=0.0, repetitions=1) -> PackedEvents:
         return mrf_events(flip, TR, TI_ms=TI, phases_deg=phases, repetitions=repetitions)
 
-    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions):
+    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions, phase_ev=None):
         flip = protocol.get("flip")
         tr = protocol.get("TR")
         ti = protocol.get("TI", 0.0)
@@ -309,7 +326,9 @@ class MRFSimulator(_EpgSimulator):
             t = ti.to(dev, torch.float32).reshape(()) * 1e-3
             idx = torch.from_numpy(where["ti"]).to(dev)
             dur_ev = dur_ev.index_add(1, idx, (t - t.detach()).expand(idx.numel())[None])
-        return flip_ev, dur_ev
+        if isinstance(protocol.get("phases"), torch.Tensor) and protocol["phases"].requires_grad:
+            raise NotImplementedError("MRFSimulator: gradients w.r.t. phases are not built")
+        return flip_ev, dur_ev, phase_ev
 
 
 class FSESimulator(_EpgSimulator):
@@ -335,6 +354,29 @@ class FSESimulator(_EpgSimulator):
         maps = super()._kernel_maps(held)
         maps["M0"] = None  # applied after the kernel
         return maps
+
+    def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions, phase_ev=None):
+        """Refocusing flips (deg) and phases (deg) onto the train's events:
+        echo j's pulse is event 1 + 3j and its ADC 2 + 3j
+        (:func:`torchsim_gb300.sequence.fse_events`), the ADC sharing the
+        pulse's phase."""
+        other = [k for k in protocol if k not in ("flip", "phases")]
+        if any(isinstance(protocol[k], torch.Tensor) and protocol[k].requires_grad for k in other):
+            raise NotImplementedError("FSESimulator: gradients w.r.t. ESP, TR and the excitation "
+                                      "are not built")
+        dev = flip_ev.device
+        flip = protocol.get("flip")
+        n = (events.events - 1) // 3
+        pulses = torch.from_numpy(1 + 3 * np.arange(n)).to(dev)
+        if isinstance(flip, torch.Tensor) and flip.requires_grad:
+            played = played_flip_torch(torch.atleast_1d(flip).to(dev))
+            flip_ev = flip_ev.index_add(1, pulses, (played - played.detach())[None])
+        phases = protocol.get("phases")
+        if isinstance(phases, torch.Tensor) and phases.requires_grad and phase_ev is not None:
+            turn = torch.deg2rad(torch.atleast_1d(phases).to(dev, torch.float32)).expand(n)
+            delta = (turn - turn.detach())[None]
+            phase_ev = phase_ev.index_add(1, pulses, delta).index_add(1, pulses + 1, delta)
+        return flip_ev, dur_ev, phase_ev
 
     def _kernel_names(self, names):
         kernel = [n for n in names if n in ("T1", "T2", "B1")]
