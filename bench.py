@@ -447,6 +447,27 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
                                                        launch=fwd_shape))
     bwd = timed(lambda: engine.adjoint(prog, tissue, S, seed, ckpt, c, grads, workspace=work,
                                        launch=shape))
+    del ckpt, work
+    # The complex path: the same sequence with RF phases U(-40, 40) deg and
+    # per-voxel B0 U(-40, 40) Hz and B1phase U(-0.5, 0.5) rad.
+    cev = mrf_events(flips, trs, phases_deg=rng.uniform(-40, 40, n))
+    cprog = program_for(cev, device, phased=True)
+    off, keep = engine.offaxis_maps(device, V, rng.uniform(-0.5, 0.5, V).astype(np.float32),
+                                    rng.uniform(-40, 40, V).astype(np.float32))
+    csig = torch.empty((V, n), dtype=torch.complex64, device=device)
+    tb, wb = engine.complex_adjoint_plan(cprog, V, S)
+    ctraj = torch.empty(tb, dtype=torch.uint8, device=device)
+    cwork = torch.empty(wb, dtype=torch.uint8, device=device)
+    cgrads = {k: torch.zeros(V, device=device) for k in ("t1_ms", "t2_ms", "b1", "b1_phase_rad",
+                                                         "b0_hz")}
+    for k in ("flip_rad", "duration_s", "phase_rad"):
+        cgrads[k] = torch.zeros((1, cev.events), device=device)
+    c_fwd = timed(lambda: engine.forward_complex(cprog, tissue, S, off, out=csig))
+    c_fwd_t = timed(lambda: engine.forward_complex_trajectory(cprog, tissue, S, off,
+                                                              trajectory=ctraj))
+    c_bwd = timed(lambda: engine.adjoint_complex(cprog, tissue, S, seed, ctraj, cgrads, off,
+                                                 workspace=cwork))
+    del ctraj, cwork, keep
     return {
         "workload": "MRF adjoint: 16384 voxels, 600 pulses (flip U(5,70) deg, TR U(8,15) ms), "
                     "nstates 20, loss sum |s - target|^2",
@@ -463,6 +484,16 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
         "gradient_definition": "forward with checkpoints + backward, over a plain forward (the "
                                "reference's benchmarks/anatomy.py measure: 8.4x CUDA, 4.6x CPU)",
         "forward_updates_per_s": V * n * S / (fwd * 1e-3),
+        "complex": {
+            "workload": "the same sequence with RF phases U(-40, 40) deg, B0 U(-40, 40) Hz, "
+                        "B1phase U(-0.5, 0.5) rad per voxel (the complex path)",
+            "forward_ms": c_fwd,
+            "forward_with_trajectory_ms": c_fwd_t,
+            "backward_ms": c_bwd,
+            "backward_over_forward": c_bwd / c_fwd,
+            "gradient_over_forward": (c_fwd_t + c_bwd) / c_fwd,
+            "gradients": "T1, T2, B1, B1phase, B0, flip, duration, phase",
+        },
         "timing": "best of 5 after 3 warm-up runs, CUDA events",
     }
 
