@@ -274,13 +274,11 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         host_sig = torch.empty((atoms, PULSES), dtype=torch.complex64).pin_memory()
         host_jac = torch.empty((atoms, 3, PULSES), dtype=torch.complex64).pin_memory()
 
+        host_maps = engine.TissueMaps(host_t[0], host_t[1], None, host_t[2], None)
+
         def e2e_step():
-            dev_t = [h.to(device, non_blocking=True) for h in host_t]
-            maps = engine.TissueMaps(dev_t[0], dev_t[1], None, dev_t[2], None)
-            engine.forward_tangents(program, maps, STATES, names, sig_out=sig, jac_out=jac,
-                                    launch=launch)
-            host_sig.copy_(sig, non_blocking=True)
-            host_jac.copy_(jac, non_blocking=True)
+            engine.forward_tangents_host(program, host_maps, STATES, names, host_sig, host_jac,
+                                         chunks=16, launch=launch, device=device)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -293,7 +291,8 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         e2e = {"value": updates / e2e_s, "unit": "updates/s", "ms_per_step": e2e_s * 1e3,
                "h2d_bytes_per_step": 3 * atoms * 4,
                "d2h_bytes_per_step": int(host_sig.numel() * 8 + host_jac.numel() * 8),
-               "api": "engine.forward_tangents with pinned host tissue and outputs"}
+               "api": "engine.forward_tangents_host: pinned host tissue in, pinned host signal "
+                      "and Jacobian out, 16 voxel chunks whose copies overlap the next sweep"}
         del host_sig, host_jac
 
     if rank != 0:

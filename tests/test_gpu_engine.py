@@ -9,7 +9,7 @@ import pytest
 import torch
 
 from oracle import oracle as O
-from tests.helpers import max_rel, packed_from_events
+from tests.helpers import draw_tissue, max_rel, packed_from_events
 
 pytestmark = pytest.mark.gpu
 
@@ -54,3 +54,33 @@ def test_engine_default_states_and_echo_record(cuda):
     assert res.signal.shape == (64, 12) and bool(res.echo.all())
     ref = O.forward(packed_from_events(ev, T1.cpu().numpy(), T2.cpu().numpy(), states), "f64")
     assert max_rel(-res.signal.real.cpu().numpy(), ref) <= SIGNAL_TOL
+
+
+def test_host_pipeline_matches_the_device_pass(cuda):
+    """forward_tangents_host (pinned host maps in, pinned host samples out,
+    chunked with overlapping copies) gives the device pass's bits."""
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    rng = np.random.default_rng(9)
+    ev = mrf_events(rng.uniform(5, 60, 70).astype(np.float32), 9.0)
+    prog = program_for(ev, cuda)
+    V = 1000
+    t1, t2, b1 = draw_tissue(10, V)
+    names = ("T1", "T2", "B1")
+    dev_maps = engine.tissue_maps(cuda, V, t1, t2, None, b1, None)
+    sig, jac = engine.forward_tangents(prog, dev_maps, 12, names)
+    host = engine.TissueMaps(*[torch.from_numpy(a).pin_memory() for a in (t1, t2)], None,
+                             torch.from_numpy(b1).pin_memory(), None)
+    sig_h = torch.empty((V, ev.outputs), dtype=torch.complex64).pin_memory()
+    jac_h = torch.empty((V, 3, ev.outputs), dtype=torch.complex64).pin_memory()
+    for chunks in (1, 7, 16):
+        sig_h.zero_()
+        jac_h.zero_()
+        engine.forward_tangents_host(prog, host, 12, names, sig_h, jac_h, chunks=chunks,
+                                     device=cuda)
+        torch.cuda.synchronize()
+        assert torch.equal(sig_h, sig.cpu()) and torch.equal(jac_h, jac.cpu()), chunks
+    with pytest.raises(ValueError):
+        engine.forward_tangents_host(prog, host, 12, names, torch.empty_like(sig_h, device="cpu"),
+                                     jac_h, device=cuda)

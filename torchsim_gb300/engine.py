@@ -229,6 +229,63 @@ def forward_tangents(program: Program, tissue: TissueMaps, states: int, names: S
     return sig, jac
 
 
+def forward_tangents_host(program: Program, tissue: TissueMaps, states: int,
+                          names: Sequence[str], sig_host: torch.Tensor, jac_host: torch.Tensor,
+                          *, chunks: int = 16, launch=None, device: torch.device | None = None):
+    """Signal and Jacobian of host-resident tissue into host memory: the
+    voxels go in ``chunks`` pieces, each uploaded, swept (the fused pass of
+    :func:`forward_tangents`) into one of two device buffers, and copied
+    back on a second stream while the next piece is swept, so the
+    device-to-host transfer, which bounds this call, overlaps the compute.
+
+    ``tissue`` holds pinned host maps; ``sig_host`` ``(voxels, P)`` and
+    ``jac_host`` ``(voxels, k, P)`` are pinned complex64. Returns when the
+    copies are queued (synchronise the current stream before reading)."""
+    device = require_cuda(device)
+    if program.trains != 1:
+        raise ValueError("the host-buffer pipeline takes single-train programs")
+    for t in (sig_host, jac_host, tissue.t1, tissue.t2):
+        if t.device.type != "cpu" or not t.is_pinned():
+            raise ValueError("host buffers must be pinned (page-locked) CPU tensors")
+    V = tissue.voxels
+    k = len(names)
+    chunks = max(1, min(int(chunks), V))
+    step = (V + chunks - 1) // chunks
+    compute = torch.cuda.current_stream(device)
+    copy = torch.cuda.Stream(device)
+    sig_d = [torch.empty((step, program.outputs), dtype=torch.complex64, device=device)
+             for _ in range(2)]
+    jac_d = [torch.empty((step, k, program.outputs), dtype=torch.complex64, device=device)
+             for _ in range(2)]
+    freed = [None, None]  # copy-done events of each device buffer
+    for c, a in enumerate(range(0, V, step)):
+        b = min(a + step, V)
+        slot = c % 2
+        if freed[slot] is not None:
+            compute.wait_event(freed[slot])
+
+        def up(x):
+            return None if x is None else x[a:b].to(device, non_blocking=True)
+
+        maps = TissueMaps(up(tissue.t1), up(tissue.t2), up(tissue.m0), up(tissue.b1),
+                          up(tissue.inv))
+        sig, jac = sig_d[slot][: b - a], jac_d[slot][: b - a]
+        forward_tangents(program, maps, states, names, sig_out=sig, jac_out=jac, launch=launch)
+        done = torch.cuda.Event()
+        done.record(compute)
+        copy.wait_event(done)
+        with torch.cuda.stream(copy):
+            sig_host[a:b].copy_(sig, non_blocking=True)
+            jac_host[a:b].copy_(jac, non_blocking=True)
+            freed[slot] = torch.cuda.Event()
+            freed[slot].record(copy)
+        for x in (maps.t1, maps.t2, maps.m0, maps.b1, maps.inv, sig, jac):
+            if x is not None:
+                x.record_stream(copy)
+    compute.wait_stream(copy)
+    return sig_host, jac_host
+
+
 # (lanes per voxel, orders per lane) instantiated per kernel family, as in the
 # sweep tables of csrc/sweep_*.cu.
 FAMILY_SHAPES = {
