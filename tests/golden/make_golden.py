@@ -478,6 +478,42 @@ def case_second(ts, rec) -> dict:
     return out
 
 
+def case_double_backward(ts, rec) -> dict:
+    """Reverse over reverse through the public simulator: the gradient of
+    <directions, d<seed, s>/d(inputs)> with respect to the inputs and the
+    seed (the reference's _NativeEpg backward differentiated once more)."""
+    import torch
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(9)
+    n, pulses = 4, 25
+    t1, t2, b1 = draw_tissue(rng, n)
+    m0 = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    leaves = {k: torch.from_numpy(v).clone().requires_grad_(True) for k, v in
+              (("T1", t1), ("T2", t2), ("B1", b1), ("M0", m0))}
+    theta = torch.from_numpy(flip).clone().requires_grad_(True)
+    tau = torch.from_numpy(tr).clone().requires_grad_(True)
+    sig = MRFSimulator(flip=theta, TR=tau, states=8).simulate(**leaves)
+    gen = torch.Generator().manual_seed(4)
+    seed = torch.randn(sig.shape, generator=gen, dtype=torch.complex64).requires_grad_(True)
+    inputs = (theta, tau, *leaves.values())
+    grads = torch.autograd.grad(sig, inputs, seed, create_graph=True)
+    directions = [torch.randn(g.shape, generator=gen) for g in grads]
+    contraction = sum((g * d).sum() for g, d in zip(grads, directions, strict=True))
+    second = torch.autograd.grad(contraction, (*inputs, seed))
+    out = {"flip_deg": flip, "tr_ms": tr, "t1": t1, "t2": t2, "b1": b1, "m0": m0,
+           "states": np.int64(8), "seed": _np(seed), "contraction": _np(contraction)}
+    names = ("flip_deg", "tr_ms", "T1", "T2", "B1", "M0")
+    for name, g, d, h in zip(names, grads, directions, second[:-1], strict=True):
+        out[f"grad_{name}"] = _np(g)
+        out[f"direction_{name}"] = _np(d)
+        out[f"second_{name}"] = _np(h)
+    out["second_seed"] = _np(second[-1])
+    return out
+
+
 def _accelerators_of(ts):
     from torchsim.sequence import _accelerators
 
@@ -516,7 +552,7 @@ def case_gn(ts, rec) -> dict:
 
 
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
-         "mrf_second", "complex_adjoint")
+         "mrf_second", "complex_adjoint", "double_backward")
 
 
 def main() -> None:
@@ -538,7 +574,8 @@ def main() -> None:
     for name, fn in (("mrf880", case_mrf880), ("mrf_prep", case_mrf_prep),
                      ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn),
                      ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
-                     ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint)):
+                     ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint),
+                     ("double_backward", case_double_backward)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

@@ -212,3 +212,63 @@ def test_adjoint_block_size_is_checked(cuda):
     prog = program_for(mrf_events(np.full(8, 20.0, np.float32), 9.0), cuda)
     with pytest.raises(ValueError):
         engine.adjoint_plan(prog, 16, 10, (5, 2, 8), 0)
+
+
+def test_second_backward_matches_reference(cuda, golden):
+    """Reverse over reverse through the public simulator: the gradient of
+    <directions, d<seed, s>/d(inputs)> with respect to the inputs and the
+    seed against the reference's (its _NativeEpg backward differentiated once
+    more; here the second-order sweep)."""
+    from torchsim_gb300 import MRFSimulator
+
+    d = golden("double_backward")
+    leaves = {k: torch.tensor(d[v], device=cuda, requires_grad=True) for k, v in
+              (("T1", "t1"), ("T2", "t2"), ("B1", "b1"), ("M0", "m0"))}
+    theta = torch.tensor(d["flip_deg"], device=cuda, requires_grad=True)
+    tau = torch.tensor(d["tr_ms"], device=cuda, requires_grad=True)
+    sig = MRFSimulator(flip=theta, TR=tau, states=int(d["states"])).simulate(**leaves)
+    seed = torch.tensor(d["seed"], device=cuda, requires_grad=True)
+    inputs = (theta, tau, *leaves.values())
+    grads = torch.autograd.grad(sig, inputs, seed, create_graph=True)
+    names = ("flip_deg", "tr_ms", "T1", "T2", "B1", "M0")
+    for name, g in zip(names, grads, strict=True):
+        assert max_rel(g.detach().cpu().numpy(), d[f"grad_{name}"]) <= GRAD_TOL, name
+    directions = [torch.tensor(d[f"direction_{n}"], device=cuda) for n in names]
+    contraction = sum((g * v).sum() for g, v in zip(grads, directions, strict=True))
+    assert abs(contraction.item() - float(d["contraction"])) <= 1e-4 * abs(float(d["contraction"]))
+    second = torch.autograd.grad(contraction, (*inputs, seed))
+    for name, h in zip(names, second[:-1], strict=True):
+        assert max_rel(h.cpu().numpy(), d[f"second_{name}"]) <= GRAD_TOL, name
+    assert max_rel(second[-1].cpu().numpy(), d["second_seed"]) <= GRAD_TOL
+
+
+def test_hessian_vector_product_matches_finite_differences(cuda):
+    """d/dT2 of the T2 gradient of a loss along a direction, against central
+    differences of the first-order gradient (the check of the reference's
+    tests/sequence/test_vjp.py:344-385, with steps of 0.1% of each T2)."""
+    from torchsim_gb300 import MRFSimulator
+
+    rng = np.random.default_rng(21)
+    flips = rng.uniform(5, 70, 40).astype(np.float32)
+    t1, t2, b1 = draw_tissue(22, 6)
+    w = torch.from_numpy((rng.standard_normal((6, 40)) + 1j * rng.standard_normal((6, 40)))
+                         .astype(np.complex64)).to(cuda)
+    # A direction scaled by each voxel's T2, so a step is the same fraction
+    # of every voxel's T2.
+    v = torch.from_numpy((rng.standard_normal(6) * t2).astype(np.float32)).to(cuda)
+
+    def grad_t2(t2v, create):
+        x = t2v.clone().requires_grad_(True)
+        sig = MRFSimulator(flip=torch.tensor(flips), TR=10.0, states=10).simulate(
+            T1=torch.tensor(t1, device=cuda), T2=x, B1=torch.tensor(b1, device=cuda))
+        (g,) = torch.autograd.grad(sig, (x,), w, create_graph=create)
+        return x, g
+
+    base = torch.tensor(t2, device=cuda)
+    x, g = grad_t2(base, True)
+    (hv,) = torch.autograd.grad((g * v).sum(), (x,))
+    h = 1e-3
+    _, gp = grad_t2(base + h * v, False)
+    _, gm = grad_t2(base - h * v, False)
+    fd = (gp - gm) / (2 * h)
+    assert max_rel(hv.cpu().numpy(), fd.cpu().numpy()) <= 1e-2

@@ -821,7 +821,9 @@ class EpgFunction(torch.autograd.Function):
     1402-1594): inputs are the flat tissue maps and the event-level flip and
     duration buffers of the program (for gradient routing only: their values
     are baked into ``program``); the output is the complex64 signal
-    ``(trains*voxels, outputs)``.
+    ``(trains*voxels, outputs)``. The backward is itself differentiable
+    (:class:`EpgVjpFunction`): a second backward through it, as a
+    Hessian-vector product takes, runs the second-order sweep.
     """
 
     @staticmethod
@@ -835,29 +837,92 @@ class EpgFunction(torch.autograd.Function):
         forward_checkpointed(program, tissue, states, c, ckpt, out=out, launch=launch)
         ctx.program, ctx.states, ctx.launch, ctx.c = program, states, launch, c
         ctx.tissue = tissue
-        ctx.save_for_backward(ckpt)
-        ctx.present = (m0 is not None, b1 is not None, inv is not None)
+        given = (t1, t2, m0, b1, inv, flip_events, duration_events)
+        ctx.present = tuple(x is not None for x in given)
+        ctx.save_for_backward(ckpt, *(x for x in given if x is not None))
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        (ckpt,) = ctx.saved_tensors
-        tissue, program = ctx.tissue, ctx.program
+        saved = list(ctx.saved_tensors)
+        ckpt = saved.pop(0)
+        inputs = [saved.pop(0) if present else None for present in ctx.present]
         need = ctx.needs_input_grad
+        grads = EpgVjpFunction.apply(ctx.program, ctx.states, ctx.launch, ctx.c, ckpt, ctx.tissue,
+                                     need[3:10], grad_out, *inputs)
+        out = [None, None, None]
+        out += [g if n else None for g, n in zip(grads, need[3:10], strict=True)]
+        return tuple(out)
+
+
+VJP_NAMES = ("t1_ms", "t2_ms", "m0", "b1", "inversion", "flip_rad", "duration_s")
+
+
+class EpgVjpFunction(torch.autograd.Function):
+    """The adjoint kernel as a differentiable function of the seed and the
+    inputs: forward gives the first-order gradients (t1, t2, m0, b1,
+    inversion per voxel; flip, duration per event); backward, for directions
+    ``v`` on those gradients, gives ``d<v, J^T w>/dw = J v`` (the forward
+    tangent of the sweep along ``v``) and ``d<v, J^T w>/d(inputs)`` (the
+    curvature of ``<w, J v>``), both from one forward-with-trajectory and one
+    reverse of the second-order sweep. This is the reference's second
+    backward through ``_NativeEpg`` (``_run_packed_vjp_jvp`` with the
+    gradients' cotangents as the direction, sequence/_accelerators.py:
+    1649-1735). Zero-duration events, folded into the op before them, carry no
+    duration gradient of either order."""
+
+    @staticmethod
+    def forward(ctx, program, states, launch, c, ckpt, tissue, want, grad_out, t1, t2, m0, b1,
+                inv, flip_events, duration_events):
         dev = grad_out.device
         V = tissue.voxels
         grads: dict[str, torch.Tensor] = {}
-        names = ("t1_ms", "t2_ms", "m0", "b1", "inversion")
-        for k, name in enumerate(names):
-            if need[3 + k]:
-                grads[name] = torch.zeros(V, dtype=torch.float32, device=dev)
         ev_shape = (program.trains, program.events.events)
-        if need[8]:
-            grads["flip_rad"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
-        if need[9]:
-            grads["duration_s"] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
-        adjoint(program, tissue, ctx.states, grad_out, ckpt, ctx.c, grads, launch=ctx.launch)
-        out = [None, None, None]
-        out += [grads.get(n) for n in names]
-        out += [grads.get("flip_rad"), grads.get("duration_s")]
+        for name, w in zip(VJP_NAMES, want, strict=True):
+            if w:
+                shape = ev_shape if name in ("flip_rad", "duration_s") else (V,)
+                grads[name] = torch.zeros(shape, dtype=torch.float32, device=dev)
+        adjoint(program, tissue, states, grad_out.detach(), ckpt, c, grads, launch=launch)
+        ctx.program, ctx.states, ctx.launch, ctx.tissue = program, states, launch, tissue
+        ctx.save_for_backward(grad_out)
+        out = []
+        for name in VJP_NAMES:
+            g = grads.get(name)
+            shape = ev_shape if name in ("flip_rad", "duration_s") else (V,)
+            out.append(g if g is not None else torch.zeros(shape, dtype=torch.float32, device=dev))
         return tuple(out)
+
+    @staticmethod
+    def backward(ctx, *vs):
+        (grad_out,) = ctx.saved_tensors
+        program, tissue, states = ctx.program, ctx.tissue, ctx.states
+        dev = grad_out.device
+        present = {"m0": tissue.m0 is not None, "b1": tissue.b1 is not None,
+                   "inversion": tissue.inv is not None}
+        direction = {}
+        for name, v in zip(VJP_NAMES, vs, strict=True):
+            if v is None or not present.get(name, True):
+                continue
+            direction[name] = v.detach().to(torch.float32).contiguous()
+        need = ctx.needs_input_grad  # program, states, launch, c, ckpt, tissue, want, grad_out, ...
+        if not direction:
+            return (None,) * len(need)
+        sig, jac, traj, ws = second_forward(program, tissue, states, [direction], launch=launch_of(ctx))
+        curvature = {}
+        V = tissue.voxels
+        ev_shape = (program.trains, program.events.events)
+        for i, name in enumerate(VJP_NAMES):
+            if need[8 + i]:
+                shape = ev_shape if name in ("flip_rad", "duration_s") else (V,)
+                curvature[name] = torch.zeros(shape, dtype=torch.float32, device=dev)
+        second_reverse(program, tissue, states, [direction], grad_out.detach()[:, None, :], traj, ws,
+                       curvature=curvature, launch=launch_of(ctx))
+        out = [None] * 7
+        out.append(jac[:, 0] if need[7] else None)
+        out += [curvature.get(n) for n in VJP_NAMES]
+        return tuple(out)
+
+
+def launch_of(ctx):
+    """The second-order sweeps pick their own launch shape."""
+    return None
