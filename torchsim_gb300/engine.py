@@ -865,10 +865,9 @@ class EpgVjpFunction(torch.autograd.Function):
     ``v`` on those gradients, gives ``d<v, J^T w>/dw = J v`` (the forward
     tangent of the sweep along ``v``) and ``d<v, J^T w>/d(inputs)`` (the
     curvature of ``<w, J v>``), both from one forward-with-trajectory and one
-    reverse of the second-order sweep. This is the reference's second
-    backward through ``_NativeEpg`` (``_run_packed_vjp_jvp`` with the
-    gradients' cotangents as the direction, sequence/_accelerators.py:
-    1649-1735). Zero-duration events, folded into the op before them, carry no
+    reverse of the second-order sweep. This is the reference's
+    ``_NativeEpgVjp.backward`` (``_run_packed_vjp_jvp`` with the gradients'
+    cotangents as the direction, sequence/_accelerators.py:1597-1735). Zero-duration events, folded into the op before them, carry no
     duration gradient of either order."""
 
     @staticmethod
