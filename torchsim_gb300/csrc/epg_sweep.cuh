@@ -8,10 +8,14 @@
 // in float2 registers and does the relaxation and the RF rotation of two
 // orders with one paired FP32 instruction (__ffma2_rn / __fmul2_rn): the
 // recursion is issue-bound, and pairing halves the arithmetic instructions.
-// The gradient shift moves F+ one order up and F- one order down: within a
-// lane that is a register move, across lanes a warp shuffle. The program
-// (ops) is staged in shared memory and read as a broadcast, since every
-// voxel of a block follows the same train.
+// Pairs are strided: the lane's local order l (0 <= l < R) sits in pair
+// l % RP, in .x for l < RP and in .y above. The gradient shift moves F+ one
+// order up and F- one order down; with strided pairs that moves whole pairs
+// (pair k takes pair k - 1, or k + 1) except one pair at the lane's edge, so
+// where a shift directly follows the rotation the moves fold into the
+// rotation's own results. Across lanes the shift is a warp shuffle. The
+// program (ops) is staged in shared memory and read as a broadcast, since
+// every voxel of a block follows the same train.
 //
 // Semantics follow the reference's real-subspace kernels: relaxation with
 // recovery, the real 3x3 RF rotation in alpha = flip*B1, inversion Z *= -eff,
@@ -43,13 +47,22 @@ __device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-// One gradient shift of a (F+, F-) pair of order-pair arrays spread over L
-// lanes: F- moves one order down (the top order takes what the next lane
-// held, or nothing at the voxel's top), then F+ one order up with
-// F+[0] = -F-[0] at the voxel's first lane.
+// The lane's local order l of a strided pair array (l a compile-time index
+// after unrolling).
+template <int RP>
+__device__ __forceinline__ float order_at(const float2 (&a)[RP], int l) {
+    return l < RP ? a[l % RP].x : a[l % RP].y;
+}
+
+// One gradient shift of a (F+, F-) pair of strided order-pair arrays spread
+// over L lanes: F- moves one order down (the top order takes what the next
+// lane held at its order 0, or nothing at the voxel's top), then F+ one order
+// up with F+[0] = -F-[0] at the voxel's first lane. `kill_k` (or -1) and
+// `kill_hi` name the slot of order `states`, cleared after the shift: the
+// only way into the orders past the kept ones is F+ moving up.
 template <int RP, int L>
-__device__ __forceinline__ void shift_pair(float2 (&p)[RP], float2 (&m)[RP], int q, bool kill,
-                                           int kill_r) {
+__device__ __forceinline__ void shift_pair(float2 (&p)[RP], float2 (&m)[RP], int q, int kill_k,
+                                           bool kill_hi) {
     float in_p = 0.f, in_m = 0.f;
     if constexpr (L > 1) {
         in_p = __shfl_up_sync(0xffffffffu, p[RP - 1].y, 1);
@@ -57,25 +70,21 @@ __device__ __forceinline__ void shift_pair(float2 (&p)[RP], float2 (&m)[RP], int
     }
     float top = 0.f;
     if constexpr (L > 1) top = (q == L - 1) ? 0.f : in_m;
+    const float m_edge = m[0].y;
 #pragma unroll
-    for (int k = 0; k < RP; ++k) {
-        m[k].x = m[k].y;
-        m[k].y = (k + 1 < RP) ? m[k + 1].x : top;
-    }
+    for (int k = 0; k + 1 < RP; ++k) m[k] = m[k + 1];
+    m[RP - 1] = make_float2(m_edge, top);
     float bottom = -m[0].x;
     if constexpr (L > 1) bottom = (q == 0) ? -m[0].x : in_p;
+    const float p_edge = p[RP - 1].x;
 #pragma unroll
-    for (int k = RP - 1; k >= 0; --k) {
-        p[k].y = p[k].x;
-        p[k].x = (k > 0) ? p[k - 1].y : bottom;
-    }
-    // Orders at and above `states` stay empty: the only way in is F+ moving
-    // up from the top kept order, so that one slot is cleared after a shift.
-    if (kill) {
+    for (int k = RP - 1; k > 0; --k) p[k] = p[k - 1];
+    p[0] = make_float2(bottom, p_edge);
 #pragma unroll
-        for (int k = 0; k < RP; ++k) {
-            if (2 * k == kill_r) p[k].x = 0.f;
-            if (2 * k + 1 == kill_r) p[k].y = 0.f;
+    for (int k = 0; k < RP; ++k) {
+        if (k == kill_k) {
+            if (kill_hi) p[k].y = 0.f;
+            else p[k].x = 0.f;
         }
     }
 }
@@ -91,12 +100,32 @@ __device__ __forceinline__ void put_sample(int layout, float* a, float* b, int64
     }
 }
 
+// Whether the relaxation-folded tangent step fits the register budget of a
+// launch with at least `minb` blocks of 128 threads per SM: it holds about
+// 16 + RP (18 + 12 NT) registers (124 at RP 2, NT 3; 70 at RP 1, NT 3, by
+// ptxas), against 65536 / (128 minb) a thread.
+constexpr bool fold_fits(int rp, int nt, int minb) {
+    return minb <= 1 || 65536 / (128 * minb) >= 16 + rp * (18 + 12 * nt);
+}
+
+// The op shape of an MRF repetition and of most spoiled sequences: relax,
+// rotate, (record), one shift after, and nothing else. It takes a
+// straight-line path with the shift folded into the rotation's results.
+constexpr uint32_t kFastMask = OP_RELAX | (3u << OP_SHIFT1_SHIFT) | (3u << OP_RF_SHIFT) |
+                               (3u << OP_SHIFT2_SHIFT) | OP_SPOIL1 | (3u << OP_SHIFT3_SHIFT) |
+                               OP_SPOIL2;
+constexpr uint32_t kFastBits = OP_RELAX | (uint32_t(RF_ROTATE) << OP_RF_SHIFT) |
+                               (1u << OP_SHIFT3_SHIFT);
+
 template <int RP, int L, int TM, bool GEN, bool GN = false, int MINB = 1>
 __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(const SweepArgs a) {
     using S = SystemLayout<TM, GEN>;
     constexpr int NT = S::N;
     constexpr int R = 2 * RP;
     constexpr int VPW = 32 / L;
+    // Relaxation folded into the rotation: always for the signal alone;
+    // with tangents where the register budget holds it.
+    constexpr bool FOLD = NT == 0 || (!GEN && fold_fits(RP, NT, MINB));
     __shared__ Op s_ops[kOpChunk];
     __shared__ float2 s_dir[GEN ? kOpChunk : 1];
 
@@ -129,8 +158,12 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
         g_inv = (a.g_inv && a.inv) ? a.g_inv[ac] : 0.f;
     }
 
-    const bool kill = L * R > a.states;
+    // The slot of order `states` in this lane, if the lane holds it and
+    // the lanes hold more orders than are kept.
     const int kill_r = a.states - q * R;
+    const bool kill = L * R > a.states && kill_r >= 0 && kill_r < R;
+    const int kill_k = kill ? kill_r % RP : -1;
+    const bool kill_hi = kill_r >= RP;
     const float2 neg1 = dup(-1.f);
 
     float2 P[RP], M[RP], Z[RP];
@@ -174,6 +207,280 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     // them with a shuffle, so each lane evaluates one sincosf per L pulses.
     float my_si = 0.f, my_co = 1.f;
     const int first_lane = lane - q;
+    float ddt = 0.f, dfl = 0.f;
+
+    auto pulse = [&](const Op& op, int g, float& si, float& co) {
+        if constexpr (L > 1) {
+            si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
+            co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
+        } else {
+            sincosf(op.flip * b1, &si, &co);
+        }
+    };
+
+    // Relaxation and rotation in one 3x3 per order for the signal alone,
+    // with the recovery of order 0 added after.
+    auto fold_signal = [&](float si, float co) {
+        const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
+        const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
+        const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
+        const float2 czp = dup(hs * e2), czz = dup(co * e1);
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            const float2 p = P[k], m = M[k], z = Z[k];
+            const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
+            P[k] = fma2(cpp, p, fma2(cpm, m, nt));
+            M[k] = fma2(cpm, p, fma2(cpp, m, t));
+            Z[k] = fma2(czp, fma2(neg1, m, p), mul2(czz, z));
+        }
+        if (q == 0) {
+            const float rec = 1.f - e1;
+            P[0].x = fmaf(-si, rec, P[0].x);
+            M[0].x = fmaf(si, rec, M[0].x);
+            Z[0].x = fmaf(co, rec, Z[0].x);
+        }
+    };
+
+    // Relaxation folded into the rotation for the signal and every tangent:
+    // with X0 the state before the interval, X = E X0 + r and dX = E dX0 +
+    // dE X0 (+ dr), so the pulse acts through R E on X0, on dX0 + E^-1 dE X0
+    // (T2 adds dt w2 (p, m), T1 dt w1 z), and the recovery r and its T1
+    // derivative enter order 0 after the fact.
+    auto fold_tangents = [&](const Op& op, float si, float co) {
+        const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
+        const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
+        const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
+        const float2 czp = dup(hs * e2), czz = dup(co * e1);
+        const float2 cvw = dup(0.5f * co * e2);  // V = d(Zn)/d alpha
+        float at_b1 = 0.f;
+        if constexpr (S::B1) at_b1 = op.flip;
+        const float2 g1 = dup(op.dt * w1), g2 = dup(op.dt * w2);
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            const float2 p = P[k], m = M[k], z = Z[k];
+            const float2 w = fma2(neg1, m, p);
+            const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
+            const float2 Pn = fma2(cpp, p, fma2(cpm, m, nt));
+            const float2 Mn = fma2(cpm, p, fma2(cpp, m, t));
+            const float2 Zn = fma2(czp, w, mul2(czz, z));
+            float2 V = dup(0.f);
+            if constexpr (S::B1) V = fma2(cvw, w, nt);
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
+                if (S::T1 && j == S::I_T1) dz = fma2(g1, z, dz);
+                if (S::T2 && j == S::I_T2) {
+                    dp = fma2(g2, p, dp);
+                    dm = fma2(g2, m, dm);
+                }
+                const float2 dt_ = mul2(cpz, dz), ndt = mul2(ncpz, dz);
+                float2 np = fma2(cpp, dp, fma2(cpm, dm, ndt));
+                float2 nm = fma2(cpm, dp, fma2(cpp, dm, dt_));
+                float2 nz = fma2(czp, fma2(neg1, dm, dp), mul2(czz, dz));
+                if (S::B1 && j == S::I_B1) {
+                    // d alpha / d B1 = flip: (-Zn, Zn, V) of the relaxed state.
+                    np = fma2(dup(-at_b1), Zn, np);
+                    nm = fma2(dup(at_b1), Zn, nm);
+                    nz = fma2(dup(at_b1), V, nz);
+                }
+                dP[j][k] = np;
+                dM[j][k] = nm;
+                dZ[j][k] = nz;
+            }
+            P[k] = Pn;
+            M[k] = Mn;
+            Z[k] = Zn;
+        }
+        if (q == 0) {
+            // The recovery (1 - e1) of order 0 and its T1 derivative (-k1)
+            // through the pulse: R (0, 0, c) = (-si c, si c, co c); for B1
+            // the recovery also moves Zn (used above without it) and V by
+            // (co, -si) c.
+            const float rec = 1.f - e1;
+            if constexpr (S::B1) {
+                dP[S::I_B1][0].x = fmaf(-at_b1 * co, rec, dP[S::I_B1][0].x);
+                dM[S::I_B1][0].x = fmaf(at_b1 * co, rec, dM[S::I_B1][0].x);
+                dZ[S::I_B1][0].x = fmaf(-at_b1 * si, rec, dZ[S::I_B1][0].x);
+            }
+            if constexpr (S::T1) {
+                dP[S::I_T1][0].x = fmaf(si, k1, dP[S::I_T1][0].x);
+                dM[S::I_T1][0].x = fmaf(-si, k1, dM[S::I_T1][0].x);
+                dZ[S::I_T1][0].x = fmaf(-co, k1, dZ[S::I_T1][0].x);
+            }
+            P[0].x = fmaf(-si, rec, P[0].x);
+            M[0].x = fmaf(si, rec, M[0].x);
+            Z[0].x = fmaf(co, rec, Z[0].x);
+        }
+    };
+
+    auto relax_all = [&](const Op& op) {
+        const float2 E1 = dup(e1), E2 = dup(e2);
+        float e1g = 0.f, e2g = 0.f;
+        if constexpr (GEN) {
+            e1g = e1 * (op.dt * g_t1 * w1 - r1 * ddt);
+            e2g = e2 * (op.dt * g_t2 * w2 - r2 * ddt);
+        }
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            if constexpr (S::T1) {
+                dP[S::I_T1][k] = mul2(dP[S::I_T1][k], E2);
+                dM[S::I_T1][k] = mul2(dM[S::I_T1][k], E2);
+                dZ[S::I_T1][k] = fma2(dZ[S::I_T1][k], E1, mul2(Z[k], dup(k1)));
+            }
+            if constexpr (S::T2) {
+                dP[S::I_T2][k] = fma2(dP[S::I_T2][k], E2, mul2(P[k], dup(k2)));
+                dM[S::I_T2][k] = fma2(dM[S::I_T2][k], E2, mul2(M[k], dup(k2)));
+                dZ[S::I_T2][k] = mul2(dZ[S::I_T2][k], E1);
+            }
+            if constexpr (S::B1) {
+                dP[S::I_B1][k] = mul2(dP[S::I_B1][k], E2);
+                dM[S::I_B1][k] = mul2(dM[S::I_B1][k], E2);
+                dZ[S::I_B1][k] = mul2(dZ[S::I_B1][k], E1);
+            }
+            if constexpr (S::INV) {
+                dP[S::I_INV][k] = mul2(dP[S::I_INV][k], E2);
+                dM[S::I_INV][k] = mul2(dM[S::I_INV][k], E2);
+                dZ[S::I_INV][k] = mul2(dZ[S::I_INV][k], E1);
+            }
+            if constexpr (GEN) {
+                dP[S::I_GEN][k] = fma2(dP[S::I_GEN][k], E2, mul2(P[k], dup(e2g)));
+                dM[S::I_GEN][k] = fma2(dM[S::I_GEN][k], E2, mul2(M[k], dup(e2g)));
+                dZ[S::I_GEN][k] = fma2(dZ[S::I_GEN][k], E1, mul2(Z[k], dup(e1g)));
+            }
+            P[k] = mul2(P[k], E2);
+            M[k] = mul2(M[k], E2);
+            Z[k] = mul2(Z[k], E1);
+        }
+        if (q == 0) {
+            Z[0].x += 1.f - e1;
+            if constexpr (S::T1) dZ[S::I_T1][0].x -= k1;
+            if constexpr (GEN) dZ[S::I_GEN][0].x -= e1g;
+        }
+    };
+
+    auto rotate_all = [&](const Op& op, float si, float co) {
+        const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
+        const float2 hs = dup(0.5f * si), hc = dup(0.5f * co);
+        const float2 si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
+        float at_b1 = 0.f, at_gen = 0.f;
+        if constexpr (S::B1) at_b1 = op.flip;
+        if constexpr (GEN) at_gen = dfl * b1 + op.flip * g_b1;
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            const float2 p = P[k], m = M[k], z = Z[k];
+            const float2 t = mul2(si2, z), nt = mul2(nsi2, z);
+            const float2 w = fma2(neg1, m, p);
+            const float2 Pn = fma2(ch, p, fma2(sh, m, nt));
+            const float2 Mn = fma2(sh, p, fma2(ch, m, t));
+            const float2 Zn = fma2(hs, w, mul2(co2, z));
+            // d/dalpha of the rotation: dP = -Zn, dM = Zn, dZ = V.
+            float2 V = dup(0.f);
+            if constexpr (S::B1 || GEN) V = fma2(hc, w, nt);
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                const float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
+                const float2 dt = mul2(si2, dz), ndt = mul2(nsi2, dz);
+                float2 np = fma2(ch, dp, fma2(sh, dm, ndt));
+                float2 nm = fma2(sh, dp, fma2(ch, dm, dt));
+                float2 nz = fma2(hs, fma2(neg1, dm, dp), mul2(co2, dz));
+                if ((S::B1 && j == S::I_B1) || (GEN && j == S::I_GEN)) {
+                    const float at = (S::B1 && j == S::I_B1) ? at_b1 : at_gen;
+                    np = fma2(dup(-at), Zn, np);
+                    nm = fma2(dup(at), Zn, nm);
+                    nz = fma2(dup(at), V, nz);
+                }
+                dP[j][k] = np;
+                dM[j][k] = nm;
+                dZ[j][k] = nz;
+            }
+            P[k] = Pn;
+            M[k] = Mn;
+            Z[k] = Zn;
+        }
+    };
+
+    auto shift_all = [&]() {
+        shift_pair<RP, L>(P, M, q, kill_k, kill_hi);
+#pragma unroll
+        for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill_k, kill_hi);
+    };
+
+    auto spoil_all = [&]() {
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            P[k] = M[k] = dup(0.f);
+#pragma unroll
+            for (int j = 0; j < NT; ++j) dP[j][k] = dM[j][k] = dup(0.f);
+        }
+    };
+
+    // The record of an op: the API samples m0 F+[0] of the signal and of
+    // each tangent column, or (GN sweeps) the voxel's normal-equation sums.
+    auto record = [&](const Op& op) {
+        if constexpr (GN) {
+            if (q == 0 && active) {
+                // API signal s = -v (v = m0 F+[0]); r = s - y. Columns of
+                // dv: T1, T2 (tangents), M0 (F+[0]); J^T J and J^T r carry
+                // the sign of s twice or not at all.
+                const float2 y = yrow[op.record];
+                const float p0 = P[0].x;
+                const float v = m0 * p0;
+                const float res = v + y.x;  // -(r.real)
+                const float j1 = m0 * dP[S::I_T1][0].x;
+                const float j2 = m0 * dP[S::I_T2][0].x;
+                const float j3 = p0;
+                cs[0] = fmaf(res, res, fmaf(y.y, y.y, cs[0]));
+                cs[1] = fmaf(j1, j1, cs[1]);
+                cs[2] = fmaf(j1, j2, cs[2]);
+                cs[3] = fmaf(j1, j3, cs[3]);
+                cs[4] = fmaf(j2, j2, cs[4]);
+                cs[5] = fmaf(j2, j3, cs[5]);
+                cs[6] = fmaf(j3, j3, cs[6]);
+                cs[7] = fmaf(j1, res, cs[7]);
+                cs[8] = fmaf(j2, res, cs[8]);
+                cs[9] = fmaf(j3, res, cs[9]);
+                if (++in_chunk == 32) {
+#pragma unroll
+                    for (int k = 0; k < 10; ++k) {
+                        cd[k] += double(cs[k]);
+                        cs[k] = 0.f;
+                    }
+                    in_chunk = 0;
+                }
+            }
+        } else if (q == 0 && active) {
+            const int rec = op.record;
+            const float p0 = P[0].x;
+            if constexpr (NT == 0 && !GEN)
+                if (a.traj_rec != nullptr) a.traj_rec[(train * a.outputs + rec) * a.atoms + atom] = p0;
+            if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
+                if (a.sig_a != nullptr || a.sig_b != nullptr)
+                    put_sample(a.layout, a.sig_a, a.sig_b, sig_base + rec, m0 * p0);
+            }
+            if constexpr (S::T1)
+                if (a.col_t1 >= 0)
+                    put_sample(a.layout, a.jac_a, a.jac_b, jbase + (a.col_t1 * a.outputs + rec),
+                               m0 * dP[S::I_T1][0].x);
+            if constexpr (S::T2)
+                if (a.col_t2 >= 0)
+                    put_sample(a.layout, a.jac_a, a.jac_b, jbase + (a.col_t2 * a.outputs + rec),
+                               m0 * dP[S::I_T2][0].x);
+            if constexpr (S::B1)
+                if (a.col_b1 >= 0)
+                    put_sample(a.layout, a.jac_a, a.jac_b, jbase + (a.col_b1 * a.outputs + rec),
+                               m0 * dP[S::I_B1][0].x);
+            if constexpr (S::INV)
+                if (a.col_inv >= 0)
+                    put_sample(a.layout, a.jac_a, a.jac_b, jbase + (a.col_inv * a.outputs + rec),
+                               m0 * dP[S::I_INV][0].x);
+            if constexpr (GEN)
+                if (a.col_gen >= 0)
+                    put_sample(a.layout, a.jac_a, a.jac_b, jbase + (a.col_gen * a.outputs + rec),
+                               fmaf(g_m0, p0, m0 * dP[S::I_GEN][0].x));
+            if (a.col_m0 >= 0)
+                put_sample(a.layout, a.jac_a, a.jac_b, jbase + (a.col_m0 * a.outputs + rec), p0);
+        }
+    };
 
     for (int base = 0; base < a.n_ops; base += kOpChunk) {
         const int count = min(kOpChunk, a.n_ops - base);
@@ -200,33 +507,28 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 }
             }
             if constexpr (NT == 0 && !GEN && !GN) {
-            if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
-                // State entering this op, for the adjoint's segments; atoms
-                // innermost, so a warp's stores of one order are contiguous.
-                const int k = (base + i) / a.ckpt_every;
-                const int Sn = a.states;
-                const int64_t n = a.atoms;
-                float* dst = a.ckpt + (train * a.ckpt_count + k) * (3 * int64_t(Sn)) * n + atom;
+                if (a.ckpt != nullptr && ((base + i) % a.ckpt_every) == 0 && active) {
+                    // State entering this op, for the adjoint's segments;
+                    // atoms innermost, so a warp's stores of one order are
+                    // contiguous.
+                    const int k = (base + i) / a.ckpt_every;
+                    const int Sn = a.states;
+                    const int64_t n = a.atoms;
+                    float* dst = a.ckpt + (train * a.ckpt_count + k) * (3 * int64_t(Sn)) * n + atom;
 #pragma unroll
-                for (int kk = 0; kk < RP; ++kk) {
-                    const int o = q * R + 2 * kk;
-                    if (o < Sn) {
-                        dst[o * n] = P[kk].x;
-                        dst[(Sn + o) * n] = M[kk].x;
-                        dst[(2 * Sn + o) * n] = Z[kk].x;
-                    }
-                    if (o + 1 < Sn) {
-                        dst[(o + 1) * n] = P[kk].y;
-                        dst[(Sn + o + 1) * n] = M[kk].y;
-                        dst[(2 * Sn + o + 1) * n] = Z[kk].y;
+                    for (int l = 0; l < R; ++l) {
+                        const int o = q * R + l;
+                        if (o < Sn) {
+                            dst[o * n] = order_at(P, l);
+                            dst[(Sn + o) * n] = order_at(M, l);
+                            dst[(2 * Sn + o) * n] = order_at(Z, l);
+                        }
                     }
                 }
-            }
-            }
-            if constexpr (NT == 0 && !GEN && !GN) {
                 if (a.traj != nullptr && active) {
-                    // Every op's entry state as this lane's order pairs, in
-                    // tiles of 32 atoms: [train][tile][op][plane][pair][32].
+                    // Every op's entry state as consecutive order pairs
+                    // (2 pj, 2 pj + 1), in tiles of 32 atoms:
+                    // [train][tile][op][plane][pair][32].
                     const int np = (a.states + 1) >> 1;
                     const int64_t tiles = (a.atoms + 31) >> 5;
                     float2* dst = a.traj +
@@ -237,14 +539,15 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                     for (int kk = 0; kk < RP; ++kk) {
                         const int pj = q * RP + kk;
                         if (pj < np) {
-                            dst[pj * 32] = P[kk];
-                            dst[(np + pj) * 32] = M[kk];
-                            dst[(2 * np + pj) * 32] = Z[kk];
+                            dst[pj * 32] = make_float2(order_at(P, 2 * kk), order_at(P, 2 * kk + 1));
+                            dst[(np + pj) * 32] =
+                                make_float2(order_at(M, 2 * kk), order_at(M, 2 * kk + 1));
+                            dst[(2 * np + pj) * 32] =
+                                make_float2(order_at(Z, 2 * kk), order_at(Z, 2 * kk + 1));
                         }
                     }
                 }
             }
-            float ddt = 0.f, dfl = 0.f;
             if constexpr (GEN) {
                 ddt = s_dir[i].x;
                 dfl = s_dir[i].y;
@@ -258,321 +561,54 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 k1 = e1 * (op.dt * w1);
                 k2 = e2 * (op.dt * w2);
             }
-            const int n1 = op_shift1(code);
-            if constexpr (NT == 0) {
-                if (relax && rf == RF_ROTATE && n1 == 0) {
-                    // Relaxation folded into the rotation: one 3x3 per order
-                    // with the recovery of order 0 added after.
+            if constexpr (!GEN) {
+                if ((code & kFastMask) == kFastBits) {
                     float si, co;
-                    if constexpr (L > 1) {
-                        si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
-                        co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
-                    } else {
-                        sincosf(op.flip * b1, &si, &co);
+                    pulse(op, g, si, co);
+                    if constexpr (NT == 0) fold_signal(si, co);
+                    else if constexpr (FOLD) fold_tangents(op, si, co);
+                    else {
+                        relax_all(op);
+                        rotate_all(op, si, co);
                     }
-                    const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
-                    const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
-                    const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
-                    const float2 czp = dup(hs * e2), czz = dup(co * e1);
-#pragma unroll
-                    for (int k = 0; k < RP; ++k) {
-                        const float2 p = P[k], m = M[k], z = Z[k];
-                        const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
-                        P[k] = fma2(cpp, p, fma2(cpm, m, nt));
-                        M[k] = fma2(cpm, p, fma2(cpp, m, t));
-                        Z[k] = fma2(czp, fma2(neg1, m, p), mul2(czz, z));
-                    }
-                    if (q == 0) {
-                        const float rec = 1.f - e1;
-                        P[0].x = fmaf(-si, rec, P[0].x);
-                        M[0].x = fmaf(si, rec, M[0].x);
-                        Z[0].x = fmaf(co, rec, Z[0].x);
-                    }
-                    goto after_rf;
+                    if (code & OP_RECORD) record(op);
+                    shift_all();
+                    continue;
                 }
             }
-            // The folded tangent step keeps more values live than the
-            // unfolded one; under a tight register budget (5 or more blocks
-            // per SM) the spills it causes cost more than it saves.
-            if constexpr (NT > 0 && !GEN && MINB < 5) {
-                if (relax && rf == RF_ROTATE && n1 == 0) {
-                    // Relaxation folded into the rotation for the primal and
-                    // every tangent: with X0 the state before the interval,
-                    // X = E X0 + r and dX = E dX0 + dE X0 (+ dr), so the pulse
-                    // acts through R E on X0, on dX0 + E^-1 dE X0 (T2 adds
-                    // dt w2 (p, m), T1 dt w1 z), and the recovery r and its
-                    // T1 derivative enter order 0 after the fact.
+            const int n1 = op_shift1(code);
+            if (FOLD && relax && rf == RF_ROTATE && n1 == 0) {
+                float si, co;
+                pulse(op, g, si, co);
+                if constexpr (NT == 0) fold_signal(si, co);
+                else if constexpr (FOLD) fold_tangents(op, si, co);
+            } else {
+                if (relax) relax_all(op);
+                for (int s = 0; s < n1; ++s) shift_all();
+                if (rf == RF_ROTATE) {
                     float si, co;
-                    if constexpr (L > 1) {
-                        si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
-                        co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
-                    } else {
-                        sincosf(op.flip * b1, &si, &co);
-                    }
-                    const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
-                    const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
-                    const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
-                    const float2 czp = dup(hs * e2), czz = dup(co * e1);
-                    const float2 cvw = dup(0.5f * co * e2);  // V = d(Zn)/d alpha
-                    float at_b1 = 0.f;
-                    if constexpr (S::B1) at_b1 = op.flip;
-                    const float2 g1 = dup(op.dt * w1), g2 = dup(op.dt * w2);
+                    pulse(op, g, si, co);
+                    rotate_all(op, si, co);
+                } else if (rf == RF_INVERT) {
+                    const float2 f = dup(-eff);
 #pragma unroll
                     for (int k = 0; k < RP; ++k) {
-                        const float2 p = P[k], m = M[k], z = Z[k];
-                        const float2 w = fma2(neg1, m, p);
-                        const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
-                        const float2 Pn = fma2(cpp, p, fma2(cpm, m, nt));
-                        const float2 Mn = fma2(cpm, p, fma2(cpp, m, t));
-                        const float2 Zn = fma2(czp, w, mul2(czz, z));
-                        float2 V = dup(0.f);
-                        if constexpr (S::B1) V = fma2(cvw, w, nt);
 #pragma unroll
                         for (int j = 0; j < NT; ++j) {
-                            float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
-                            if (S::T1 && j == S::I_T1) dz = fma2(g1, z, dz);
-                            if (S::T2 && j == S::I_T2) {
-                                dp = fma2(g2, p, dp);
-                                dm = fma2(g2, m, dm);
-                            }
-                            const float2 dt_ = mul2(cpz, dz), ndt = mul2(ncpz, dz);
-                            float2 np = fma2(cpp, dp, fma2(cpm, dm, ndt));
-                            float2 nm = fma2(cpm, dp, fma2(cpp, dm, dt_));
-                            float2 nz = fma2(czp, fma2(neg1, dm, dp), mul2(czz, dz));
-                            if (S::B1 && j == S::I_B1) {
-                                // d alpha / d B1 = flip: (-Zn, Zn, V) of the relaxed state.
-                                np = fma2(dup(-at_b1), Zn, np);
-                                nm = fma2(dup(at_b1), Zn, nm);
-                                nz = fma2(dup(at_b1), V, nz);
-                            }
-                            dP[j][k] = np;
-                            dM[j][k] = nm;
+                            float2 nz = mul2(dZ[j][k], f);
+                            if (S::INV && j == S::I_INV) nz = fma2(neg1, Z[k], nz);
+                            if (GEN && j == S::I_GEN) nz = fma2(Z[k], dup(-g_inv), nz);
                             dZ[j][k] = nz;
                         }
-                        P[k] = Pn;
-                        M[k] = Mn;
-                        Z[k] = Zn;
-                    }
-                    if (q == 0) {
-                        // The recovery (1 - e1) of order 0 and its T1
-                        // derivative (-k1) through the pulse: R (0, 0, c) =
-                        // (-si c, si c, co c); for B1 the recovery also moves
-                        // Zn (used above without it) and V by (co, -si) c.
-                        const float rec = 1.f - e1;
-                        if constexpr (S::B1) {
-                            dP[S::I_B1][0].x = fmaf(-at_b1 * co, rec, dP[S::I_B1][0].x);
-                            dM[S::I_B1][0].x = fmaf(at_b1 * co, rec, dM[S::I_B1][0].x);
-                            dZ[S::I_B1][0].x = fmaf(-at_b1 * si, rec, dZ[S::I_B1][0].x);
-                        }
-                        if constexpr (S::T1) {
-                            dP[S::I_T1][0].x = fmaf(si, k1, dP[S::I_T1][0].x);
-                            dM[S::I_T1][0].x = fmaf(-si, k1, dM[S::I_T1][0].x);
-                            dZ[S::I_T1][0].x = fmaf(-co, k1, dZ[S::I_T1][0].x);
-                        }
-                        P[0].x = fmaf(-si, rec, P[0].x);
-                        M[0].x = fmaf(si, rec, M[0].x);
-                        Z[0].x = fmaf(co, rec, Z[0].x);
-                    }
-                    goto after_rf;
-                }
-            }
-            if (relax) {
-                const float2 E1 = dup(e1), E2 = dup(e2);
-                float e1g = 0.f, e2g = 0.f;
-                if constexpr (GEN) {
-                    e1g = e1 * (op.dt * g_t1 * w1 - r1 * ddt);
-                    e2g = e2 * (op.dt * g_t2 * w2 - r2 * ddt);
-                }
-#pragma unroll
-                for (int k = 0; k < RP; ++k) {
-                    if constexpr (S::T1) {
-                        dP[S::I_T1][k] = mul2(dP[S::I_T1][k], E2);
-                        dM[S::I_T1][k] = mul2(dM[S::I_T1][k], E2);
-                        dZ[S::I_T1][k] = fma2(dZ[S::I_T1][k], E1, mul2(Z[k], dup(k1)));
-                    }
-                    if constexpr (S::T2) {
-                        dP[S::I_T2][k] = fma2(dP[S::I_T2][k], E2, mul2(P[k], dup(k2)));
-                        dM[S::I_T2][k] = fma2(dM[S::I_T2][k], E2, mul2(M[k], dup(k2)));
-                        dZ[S::I_T2][k] = mul2(dZ[S::I_T2][k], E1);
-                    }
-                    if constexpr (S::B1) {
-                        dP[S::I_B1][k] = mul2(dP[S::I_B1][k], E2);
-                        dM[S::I_B1][k] = mul2(dM[S::I_B1][k], E2);
-                        dZ[S::I_B1][k] = mul2(dZ[S::I_B1][k], E1);
-                    }
-                    if constexpr (S::INV) {
-                        dP[S::I_INV][k] = mul2(dP[S::I_INV][k], E2);
-                        dM[S::I_INV][k] = mul2(dM[S::I_INV][k], E2);
-                        dZ[S::I_INV][k] = mul2(dZ[S::I_INV][k], E1);
-                    }
-                    if constexpr (GEN) {
-                        dP[S::I_GEN][k] = fma2(dP[S::I_GEN][k], E2, mul2(P[k], dup(e2g)));
-                        dM[S::I_GEN][k] = fma2(dM[S::I_GEN][k], E2, mul2(M[k], dup(e2g)));
-                        dZ[S::I_GEN][k] = fma2(dZ[S::I_GEN][k], E1, mul2(Z[k], dup(e1g)));
-                    }
-                    P[k] = mul2(P[k], E2);
-                    M[k] = mul2(M[k], E2);
-                    Z[k] = mul2(Z[k], E1);
-                }
-                if (q == 0) {
-                    Z[0].x += 1.f - e1;
-                    if constexpr (S::T1) dZ[S::I_T1][0].x -= k1;
-                    if constexpr (GEN) dZ[S::I_GEN][0].x -= e1g;
-                }
-            }
-            for (int s = 0; s < n1; ++s) {
-                shift_pair<RP, L>(P, M, q, kill, kill_r);
-#pragma unroll
-                for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
-            }
-            if (rf == RF_ROTATE) {
-                float si, co;
-                if constexpr (L > 1) {
-                    si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
-                    co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
-                } else {
-                    sincosf(op.flip * b1, &si, &co);
-                }
-                const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
-                const float2 hs = dup(0.5f * si), hc = dup(0.5f * co);
-                const float2 si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
-                float at_b1 = 0.f, at_gen = 0.f;
-                if constexpr (S::B1) at_b1 = op.flip;
-                if constexpr (GEN) at_gen = dfl * b1 + op.flip * g_b1;
-#pragma unroll
-                for (int k = 0; k < RP; ++k) {
-                    const float2 p = P[k], m = M[k], z = Z[k];
-                    const float2 t = mul2(si2, z), nt = mul2(nsi2, z);
-                    const float2 w = fma2(neg1, m, p);
-                    const float2 Pn = fma2(ch, p, fma2(sh, m, nt));
-                    const float2 Mn = fma2(sh, p, fma2(ch, m, t));
-                    const float2 Zn = fma2(hs, w, mul2(co2, z));
-                    // d/dalpha of the rotation: dP = -Zn, dM = Zn, dZ = V.
-                    float2 V = dup(0.f);
-                    if constexpr (S::B1 || GEN) V = fma2(hc, w, nt);
-#pragma unroll
-                    for (int j = 0; j < NT; ++j) {
-                        const float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
-                        const float2 dt = mul2(si2, dz), ndt = mul2(nsi2, dz);
-                        float2 np = fma2(ch, dp, fma2(sh, dm, ndt));
-                        float2 nm = fma2(sh, dp, fma2(ch, dm, dt));
-                        float2 nz = fma2(hs, fma2(neg1, dm, dp), mul2(co2, dz));
-                        if ((S::B1 && j == S::I_B1) || (GEN && j == S::I_GEN)) {
-                            const float at = (S::B1 && j == S::I_B1) ? at_b1 : at_gen;
-                            np = fma2(dup(-at), Zn, np);
-                            nm = fma2(dup(at), Zn, nm);
-                            nz = fma2(dup(at), V, nz);
-                        }
-                        dP[j][k] = np;
-                        dM[j][k] = nm;
-                        dZ[j][k] = nz;
-                    }
-                    P[k] = Pn;
-                    M[k] = Mn;
-                    Z[k] = Zn;
-                }
-            } else if (rf == RF_INVERT) {
-                const float2 f = dup(-eff);
-#pragma unroll
-                for (int k = 0; k < RP; ++k) {
-#pragma unroll
-                    for (int j = 0; j < NT; ++j) {
-                        float2 nz = mul2(dZ[j][k], f);
-                        if (S::INV && j == S::I_INV) nz = fma2(neg1, Z[k], nz);
-                        if (GEN && j == S::I_GEN) nz = fma2(Z[k], dup(-g_inv), nz);
-                        dZ[j][k] = nz;
-                    }
-                    Z[k] = mul2(Z[k], f);
-                }
-            }
-        after_rf:
-            for (int s = 0; s < op_shift2(code); ++s) {
-                shift_pair<RP, L>(P, M, q, kill, kill_r);
-#pragma unroll
-                for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
-            }
-            if (code & OP_SPOIL1) {
-#pragma unroll
-                for (int k = 0; k < RP; ++k) {
-                    P[k] = M[k] = dup(0.f);
-#pragma unroll
-                    for (int j = 0; j < NT; ++j) dP[j][k] = dM[j][k] = dup(0.f);
-                }
-            }
-            if constexpr (GN) {
-                if ((code & OP_RECORD) && q == 0 && active) {
-                    // API signal s = -v (v = m0 F+[0]); r = s - y. Columns of
-                    // dv: T1, T2 (tangents), M0 (F+[0]); J^T J and J^T r
-                    // carry the sign of s twice or not at all.
-                    const float2 y = yrow[op.record];
-                    const float p0 = P[0].x;
-                    const float v = m0 * p0;
-                    const float res = v + y.x;  // -(r.real)
-                    const float j1 = m0 * dP[S::I_T1][0].x;
-                    const float j2 = m0 * dP[S::I_T2][0].x;
-                    const float j3 = p0;
-                    cs[0] = fmaf(res, res, fmaf(y.y, y.y, cs[0]));
-                    cs[1] = fmaf(j1, j1, cs[1]);
-                    cs[2] = fmaf(j1, j2, cs[2]);
-                    cs[3] = fmaf(j1, j3, cs[3]);
-                    cs[4] = fmaf(j2, j2, cs[4]);
-                    cs[5] = fmaf(j2, j3, cs[5]);
-                    cs[6] = fmaf(j3, j3, cs[6]);
-                    cs[7] = fmaf(j1, res, cs[7]);
-                    cs[8] = fmaf(j2, res, cs[8]);
-                    cs[9] = fmaf(j3, res, cs[9]);
-                    if (++in_chunk == 32) {
-#pragma unroll
-                        for (int k = 0; k < 10; ++k) {
-                            cd[k] += double(cs[k]);
-                            cs[k] = 0.f;
-                        }
-                        in_chunk = 0;
+                        Z[k] = mul2(Z[k], f);
                     }
                 }
             }
-            if ((code & OP_RECORD) && q == 0 && active && !GN) {
-                const int rec = op.record;
-                const float p0 = P[0].x;
-                if constexpr (NT == 0 && !GEN)
-                    if (a.traj_rec != nullptr)
-                        a.traj_rec[(train * a.outputs + rec) * a.atoms + atom] = p0;
-                if (a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) {
-                    if (a.sig_a != nullptr || a.sig_b != nullptr)
-                        put_sample(a.layout, a.sig_a, a.sig_b, sig_base + rec, m0 * p0);
-                }
-                if constexpr (S::T1)
-                    if (a.col_t1 >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_t1 * a.outputs + rec, m0 * dP[S::I_T1][0].x);
-                if constexpr (S::T2)
-                    if (a.col_t2 >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_t2 * a.outputs + rec, m0 * dP[S::I_T2][0].x);
-                if constexpr (S::B1)
-                    if (a.col_b1 >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_b1 * a.outputs + rec, m0 * dP[S::I_B1][0].x);
-                if constexpr (S::INV)
-                    if (a.col_inv >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_inv * a.outputs + rec,
-                                   m0 * dP[S::I_INV][0].x);
-                if constexpr (GEN)
-                    if (a.col_gen >= 0)
-                        put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_gen * a.outputs + rec,
-                                   fmaf(g_m0, p0, m0 * dP[S::I_GEN][0].x));
-                if (a.col_m0 >= 0) put_sample(a.layout, a.jac_a, a.jac_b, jbase + a.col_m0 * a.outputs + rec, p0);
-            }
-            for (int s = 0; s < op_shift3(code); ++s) {
-                shift_pair<RP, L>(P, M, q, kill, kill_r);
-#pragma unroll
-                for (int j = 0; j < NT; ++j) shift_pair<RP, L>(dP[j], dM[j], q, kill, kill_r);
-            }
-            if (code & OP_SPOIL2) {
-#pragma unroll
-                for (int k = 0; k < RP; ++k) {
-                    P[k] = M[k] = dup(0.f);
-#pragma unroll
-                    for (int j = 0; j < NT; ++j) dP[j][k] = dM[j][k] = dup(0.f);
-                }
-            }
+            for (int s = 0; s < op_shift2(code); ++s) shift_all();
+            if (code & OP_SPOIL1) spoil_all();
+            if (code & OP_RECORD) record(op);
+            for (int s = 0; s < op_shift3(code); ++s) shift_all();
+            if (code & OP_SPOIL2) spoil_all();
         }
     }
     if constexpr (GN) {

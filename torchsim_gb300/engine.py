@@ -299,7 +299,8 @@ FAMILY_SHAPES = {
 
 
 # (lanes, orders, min blocks per SM) register-budget variants per family.
-REGISTER_VARIANTS = {7: [(5, 4, 5), (5, 4, 6), (10, 2, 8), (4, 4, 6)]}
+REGISTER_VARIANTS = {7: [(5, 4, 5), (5, 4, 6), (10, 2, 8), (4, 4, 6), (5, 4, 4), (10, 2, 6),
+                         (10, 2, 7)]}
 
 
 def mode_of(names: Sequence[str]) -> int:
