@@ -46,6 +46,7 @@ struct SystemLayout {
 __device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
 // The lane's local order l of a strided pair array (l a compile-time index
 // after unrolling).
@@ -102,10 +103,55 @@ __device__ __forceinline__ void put_sample(int layout, float* a, float* b, int64
 
 // Whether the relaxation-folded tangent step fits the register budget of a
 // launch with at least `minb` blocks of 128 threads per SM: it holds about
-// 16 + RP (18 + 12 NT) registers (124 at RP 2, NT 3; 70 at RP 1, NT 3, by
-// ptxas), against 65536 / (128 minb) a thread.
+// 34 + RP (1 + 12 NT) registers (108 at RP 2, NT 3; 71 at RP 1, NT 3, by
+// ptxas), against 65536 / (128 minb) a thread. (At equal occupancy the
+// folded and unfolded steps measured alike on the dictionary sweep; beyond
+// the budget the folded one spills.)
 constexpr bool fold_fits(int rp, int nt, int minb) {
-    return minb <= 1 || 65536 / (128 * minb) >= 16 + rp * (18 + 12 * nt);
+    return minb <= 1 || 65536 / (128 * minb) >= 34 + rp * (1 + 12 * nt);
+}
+
+// The real rotation about x by alpha, scaled by the relaxation (E1 on Z,
+// E2 on F+ and F-; 1 and 1 for the rotation alone), in sum/difference form:
+// with s = p + m and d = p - m, A = E2 s / 2 and B = E2 cos(a) d / 2 -
+// E1 sin(a) z, the rotated state is p' = A + B, m' = A - B, z' = E2 sin(a)
+// d / 2 + E1 cos(a) z, and d/dalpha of (p', m', z') is (-z', z', B).
+struct Rotation {
+    float2 half_e2;  // E2 / 2
+    float2 hco;      // E2 cos / 2
+    float2 nsi;      // -E1 sin
+    float2 hsi;      // E2 sin / 2
+    float2 co;       // E1 cos
+};
+
+__device__ __forceinline__ Rotation rotation(float si, float co, float e1, float e2) {
+    const float h = 0.5f * e2;
+    return {dup(h), dup(h * co), dup(-e1 * si), dup(h * si), dup(e1 * co)};
+}
+
+// Rotates one pair of orders in place; leaves d and B for the derivative.
+__device__ __forceinline__ void rotate_pair(const Rotation& c, float2& p, float2& m, float2& z,
+                                            float2& d, float2& B) {
+    const float2 s = add2(p, m);
+    d = fma2(dup(-1.f), m, p);
+    const float2 A = mul2(c.half_e2, s);
+    B = fma2(c.hco, d, mul2(c.nsi, z));
+    p = add2(A, B);
+    m = fma2(dup(-1.f), B, A);
+    z = fma2(c.hsi, d, mul2(c.co, z));
+}
+
+// Rotates a tangent pair whose angle moves by `at` per unit: adds
+// at (-z', z', B) of the signal (z' its rotated Z, B from its rotation).
+__device__ __forceinline__ void rotate_pair_moved(const Rotation& c, float2& p, float2& m,
+                                                  float2& z, float at, float2 zs, float2 Bs) {
+    const float2 s = add2(p, m);
+    const float2 d = fma2(dup(-1.f), m, p);
+    const float2 A = mul2(c.half_e2, s);
+    const float2 B = fma2(dup(-at), zs, fma2(c.hco, d, mul2(c.nsi, z)));
+    p = add2(A, B);
+    m = fma2(dup(-1.f), B, A);
+    z = fma2(dup(at), Bs, fma2(c.hsi, d, mul2(c.co, z)));
 }
 
 // The op shape of an MRF repetition and of most spoiled sequences: relax,
@@ -221,17 +267,11 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     // Relaxation and rotation in one 3x3 per order for the signal alone,
     // with the recovery of order 0 added after.
     auto fold_signal = [&](float si, float co) {
-        const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
-        const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
-        const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
-        const float2 czp = dup(hs * e2), czz = dup(co * e1);
+        const Rotation c = rotation(si, co, e1, e2);
 #pragma unroll
         for (int k = 0; k < RP; ++k) {
-            const float2 p = P[k], m = M[k], z = Z[k];
-            const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
-            P[k] = fma2(cpp, p, fma2(cpm, m, nt));
-            M[k] = fma2(cpm, p, fma2(cpp, m, t));
-            Z[k] = fma2(czp, fma2(neg1, m, p), mul2(czz, z));
+            float2 d, B;
+            rotate_pair(c, P[k], M[k], Z[k], d, B);
         }
         if (q == 0) {
             const float rec = 1.f - e1;
@@ -247,49 +287,31 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     // (T2 adds dt w2 (p, m), T1 dt w1 z), and the recovery r and its T1
     // derivative enter order 0 after the fact.
     auto fold_tangents = [&](const Op& op, float si, float co) {
-        const float ch = 0.5f * (1.f + co), sh = 0.5f * (1.f - co), hs = 0.5f * si;
-        const float2 cpp = dup(ch * e2), cpm = dup(sh * e2);
-        const float2 cpz = dup(si * e1), ncpz = dup(-si * e1);
-        const float2 czp = dup(hs * e2), czz = dup(co * e1);
-        const float2 cvw = dup(0.5f * co * e2);  // V = d(Zn)/d alpha
+        const Rotation c = rotation(si, co, e1, e2);
         float at_b1 = 0.f;
         if constexpr (S::B1) at_b1 = op.flip;
         const float2 g1 = dup(op.dt * w1), g2 = dup(op.dt * w2);
 #pragma unroll
         for (int k = 0; k < RP; ++k) {
             const float2 p = P[k], m = M[k], z = Z[k];
-            const float2 w = fma2(neg1, m, p);
-            const float2 t = mul2(cpz, z), nt = mul2(ncpz, z);
-            const float2 Pn = fma2(cpp, p, fma2(cpm, m, nt));
-            const float2 Mn = fma2(cpm, p, fma2(cpp, m, t));
-            const float2 Zn = fma2(czp, w, mul2(czz, z));
-            float2 V = dup(0.f);
-            if constexpr (S::B1) V = fma2(cvw, w, nt);
+            float2 d, B;
+            rotate_pair(c, P[k], M[k], Z[k], d, B);
 #pragma unroll
             for (int j = 0; j < NT; ++j) {
-                float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
-                if (S::T1 && j == S::I_T1) dz = fma2(g1, z, dz);
+                if (S::T1 && j == S::I_T1) dZ[j][k] = fma2(g1, z, dZ[j][k]);
                 if (S::T2 && j == S::I_T2) {
-                    dp = fma2(g2, p, dp);
-                    dm = fma2(g2, m, dm);
+                    dP[j][k] = fma2(g2, p, dP[j][k]);
+                    dM[j][k] = fma2(g2, m, dM[j][k]);
                 }
-                const float2 dt_ = mul2(cpz, dz), ndt = mul2(ncpz, dz);
-                float2 np = fma2(cpp, dp, fma2(cpm, dm, ndt));
-                float2 nm = fma2(cpm, dp, fma2(cpp, dm, dt_));
-                float2 nz = fma2(czp, fma2(neg1, dm, dp), mul2(czz, dz));
                 if (S::B1 && j == S::I_B1) {
-                    // d alpha / d B1 = flip: (-Zn, Zn, V) of the relaxed state.
-                    np = fma2(dup(-at_b1), Zn, np);
-                    nm = fma2(dup(at_b1), Zn, nm);
-                    nz = fma2(dup(at_b1), V, nz);
+                    // d alpha / d B1 = flip: (-Zn, Zn, V) of the relaxed
+                    // state, V = B of the signal's rotation.
+                    rotate_pair_moved(c, dP[j][k], dM[j][k], dZ[j][k], at_b1, Z[k], B);
+                } else {
+                    float2 dd, dB;
+                    rotate_pair(c, dP[j][k], dM[j][k], dZ[j][k], dd, dB);
                 }
-                dP[j][k] = np;
-                dM[j][k] = nm;
-                dZ[j][k] = nz;
             }
-            P[k] = Pn;
-            M[k] = Mn;
-            Z[k] = Zn;
         }
         if (q == 0) {
             // The recovery (1 - e1) of order 0 and its T1 derivative (-k1)
@@ -359,43 +381,25 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     };
 
     auto rotate_all = [&](const Op& op, float si, float co) {
-        const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
-        const float2 hs = dup(0.5f * si), hc = dup(0.5f * co);
-        const float2 si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
+        const Rotation c = rotation(si, co, 1.f, 1.f);
         float at_b1 = 0.f, at_gen = 0.f;
         if constexpr (S::B1) at_b1 = op.flip;
         if constexpr (GEN) at_gen = dfl * b1 + op.flip * g_b1;
 #pragma unroll
         for (int k = 0; k < RP; ++k) {
-            const float2 p = P[k], m = M[k], z = Z[k];
-            const float2 t = mul2(si2, z), nt = mul2(nsi2, z);
-            const float2 w = fma2(neg1, m, p);
-            const float2 Pn = fma2(ch, p, fma2(sh, m, nt));
-            const float2 Mn = fma2(sh, p, fma2(ch, m, t));
-            const float2 Zn = fma2(hs, w, mul2(co2, z));
-            // d/dalpha of the rotation: dP = -Zn, dM = Zn, dZ = V.
-            float2 V = dup(0.f);
-            if constexpr (S::B1 || GEN) V = fma2(hc, w, nt);
+            // d/dalpha of the rotation: dP = -Zn, dM = Zn, dZ = V, V = B.
+            float2 d, B;
+            rotate_pair(c, P[k], M[k], Z[k], d, B);
 #pragma unroll
             for (int j = 0; j < NT; ++j) {
-                const float2 dp = dP[j][k], dm = dM[j][k], dz = dZ[j][k];
-                const float2 dt = mul2(si2, dz), ndt = mul2(nsi2, dz);
-                float2 np = fma2(ch, dp, fma2(sh, dm, ndt));
-                float2 nm = fma2(sh, dp, fma2(ch, dm, dt));
-                float2 nz = fma2(hs, fma2(neg1, dm, dp), mul2(co2, dz));
                 if ((S::B1 && j == S::I_B1) || (GEN && j == S::I_GEN)) {
                     const float at = (S::B1 && j == S::I_B1) ? at_b1 : at_gen;
-                    np = fma2(dup(-at), Zn, np);
-                    nm = fma2(dup(at), Zn, nm);
-                    nz = fma2(dup(at), V, nz);
+                    rotate_pair_moved(c, dP[j][k], dM[j][k], dZ[j][k], at, Z[k], B);
+                } else {
+                    float2 dd, dB;
+                    rotate_pair(c, dP[j][k], dM[j][k], dZ[j][k], dd, dB);
                 }
-                dP[j][k] = np;
-                dM[j][k] = nm;
-                dZ[j][k] = nz;
             }
-            P[k] = Pn;
-            M[k] = Mn;
-            Z[k] = Zn;
         }
     };
 
