@@ -248,6 +248,50 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     // Column offsets (col * outputs) are the same for every thread.
     const int64_t sig_base = row * a.outputs;
     const int64_t jbase = row * a.jac_cols * a.outputs;
+    // Distributed records: with at least as many lanes per voxel as output
+    // columns (the signal, each tangent's column in system order, M0), lane
+    // q of the voxel writes column q from its own row pointer, so one store
+    // instruction serves every column; the values come from lane 0 by
+    // shuffles. Otherwise lane 0 writes every column.
+    constexpr bool DIST = !GN && L >= NT + 2;
+    float* row_a = nullptr;  // this lane's column row: plane a, or the complex row
+    float* row_b = nullptr;  // plane b of the planes layout
+    if constexpr (DIST) {
+        float* base_a = nullptr;
+        float* base_b = nullptr;
+        int64_t off = 0;
+        int col = -1;
+        if (q >= 1 && q <= NT) {
+            const int j = q - 1;
+            if constexpr (S::T1) if (j == S::I_T1) col = a.col_t1;
+            if constexpr (S::T2) if (j == S::I_T2) col = a.col_t2;
+            if constexpr (S::B1) if (j == S::I_B1) col = a.col_b1;
+            if constexpr (S::INV) if (j == S::I_INV) col = a.col_inv;
+            if constexpr (GEN) if (j == S::I_GEN) col = a.col_gen;
+        } else if (q == NT + 1) {
+            col = a.col_m0;
+        }
+        if (q == 0) {
+            if ((a.sig_b != nullptr || a.layout != TSG_LAYOUT_PLANES) &&
+                (a.sig_a != nullptr || a.sig_b != nullptr)) {
+                base_a = a.sig_a;
+                base_b = a.sig_b;
+                off = sig_base;
+            }
+        } else if (col >= 0) {
+            base_a = a.jac_a;
+            base_b = a.jac_b;
+            off = jbase + int64_t(col) * a.outputs;
+        }
+        if (active && q <= NT + 1) {
+            if (a.layout == TSG_LAYOUT_PLANES) {
+                row_a = base_a ? base_a + off : nullptr;
+                row_b = base_b ? base_b + off : nullptr;
+            } else if (base_a) {
+                row_a = reinterpret_cast<float*>(reinterpret_cast<float2*>(base_a) + off);
+            }
+        }
+    }
     // Each pulse's sin/cos is the same for all L lanes of a voxel: lane q
     // computes it for one of the next L ops and the voxel's lanes exchange
     // them with a shuffle, so each lane evaluates one sincosf per L pulses.
@@ -451,6 +495,32 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                     }
                     in_chunk = 0;
                 }
+            }
+        } else if constexpr (DIST) {
+            const int rec = op.record;
+            const float p0 = __shfl_sync(0xffffffffu, P[0].x, first_lane);
+            if constexpr (NT == 0 && !GEN)
+                if (q == 0 && active && a.traj_rec != nullptr)
+                    a.traj_rec[(train * a.outputs + rec) * a.atoms + atom] = p0;
+            float v = m0 * p0;  // lane 0: the signal
+#pragma unroll
+            for (int j = 0; j < NT; ++j) {
+                const float d = __shfl_sync(0xffffffffu, dP[j][0].x, first_lane);
+                if (q == j + 1) {
+                    v = m0 * d;
+                    if constexpr (GEN)
+                        if (j == S::I_GEN) v = fmaf(g_m0, p0, v);
+                }
+            }
+            if (q == NT + 1) v = p0;  // the M0 column
+            if (a.layout == TSG_LAYOUT_PLANES) {
+                if (row_b != nullptr) {
+                    if (row_a != nullptr) __stcs(row_a + rec, 0.f);
+                    __stcs(row_b + rec, v);
+                }
+            } else if (row_a != nullptr) {
+                float2* dst = reinterpret_cast<float2*>(row_a) + rec;
+                __stcs(dst, a.layout == TSG_LAYOUT_COMPLEX ? make_float2(0.f, v) : make_float2(-v, 0.f));
             }
         } else if (q == 0 && active) {
             const int rec = op.record;
