@@ -302,6 +302,45 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
                                   lane * RP
                             : nullptr;
     const bool lane0 = active && q == 0;
+    // Distributed records: with 2K + 3 lanes per voxel or more, lane q of
+    // the voxel writes one output of a record from a pointer set up once
+    // (q = 0 the signal, 1..K the derivative columns, K + 1 the M0 column,
+    // K + 2 + s state s's recorded F+[0] for the reverse), the values coming
+    // from lane 0 by shuffle: one store instruction per record instead of up
+    // to 2K + 3 serial ones in lane 0.
+    constexpr bool DIST = L >= 2 * K + 3;
+    float* row_a = nullptr;    // this lane's output row: plane a, or the complex row
+    float* row_b = nullptr;    // plane b of the planes layout
+    float* rec_row = nullptr;  // this lane's recorded-F+[0] row of the trajectory
+    if constexpr (DIST) {
+        if (active) {
+            float* ba = nullptr;
+            float* bb = nullptr;
+            int64_t off = 0;
+            const int jc = K + a.with_m0;
+            if (q == 0) {
+                if (a.sig_a != nullptr || a.sig_b != nullptr) {
+                    ba = a.sig_a;
+                    bb = a.sig_b;
+                    off = row * a.outputs;
+                }
+            } else if (q <= K || (q == K + 1 && a.with_m0)) {
+                if (a.jac_a != nullptr || a.jac_b != nullptr) {
+                    ba = a.jac_a;
+                    bb = a.jac_b;
+                    off = (row * jc + (q - 1)) * a.outputs;
+                }
+            } else if (q >= K + 2 && q < K + 2 + NS && a.traj_rec != nullptr) {
+                rec_row = a.traj_rec + (train * a.outputs * NS + (q - K - 2)) * a.atoms + atom;
+            }
+            if (a.layout == TSG_LAYOUT_PLANES) {
+                row_a = ba ? ba + off : nullptr;
+                row_b = bb ? bb + off : nullptr;
+            } else if (ba) {
+                row_a = reinterpret_cast<float*>(reinterpret_cast<float2*>(ba) + off);
+            }
+        }
+    }
 
     for (int base = 0; base < a.n_ops; base += kOpChunk) {
         const int count = min(kOpChunk, a.n_ops - base);
@@ -381,7 +420,31 @@ __global__ void __launch_bounds__(128) second_forward_kernel(const SecondArgs a)
             }
             for (int s = 0; s < op_shift2(code); ++s) shift_all<RP, L, K>(P, M, q, kill, kill_r);
             if (code & OP_SPOIL1) spoil_all<RP, K>(P, M);
-            if ((code & OP_RECORD) && lane0) {
+            if (DIST && (code & OP_RECORD)) {
+                const int64_t rec = op.record;
+                const int first = lane - q;
+                const float p0 = __shfl_sync(0xffffffffu, P[0][0].x, first);
+                float val = v.m0 * p0;  // q = 0: the signal
+                float raw = p0;         // q = K + 2: state 0's recorded F+[0]
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const float d = __shfl_sync(0xffffffffu, P[k + 1][0].x, first);
+                    if (q == k + 1) val = HOT ? v.m0 * d : fmaf(v.m0, d, v.dm0[k] * p0);
+                    if (q == K + 3 + k) raw = d;
+                }
+                if (q == K + 1) val = p0;  // the M0 column
+                if (a.layout == TSG_LAYOUT_PLANES) {
+                    if (row_b != nullptr) {
+                        if (row_a != nullptr) row_a[rec] = 0.f;
+                        row_b[rec] = val;
+                    }
+                } else if (row_a != nullptr) {
+                    reinterpret_cast<float2*>(row_a)[rec] = a.layout == TSG_LAYOUT_COMPLEX
+                                                                ? make_float2(0.f, val)
+                                                                : make_float2(-val, 0.f);
+                }
+                if (rec_row != nullptr) rec_row[rec * NS * a.atoms] = raw;
+            } else if ((code & OP_RECORD) && lane0) {
                 const int64_t rec = op.record;
                 const float p0 = P[0][0].x;
                 if (a.sig_a != nullptr || a.sig_b != nullptr)
