@@ -66,6 +66,12 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
     const int64_t jac_base = row * a.jac_cols * a.outputs;
     float last_dt = __int_as_float(0x7fffffff);
     float e1 = 1.f, tr = 1.f, ti = 0.f, k1 = 0.f, k2f = 0.f;
+    // Each op's transcendentals are the same for the L lanes of a voxel:
+    // lane q evaluates them for one of the next L ops (the pulse's flip and
+    // phase, the receiver phase of a record) and the lanes exchange them by
+    // shuffle, so each lane evaluates one op's in L.
+    float my_sa = 0.f, my_ca = 1.f, my_sp = 0.f, my_cp = 1.f, my_sr = 0.f, my_cr = 1.f;
+    const int first_lane = lane - q;
 
     for (int base = 0; base < a.n_ops; base += kComplexOpChunk) {
         const int count = min(kComplexOpChunk, a.n_ops - base);
@@ -78,6 +84,27 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
         for (int i = 0; i < count; ++i) {
             const Op op = s_ops[i];
             const uint32_t code = op.code;
+            const int g = i % L;
+            if constexpr (L > 1) {
+                if (g == 0) {
+                    const int j = i + q;
+                    float sa = 0.f, ca = 1.f, sp = 0.f, cp = 1.f, sr = 0.f, cr = 1.f;
+                    if (j < count) {
+                        const uint32_t cj = s_ops[j].code;
+                        if (op_rf(cj) == RF_ROTATE) {
+                            sincosf(s_ops[j].flip * b1, &sa, &ca);
+                            sincosf(s_ph[j].x + b1_phase, &sp, &cp);
+                        }
+                        if (cj & OP_RECORD) sincosf(s_ph[j].y, &sr, &cr);
+                    }
+                    my_sa = sa;
+                    my_ca = ca;
+                    my_sp = sp;
+                    my_cp = cp;
+                    my_sr = sr;
+                    my_cr = cr;
+                }
+            }
             if (code & OP_RELAX) {
                 if (op.dt != last_dt) {
                     last_dt = op.dt;
@@ -146,8 +173,16 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
             const int rf = op_rf(code);
             if (rf == RF_ROTATE) {
                 float sa, ca, sp, cp;
-                sincosf(op.flip * b1, &sa, &ca);
-                sincosf(s_ph[i].x + b1_phase, &sp, &cp);
+                if constexpr (L > 1) {
+                    const int src = first_lane + g;
+                    sa = __shfl_sync(0xffffffffu, my_sa, src);
+                    ca = __shfl_sync(0xffffffffu, my_ca, src);
+                    sp = __shfl_sync(0xffffffffu, my_sp, src);
+                    cp = __shfl_sync(0xffffffffu, my_cp, src);
+                } else {
+                    sincosf(op.flip * b1, &sa, &ca);
+                    sincosf(s_ph[i].x + b1_phase, &sp, &cp);
+                }
                 // e^{2i phi} from e^{i phi}.
                 const float c2 = cp * cp - sp * sp, s2 = 2.f * cp * sp;
                 const Pulse u = pulse_of(0.5f * (1.f + ca), ca, 0.5f * (1.f - ca), sa, 0.5f * sa,
@@ -211,10 +246,17 @@ __global__ void __launch_bounds__(256) epg_complex_kernel(const ComplexArgs a) {
                     for (int j = 0; j < NT; ++j) dPr[j][k] = dPi[j][k] = dMr[j][k] = dMi[j][k] = dup(0.f);
                 }
             }
+            float sr = 0.f, cr = 1.f;
+            if (code & OP_RECORD) {
+                if constexpr (L > 1) {
+                    sr = __shfl_sync(0xffffffffu, my_sr, first_lane + g);
+                    cr = __shfl_sync(0xffffffffu, my_cr, first_lane + g);
+                } else {
+                    sincosf(s_ph[i].y, &sr, &cr);
+                }
+            }
             if ((code & OP_RECORD) && q == 0 && active) {
                 // m0 F+[0] demodulated by the receiver phase, and its columns.
-                float sr, cr;
-                sincosf(s_ph[i].y, &sr, &cr);
                 const int rec = op.record;
                 auto demod = [&](float xr, float xi, float& yr, float& yi) {
                     yr = xr * cr + xi * sr;
