@@ -142,6 +142,37 @@ __device__ __forceinline__ void put(int layout, float* a, float* b, int64_t idx,
     }
 }
 
+// The transcendentals of one op for one voxel: the relaxation (e1, and the
+// F+ factor e2 e^{-i 2 pi B0 dt} as tr + i ti), the pulse (sin/cos of the
+// flip angle alpha = flip B1 and of the RF phase plus B1phase) and the
+// receiver phase of a record. Left at the identity where the op has no such
+// step.
+struct OpTrig {
+    float e1 = 1.f, tr = 1.f, ti = 0.f;
+    float sa = 0.f, ca = 1.f, sp = 0.f, cp = 1.f;
+    float sr = 0.f, cr = 1.f;
+};
+
+__device__ __forceinline__ OpTrig op_trig(const Op& op, float2 ph, float r1, float r2, float b1,
+                                          float b1_phase, float b0, bool off_axis) {
+    OpTrig t;
+    const uint32_t code = op.code;
+    if (code & OP_RELAX) {
+        t.e1 = expf(-r1 * op.dt);
+        const float e2 = expf(-r2 * op.dt);
+        float so = 0.f, co = 1.f;
+        if (off_axis) sincosf(-2.f * 3.14159265358979323846f * b0 * op.dt, &so, &co);
+        t.tr = e2 * co;
+        t.ti = e2 * so;
+    }
+    if (op_rf(code) == RF_ROTATE) {
+        sincosf(op.flip * b1, &t.sa, &t.ca);
+        sincosf(ph.x + b1_phase, &t.sp, &t.cp);
+    }
+    if (code & OP_RECORD) sincosf(ph.y, &t.sr, &t.cr);
+    return t;
+}
+
 }  // namespace complex_detail
 
 }  // namespace tsg

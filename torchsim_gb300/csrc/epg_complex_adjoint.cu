@@ -182,6 +182,13 @@ __global__ void __launch_bounds__(128) complex_forward_traj_kernel(const Complex
                             ? a.traj + (train * n_warps + warp_global) * a.n_ops * op_stride + lane * RP
                             : nullptr;
 
+    // Each op's transcendentals are the same for the L lanes of a voxel:
+    // lane q evaluates them for one of the next L ops and the lanes exchange
+    // them by shuffle.
+    const int first_lane = lane - q;
+    const bool off_axis = a.b0 != nullptr;
+    OpTrig mine;
+
     for (int base = 0; base < a.n_ops; base += kComplexOpChunk) {
         const int count = min(kComplexOpChunk, a.n_ops - base);
         __syncthreads();
@@ -193,6 +200,19 @@ __global__ void __launch_bounds__(128) complex_forward_traj_kernel(const Complex
         for (int i = 0; i < count; ++i) {
             const Op op = s_ops[i];
             const uint32_t code = op.code;
+            const int src = first_lane + i % L;
+            if constexpr (L > 1) {
+                if (i % L == 0) {
+                    const int j = i + q;
+                    mine = j < count ? op_trig(s_ops[j], s_ph[j], r1, r2, b1, b1_phase, b0, off_axis)
+                                     : OpTrig{};
+                }
+            } else {
+                mine = op_trig(op, s_ph[i], r1, r2, b1, b1_phase, b0, off_axis);
+            }
+            // This op's value of one field (shuffled where it is used, so the
+            // fields are live only there; every lane takes part).
+            auto tv = [&](float v) { return L > 1 ? __shfl_sync(0xffffffffu, v, src) : v; };
             if (lane_traj) {
                 float2* dst = lane_traj + int64_t(base + i) * op_stride;
 #pragma unroll
@@ -201,10 +221,8 @@ __global__ void __launch_bounds__(128) complex_forward_traj_kernel(const Complex
                     for (int k = 0; k < RP; ++k) dst[p * 32 * RP + k] = X[p][k];
             }
             if (code & OP_RELAX) {
-                const float e1 = expf(-r1 * op.dt), e2 = expf(-r2 * op.dt);
-                float so = 0.f, co = 1.f;
-                if (a.b0) sincosf(-2.f * 3.14159265358979323846f * b0 * op.dt, &so, &co);
-                const float2 T = dup(e2 * co), Ti = dup(e2 * so), nTi = dup(-e2 * so), E1 = dup(e1);
+                const float e1 = tv(mine.e1), tr = tv(mine.tr), ti = tv(mine.ti);
+                const float2 T = dup(tr), Ti = dup(ti), nTi = dup(-ti), E1 = dup(e1);
 #pragma unroll
                 for (int k = 0; k < RP; ++k) {
                     const float2 pr = X[0][k], pi = X[1][k], mr = X[2][k], mi = X[3][k];
@@ -221,9 +239,7 @@ __global__ void __launch_bounds__(128) complex_forward_traj_kernel(const Complex
                 shift_complex<RP, L>(X[0], X[1], X[2], X[3], q, kill, kill_r);
             const int rf = op_rf(code);
             if (rf == RF_ROTATE) {
-                float sa, ca, sp, cp;
-                sincosf(op.flip * b1, &sa, &ca);
-                sincosf(s_ph[i].x + b1_phase, &sp, &cp);
+                const float sa = tv(mine.sa), ca = tv(mine.ca), sp = tv(mine.sp), cp = tv(mine.cp);
                 const float c2 = cp * cp - sp * sp, s2 = 2.f * cp * sp;
                 const Pulse u = pulse_of(0.5f * (1.f + ca), ca, 0.5f * (1.f - ca), sa, 0.5f * sa,
                                          c2, s2, cp, sp);
@@ -245,9 +261,12 @@ __global__ void __launch_bounds__(128) complex_forward_traj_kernel(const Complex
 #pragma unroll
                 for (int k = 0; k < RP; ++k) X[0][k] = X[1][k] = X[2][k] = X[3][k] = dup(0.f);
             }
+            float sr = 0.f, cr = 1.f;
+            if (code & OP_RECORD) {
+                sr = tv(mine.sr);
+                cr = tv(mine.cr);
+            }
             if ((code & OP_RECORD) && q == 0 && active) {
-                float sr, cr;
-                sincosf(s_ph[i].y, &sr, &cr);
                 const float xr = X[0][0].x, xi = X[1][0].x;
                 a.traj_rec[(train * a.outputs + op.record) * a.atoms + atom] = make_float2(xr, xi);
                 if (a.out_a)
@@ -274,8 +293,11 @@ __device__ __forceinline__ float2 dot_acc(const float2 (&y)[RP], const float2 (&
 
 // The reverse sweep. Dynamic shared memory: the entry-state ring
 // [D][6][T][RP] float2, then the ops [n_ops] and their phases [n_ops].
+// Two orders per lane (the default shapes) hold the reverse step in 96
+// registers, ten blocks per SM; four orders per lane take what they need.
 template <int RP, int L>
-__global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const ComplexAdjointArgs a) {
+__global__ void __launch_bounds__(32 * kCxWarps, RP == 1 ? 10 : 1)
+    complex_adjoint_kernel(const ComplexAdjointArgs a) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     constexpr int W = kCxWarps;
     constexpr int T = 32 * W;
@@ -366,6 +388,12 @@ __global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const Co
     }
     float2* event_out = a.event_partial + (train * a.warps_per_train + warp_global) * int64_t(n_ops) * 2;
     int use_slot = 0, fill_slot = D - 1;
+    // Each op's transcendentals, evaluated once per voxel: lane q takes one
+    // of the next L ops of the reverse sweep (op o - q) and the lanes
+    // exchange them by shuffle.
+    const int first_lane = lane - q;
+    const bool off_axis = a.b0 != nullptr;
+    OpTrig mine;
 
     for (int o = n_ops - 1; o >= 0; --o) {
         if (o - (D - 1) >= 0) fetch(o - (D - 1), fill_slot);
@@ -374,6 +402,20 @@ __global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const Co
         const Op op = s_ops[o];
         const float2 ph = s_ph[o];
         const uint32_t code = op.code;
+        const int g = (n_ops - 1 - o) % L;
+        const int src = first_lane + g;
+        if constexpr (L > 1) {
+            if (g == 0) {
+                const int j = o - q;
+                mine = j >= 0 ? op_trig(s_ops[j], s_ph[j], r1, r2, b1, b1_phase, b0, off_axis)
+                              : OpTrig{};
+            }
+        } else {
+            mine = op_trig(op, ph, r1, r2, b1, b1_phase, b0, off_axis);
+        }
+        // This op's value of one field (shuffled where it is used, so the
+        // fields are live only there; every lane takes part).
+        auto tv = [&](float v) { return L > 1 ? __shfl_sync(0xffffffffu, v, src) : v; };
         asm volatile("cp.async.wait_group %0;\n" ::"n"(D - 1) : "memory");
         const float2* ring = s_ring + use_slot * (6 * T * RP) + threadIdx.x * RP;
         use_slot = use_slot + 1 == D ? 0 : use_slot + 1;
@@ -387,12 +429,9 @@ __global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const Co
         const bool relax = (code & OP_RELAX) != 0;
         float e1 = 1.f, tr = 1.f, ti = 0.f;
         if (relax) {
-            e1 = expf(-r1 * op.dt);
-            const float e2 = expf(-r2 * op.dt);
-            float so = 0.f, co = 1.f;
-            if (a.b0) sincosf(-kTwoPi * b0 * op.dt, &so, &co);
-            tr = e2 * co;
-            ti = e2 * so;
+            e1 = tv(mine.e1);
+            tr = tv(mine.tr);
+            ti = tv(mine.ti);
             const float2 Tr = dup(tr), Ti = dup(ti), nTi = dup(-ti), E1 = dup(e1);
 #pragma unroll
             for (int k = 0; k < RP; ++k) {
@@ -417,6 +456,11 @@ __global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const Co
         for (int s = 0; s < op_shift3(code); ++s)
             shift_complex_adjoint<RP, L>(B[0], B[1], B[2], B[3], q, kill, kill_r);
         float e_rec = 0.f;  // this lane's d/d(receiver phase)
+        float sr = 0.f, cr = 1.f;
+        if (code & OP_RECORD) {
+            sr = tv(mine.sr);
+            cr = tv(mine.cr);
+        }
         if ((code & OP_RECORD) && lane0) {
             const int64_t r = op.record;
             const int64_t idx = row * a.outputs + r;
@@ -430,8 +474,6 @@ __global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const Co
                 gi = gs.y;
             }
             const float2 x0 = rec_col[r * n];
-            float sr, cr;
-            sincosf(ph.y, &sr, &cr);
             // d = e^{-i phi_r}: x0 d, and v = m0 x0 d.
             const float fr = x0.x * cr + x0.y * sr, fi = x0.y * cr - x0.x * sr;
             g_m0 = fmaf(gr, fr, fmaf(gi, fi, g_m0));
@@ -451,9 +493,7 @@ __global__ void __launch_bounds__(32 * kCxWarps) complex_adjoint_kernel(const Co
         float e_flip = 0.f, e_rf = 0.f;
         const int rf = op_rf(code);
         if (rf == RF_ROTATE) {
-            float sa, ca, sp, cp;
-            sincosf(op.flip * b1, &sa, &ca);
-            sincosf(ph.x + b1_phase, &sp, &cp);
+            const float sa = tv(mine.sa), ca = tv(mine.ca), sp = tv(mine.sp), cp = tv(mine.cp);
             const float c2 = cp * cp - sp * sp, s2 = 2.f * cp * sp;
             const Pulse u = pulse_of(0.5f * (1.f + ca), ca, 0.5f * (1.f - ca), sa, 0.5f * sa, c2,
                                      s2, cp, sp);
