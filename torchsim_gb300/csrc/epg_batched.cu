@@ -22,35 +22,44 @@ __device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
-// One gradient shift of the lane's order pairs (orders 2k, 2k+1 in pair k)
-// with a per-sequence lane count L: F- moves one order down, F+ one order up,
-// F+[0] = -F-[0] on the voxel's first lane, nothing crosses a voxel's edge,
-// and the slot at order `states` is cleared (truncation).
+// One gradient shift of the lane's strided order pairs (local order l in
+// pair l % RP, .x below RP and .y above) with a per-sequence lane count L:
+// F- moves one order down, F+ one order up, F+[0] = -F-[0] on the voxel's
+// first lane, nothing crosses a voxel's edge, and the slot of order `states`
+// (kill_k, kill_hi; kill_k -1 where the lane has none) is cleared
+// (truncation). Whole pairs move except one at each edge.
 template <int RP>
 __device__ __forceinline__ void shift_pairs(float2 (&p)[RP], float2 (&m)[RP], int q, int L,
-                                            bool kill, int kill_r) {
+                                            int kill_k, bool kill_hi) {
     const float in_p = __shfl_up_sync(0xffffffffu, p[RP - 1].y, 1);
     const float in_m = __shfl_down_sync(0xffffffffu, m[0].x, 1);
     const float top = (q == L - 1) ? 0.f : in_m;
+    const float m_edge = m[0].y;
+#pragma unroll
+    for (int k = 0; k + 1 < RP; ++k) m[k] = m[k + 1];
+    m[RP - 1] = make_float2(m_edge, top);
+    const float bottom = (q == 0) ? -m[0].x : in_p;
+    const float p_edge = p[RP - 1].x;
+#pragma unroll
+    for (int k = RP - 1; k > 0; --k) p[k] = p[k - 1];
+    p[0] = make_float2(bottom, p_edge);
 #pragma unroll
     for (int k = 0; k < RP; ++k) {
-        m[k].x = m[k].y;
-        m[k].y = (k + 1 < RP) ? m[k + 1].x : top;
-    }
-    const float bottom = (q == 0) ? -m[0].x : in_p;
-#pragma unroll
-    for (int k = RP - 1; k >= 0; --k) {
-        p[k].y = p[k].x;
-        p[k].x = (k > 0) ? p[k - 1].y : bottom;
-    }
-    if (kill) {
-#pragma unroll
-        for (int k = 0; k < RP; ++k) {
-            if (2 * k == kill_r) p[k].x = 0.f;
-            if (2 * k + 1 == kill_r) p[k].y = 0.f;
+        if (k == kill_k) {
+            if (kill_hi) p[k].y = 0.f;
+            else p[k].x = 0.f;
         }
     }
 }
+
+// A refocusing op of a CPMG echo: relax, shift, rotate, shift, nothing else.
+// It takes a straight-line path in which the shifts' moves fold into the
+// relaxation's and the rotation's own results.
+constexpr uint32_t kEchoMask = OP_RELAX | (3u << OP_SHIFT1_SHIFT) | (3u << OP_RF_SHIFT) |
+                               (3u << OP_SHIFT2_SHIFT) | OP_SPOIL1 | OP_RECORD |
+                               (3u << OP_SHIFT3_SHIFT) | OP_SPOIL2;
+constexpr uint32_t kEchoBits = OP_RELAX | (1u << OP_SHIFT1_SHIFT) |
+                               (uint32_t(RF_ROTATE) << OP_RF_SHIFT) | (1u << OP_SHIFT2_SHIFT);
 
 }  // namespace
 
@@ -93,8 +102,10 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
         const float r1 = 1000.f / t1;
         const float r2 = 1000.f / t2;
         const int S = sq.states;
-        const bool kill = L * R > S;
         const int kill_r = S - q * R;
+        const bool kill = L * R > S && kill_r >= 0 && kill_r < R;
+        const int kill_k = kill ? kill_r % RP : -1;
+        const bool kill_hi = kill_r >= RP;
         float2 P[RP], M[RP], Z[RP];
 #pragma unroll
         for (int k = 0; k < RP; ++k) P[k] = M[k] = Z[k] = dup(0.f);
@@ -125,7 +136,7 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                 }
                 const Op op = s_ops[i];
                 const uint32_t code = op.code;
-                if (code & OP_RELAX) {
+                auto relax = [&]() {
                     if (op.dt != last_dt) {
                         last_dt = op.dt;
                         e1 = expf(-r1 * op.dt);
@@ -139,10 +150,8 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                         Z[k] = mul2(Z[k], E1);
                     }
                     if (q == 0) Z[0].x += 1.f - e1;
-                }
-                for (int s = 0; s < op_shift1(code); ++s) shift_pairs<RP>(P, M, q, L, kill, kill_r);
-                const int rf = op_rf(code);
-                if (rf == RF_ROTATE) {
+                };
+                auto rotate = [&]() {
                     const float si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
                     const float co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
                     const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
@@ -154,19 +163,33 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                         M[k] = fma2(sh, p, fma2(ch, m, mul2(si2, z)));
                         Z[k] = fma2(hs, fma2(neg1, m, p), mul2(co2, z));
                     }
+                };
+                if ((code & kEchoMask) == kEchoBits) {
+                    relax();
+                    shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                    rotate();
+                    ++g;
+                    shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                    continue;
+                }
+                if (code & OP_RELAX) relax();
+                for (int s = 0; s < op_shift1(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                const int rf = op_rf(code);
+                if (rf == RF_ROTATE) {
+                    rotate();
                 } else if (rf == RF_INVERT) {
 #pragma unroll
                     for (int k = 0; k < RP; ++k) Z[k] = mul2(Z[k], neg1);
                 }
                 ++g;
-                for (int s = 0; s < op_shift2(code); ++s) shift_pairs<RP>(P, M, q, L, kill, kill_r);
+                for (int s = 0; s < op_shift2(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
                 if (code & OP_SPOIL1) {
 #pragma unroll
                     for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
                 }
                 if ((code & OP_RECORD) && q == 0 && active)
                     __stcs(orow + op.record, make_float2(0.f, m0 * P[0].x));
-                for (int s = 0; s < op_shift3(code); ++s) shift_pairs<RP>(P, M, q, L, kill, kill_r);
+                for (int s = 0; s < op_shift3(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
                 if (code & OP_SPOIL2) {
 #pragma unroll
                     for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
