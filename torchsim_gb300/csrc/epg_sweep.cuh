@@ -162,6 +162,11 @@ constexpr uint32_t kFastMask = OP_RELAX | (3u << OP_SHIFT1_SHIFT) | (3u << OP_RF
                                OP_SPOIL2;
 constexpr uint32_t kFastBits = OP_RELAX | (uint32_t(RF_ROTATE) << OP_RF_SHIFT) |
                                (1u << OP_SHIFT3_SHIFT);
+// The refocusing op of a CPMG echo: relax, shift, rotate, shift, nothing
+// else; straight-line too.
+constexpr uint32_t kEchoMask = kFastMask | OP_RECORD;
+constexpr uint32_t kEchoBits = OP_RELAX | (1u << OP_SHIFT1_SHIFT) |
+                               (uint32_t(RF_ROTATE) << OP_RF_SHIFT) | (1u << OP_SHIFT2_SHIFT);
 
 template <int RP, int L, int TM, bool GEN, bool GN = false, int MINB = 1>
 __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(const SweepArgs a) {
@@ -646,6 +651,15 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                         rotate_all(op, si, co);
                     }
                     if (code & OP_RECORD) record(op);
+                    shift_all();
+                    continue;
+                }
+                if ((code & kEchoMask) == kEchoBits) {
+                    relax_all(op);
+                    shift_all();
+                    float si, co;
+                    pulse(op, g, si, co);
+                    rotate_all(op, si, co);
                     shift_all();
                     continue;
                 }
