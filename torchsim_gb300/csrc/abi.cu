@@ -68,7 +68,7 @@ const SweepEntry* choose(int mode, int states, int64_t work_items, const tsg_lau
     static const Preferred kPreferred[] = {
         {MODE_FORWARD, 10, 1, 10, 0, 0}, {MODE_FORWARD, 20, 1, 20, 0, 0},
         {MODE_T12, 10, 1, 10, 0, 0},     {MODE_GENERAL, 10, 1, 10, 0, 0},
-        {MODE_GN, 10, 1, 10, 0, 0},      {MODE_T12B, 20, 5, 4, 5, 65536},
+        {MODE_GN, 10, 1, 10, 3, 0},      {MODE_T12B, 20, 5, 4, 5, 65536},
         {MODE_T12B, 20, 5, 4, 0, 0},     {MODE_T12BI, 10, 5, 2, 0, 0},
         {MODE_T12BI, 20, 5, 4, 0, 0},
     };

@@ -230,15 +230,19 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     float last_dt = __int_as_float(0x7fffffff);  // NaN: first relax computes
     float e1 = 1.f, e2 = 1.f, k1 = 0.f, k2 = 0.f;
 
-    // Gauss-Newton sums: float over chunks of 32 samples, then into doubles.
+    // Gauss-Newton sums: float over chunks of 32 samples, then into doubles
+    // kept in shared memory (they change once per chunk, so they need not
+    // hold twenty registers for the whole sweep), one column per thread.
     static_assert(!GN || (S::T1 && S::T2), "GN sweeps carry the T1 and T2 tangents");
+    __shared__ double s_cd[GN ? 10 * 256 : 1];
+    double* cd = s_cd + threadIdx.x;  // cd[k * blockDim.x]: sum k of this thread
     float cs[10];
-    double cd[10];
     int in_chunk = 0;
 #pragma unroll
-    for (int k = 0; k < 10; ++k) {
-        cs[k] = 0.f;
-        cd[k] = 0.0;
+    for (int k = 0; k < 10; ++k) cs[k] = 0.f;
+    if constexpr (GN) {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) cd[k * blockDim.x] = 0.0;
     }
     const float2* yrow = nullptr;
     if constexpr (GN) {
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                 if (++in_chunk == 32) {
 #pragma unroll
                     for (int k = 0; k < 10; ++k) {
-                        cd[k] += double(cs[k]);
+                        cd[k * blockDim.x] += double(cs[k]);
                         cs[k] = 0.f;
                     }
                     in_chunk = 0;
@@ -703,7 +707,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
         if (q == 0 && active) {
             double* dst = a.gn_out + row * 10;
 #pragma unroll
-            for (int k = 0; k < 10; ++k) dst[k] = cd[k] + double(cs[k]);
+            for (int k = 0; k < 10; ++k) dst[k] = cd[k * blockDim.x] + double(cs[k]);
         }
     }
 }
@@ -723,3 +727,5 @@ void launch_sweep(const SweepArgs& a, dim3 grid, dim3 block, size_t smem, cudaSt
 #define TSG_SWEEP_ENTRY_MINB(MODE, R, L, TM, GEN, MINB) \
     {MODE, R, L, &::tsg::launch_sweep<(R) / 2, L, TM, GEN, false, MINB>, MINB}
 #define TSG_GN_ENTRY(R, L) {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<(R) / 2, L, 3, false, true>, 0}
+#define TSG_GN_ENTRY_MINB(R, L, MINB) \
+    {::tsg::MODE_GN, R, L, &::tsg::launch_sweep<(R) / 2, L, 3, false, true, MINB>, MINB}

@@ -9,6 +9,9 @@
 
 namespace tsg {
 const SweepEntry kSweepGN[] = {
+    // One voxel per lane with three blocks of 128 threads per SM (164
+    // registers): 12 warps per SM where the unbounded kernel holds 8.
+    TSG_GN_ENTRY_MINB(10, 1, 3),
     TSG_GN_ENTRY(10, 1), TSG_GN_ENTRY(2, 5), TSG_GN_ENTRY(6, 2), TSG_GN_ENTRY(4, 5), TSG_GN_ENTRY(2, 10), TSG_GN_ENTRY(4, 4), TSG_GN_ENTRY(8, 4), TSG_GN_ENTRY(4, 8), TSG_GN_ENTRY(8, 8), TSG_GN_ENTRY(4, 16), TSG_GN_ENTRY(4, 32),
 };
 const int kSweepGNCount = sizeof(kSweepGN) / sizeof(kSweepGN[0]);
