@@ -100,8 +100,88 @@ def test_match_argument_errors(cuda):
     atoms = torch.ones((4, 16), dtype=torch.complex64)
     with pytest.raises(ValueError):
         DictionaryMatcher(dictionary=atoms, top_k=9)
-    with pytest.raises(NotImplementedError):
-        DictionaryMatcher(dictionary=atoms, groups=2)
+    with pytest.raises(ValueError):
+        DictionaryMatcher(dictionary=atoms, groups=0)
+    with pytest.raises(ValueError):
+        DictionaryMatcher(dictionary=atoms, prune=1.0)
     m = DictionaryMatcher(dictionary=atoms)
     with pytest.raises(ValueError):
         m.match(torch.ones((3, 15), dtype=torch.complex64))
+
+
+# ---- group matching (the reference's tests/estimators/test_grouped.py) -------
+
+
+@pytest.fixture(scope="module")
+def fingerprints(cuda):
+    """An MRF dictionary over a 60 x 30 T1/T2 grid (200 flips U(10, 60) deg,
+    TR 10 ms, TI 20 ms) and a noisy off-grid volume of every 37th atom."""
+    import torchsim_gb300 as ts
+
+    gen = torch.Generator().manual_seed(0)
+    flip = 10.0 + 50.0 * torch.rand(200, generator=gen)
+    grid = torch.cartesian_prod(torch.linspace(200.0, 3000.0, 60), torch.linspace(20.0, 300.0, 30))
+    atoms = ts.mrf_sim(flip, 10.0, grid[:, 0].to(cuda), grid[:, 1].to(cuda), TI=20.0, states=10)
+    noise_gen = torch.Generator().manual_seed(7)
+    picked = atoms[::37]
+    noise = torch.randn(picked.shape, generator=noise_gen, dtype=torch.complex64).to(cuda)
+    measured = picked + 0.01 * float(atoms.abs().max()) * noise
+    return atoms, grid.to(cuda), measured
+
+
+def test_grouped_matching_finds_what_direct_matching_finds(fingerprints):
+    """Where the pruned search differs from the exhaustive one it is by a grid
+    step: at least 80% agree and the mean relative error stays under 1%."""
+    from torchsim_gb300 import DictionaryMatcher
+
+    atoms, grid, measured = fingerprints
+    direct = DictionaryMatcher(dictionary=atoms, parameters=grid)(measured)
+    grouped = DictionaryMatcher(dictionary=atoms, parameters=grid, groups=24)(measured)
+    assert float((direct == grouped).all(-1).float().mean()) > 0.8
+    for column in range(grid.shape[-1]):
+        error = ((grouped[:, column] - direct[:, column]) / direct[:, column]).abs()
+        assert float(error.mean()) < 0.01
+
+
+def test_grouped_matching_rules_out_most_of_the_dictionary(fingerprints):
+    from torchsim_gb300 import DictionaryMatcher
+
+    atoms, grid, measured = fingerprints
+    matcher = DictionaryMatcher(dictionary=atoms, parameters=grid, groups=24)
+    unit = measured / torch.linalg.vector_norm(measured, dim=-1, keepdim=True)
+    kept = matcher.grouping.survivors(unit, matcher.prune)
+    assert float(kept.sum(-1).float().mean()) < 0.25 * matcher.grouping.count
+    assert float(matcher.grouping.survivors(unit, 0.2).sum(-1).float().mean()) > float(
+        matcher.grouping.survivors(unit, 0.0).sum(-1).float().mean())
+
+
+def test_grouped_scores_are_the_exact_scores_of_the_atoms_found(fingerprints):
+    """Whatever atom the pruned search returns, its score is that atom's
+    exact normalized correlation, and the top k come ranked."""
+    from torchsim_gb300 import DictionaryMatcher
+    from torchsim_gb300.matching import correlate
+
+    atoms, grid, measured = fingerprints
+    matcher = DictionaryMatcher(dictionary=atoms, parameters=grid, groups=24, top_k=3)
+    found = matcher.match(measured)
+    assert found.indices.shape == (measured.shape[0], 3)
+    assert bool((torch.diff(found.scores, dim=-1) <= 1e-5).all())
+    assert bool((found.indices < atoms.shape[0]).all())
+    unit_s = measured / torch.linalg.vector_norm(measured, dim=-1, keepdim=True)
+    unit_a = atoms / torch.linalg.vector_norm(atoms, dim=-1, keepdim=True)
+    exact = torch.gather(correlate(unit_s, unit_a), 1, found.indices)
+    torch.testing.assert_close(found.scores, exact, rtol=1e-5, atol=1e-6)
+    torch.testing.assert_close(found.parameters, grid[found.indices])
+
+
+def test_more_groups_than_atoms_gives_one_each(fingerprints):
+    from torchsim_gb300 import DictionaryMatcher
+
+    atoms, grid, measured = fingerprints
+    few = atoms[:10]
+    matcher = DictionaryMatcher(dictionary=few, parameters=grid[:10], groups=50)
+    assert matcher.grouping.count == 10
+    exhaustive = DictionaryMatcher(dictionary=few, parameters=grid[:10])
+    # One atom per group and nothing pruned: the exhaustive answer.
+    got = DictionaryMatcher(dictionary=few, parameters=grid[:10], groups=50, prune=0.999)
+    assert torch.equal(got.match(measured).indices, exhaustive.match(measured).indices)

@@ -14,6 +14,16 @@ accumulated in FP32 in tensor memory, with the selection of each voxel's best
 exists. The candidates are then rescored exactly in FP32 against the complex
 signals (``tsg_match_rescore``) and the top k kept, so the fp16 screen only
 narrows which atoms are compared exactly.
+
+Group matching (``groups``) is the reference's option for dictionaries too
+large to search exhaustively (``estimators/_grouped.py``; Cauley, Setsompop,
+Ma et al., "Fast group matching for MR fingerprinting reconstruction", MRM
+74(2), 2015): the dictionary is clustered into groups of nearly parallel
+atoms, a voxel is scored against each group's representative first, and only
+the groups within ``prune`` of its best representative score are searched.
+It is approximate (a pruned group may hold the best atom) and kept for the
+reference's semantics; on this GPU the exhaustive tensor-core search is exact
+and faster.
 """
 
 from __future__ import annotations
@@ -25,7 +35,7 @@ import torch
 
 from . import _native, engine
 
-__all__ = ["DictionaryMatcher", "MatchResult"]
+__all__ = ["DictionaryMatcher", "Grouping", "MatchResult", "correlate"]
 
 
 @dataclass(frozen=True)
@@ -47,6 +57,110 @@ def _normalized(x: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
     return x / norm[:, None], norm
 
 
+def correlate(signals: torch.Tensor, atoms: torch.Tensor) -> torch.Tensor:
+    """``|<s, d>|`` of every (normalized) signal against every (normalized)
+    atom, ``(voxels, atoms)`` real: blind to the complex scale that proton
+    density and receive phase put on a signal (``_grouped.py:212-243``). A
+    complex signal against real atoms scores both of its parts."""
+    if torch.is_complex(signals) and not torch.is_complex(atoms):
+        return torch.hypot(signals.real @ atoms.mT, signals.imag @ atoms.mT)
+    return (signals @ atoms.mH).abs()
+
+
+@dataclass(frozen=True)
+class Grouping:
+    """A dictionary split into groups of nearly parallel atoms
+    (``_grouped.py:34-161``): ``members`` the atom indices of each group,
+    ``representative`` ``(groups, contrasts)`` each group's unit mean signal,
+    ``atoms`` each group's unit atoms in the dictionary's own basis."""
+
+    members: tuple[torch.Tensor, ...]
+    representative: torch.Tensor
+    atoms: tuple[torch.Tensor, ...]
+
+    @property
+    def count(self) -> int:
+        return len(self.members)
+
+    @property
+    def sizes(self) -> tuple[int, ...]:
+        return tuple(int(m.numel()) for m in self.members)
+
+    @property
+    def condition(self) -> float:
+        """Condition number of the representatives: it climbs once groups
+        start to look alike, which is when there are too many to prune with."""
+        s = torch.linalg.svdvals(self.representative.to(torch.complex64))
+        return float(s[0] / s[-1].clamp_min(torch.finfo(torch.float32).tiny))
+
+    @classmethod
+    def fit(cls, dictionary: torch.Tensor, count: int) -> Grouping:
+        """Greedy clustering into ``count`` groups (``_grouped.py:76-131``):
+        the first atom not yet in a group seeds one and takes the
+        ceil(atoms / count) unassigned atoms most correlated with it
+        (itself among them); repeated until every atom has a group, so all
+        groups but the last hold a full share."""
+        total = int(dictionary.shape[0])
+        if not 1 <= count <= total:
+            raise ValueError(f"count must be between one and the {total} atoms, got {count}")
+        unit = dictionary
+        if not (torch.is_complex(unit) or torch.is_floating_point(unit)):
+            unit = unit.to(torch.float32)
+        unit, _ = _normalized(unit)
+        share = -(-total // count)
+        free = torch.ones(total, dtype=torch.bool, device=unit.device)
+        floor = torch.full((total,), -1.0, dtype=unit.real.dtype, device=unit.device)
+        members = []
+        left = total
+        while left:
+            seed = int(torch.argmax(free.to(torch.int8)))  # the first free atom
+            alike = torch.where(free, (unit @ unit[seed].conj()).abs(), floor)
+            take = min(share, left)
+            chosen = torch.topk(alike, take).indices
+            members.append(chosen)
+            free[chosen] = False
+            left -= take
+        representative = torch.cat([_normalized(unit[m].mean(0, keepdim=True))[0] for m in members])
+        return cls(members=tuple(members), representative=representative,
+                   atoms=tuple(unit[m] for m in members))
+
+    def survivors(self, signals: torch.Tensor, prune: float) -> torch.Tensor:
+        """``(voxels, groups)`` bool: the groups whose representative scores
+        within ``prune`` (a fraction) of a voxel's best representative score
+        (``_grouped.py:133-151``). ``signals`` are normalized."""
+        scores = correlate(signals, self.representative)
+        return scores >= scores.amax(-1, keepdim=True) * (1.0 - prune)
+
+    def to(self, device: torch.device) -> Grouping:
+        if self.representative.device == torch.device(device):
+            return self
+        return Grouping(members=tuple(m.to(device) for m in self.members),
+                        representative=self.representative.to(device),
+                        atoms=tuple(x.to(device) for x in self.atoms))
+
+
+def _search_groups(signals: torch.Tensor, grouping: Grouping, top_k: int,
+                   prune: float) -> tuple[torch.Tensor, torch.Tensor]:
+    """Top-k atoms and scores of normalized ``signals`` within each voxel's
+    surviving groups (``_grouped.py:164-209``): every group that some voxel
+    kept is scored against those voxels only, and its best k merge into the
+    voxels' running top k."""
+    V = signals.shape[0]
+    scores = torch.full((V, top_k), -1.0, dtype=signals.real.dtype, device=signals.device)
+    indices = torch.zeros((V, top_k), dtype=torch.int64, device=signals.device)
+    keep = grouping.survivors(signals, prune)
+    for g in torch.nonzero(keep.any(0)).flatten().tolist():
+        rows = torch.nonzero(keep[:, g]).flatten()
+        local = correlate(signals[rows], grouping.atoms[g])
+        found, where = torch.topk(local, min(top_k, local.shape[1]), dim=-1)
+        pool_scores = torch.cat((scores[rows], found), dim=-1)
+        pool_indices = torch.cat((indices[rows], grouping.members[g][where]), dim=-1)
+        best, pick = torch.topk(pool_scores, top_k, dim=-1)
+        scores[rows] = best
+        indices[rows] = torch.gather(pool_indices, -1, pick)
+    return indices, scores
+
+
 def _pad8(x: torch.Tensor) -> torch.Tensor:
     extra = (-x.shape[-1]) % 8
     return torch.nn.functional.pad(x, (0, extra)) if extra else x
@@ -56,7 +170,10 @@ class DictionaryMatcher:
     """Match signals against ``dictionary`` ``(atoms, contrasts)`` by normalized
     complex inner products; ``parameters`` ``(atoms, n)`` are returned for the
     matched atoms. ``top_k`` (1..8) candidates per voxel; voxels are matched
-    ``query_chunk_size`` at a time. Group matching (``groups``) is not built."""
+    ``query_chunk_size`` at a time. ``groups`` clusters the dictionary into
+    that many groups (at most one per atom) and searches only the groups
+    within ``prune`` of a voxel's best group (:class:`Grouping`; read
+    :attr:`grouping` after fitting)."""
 
     def __init__(self, acquisition=None, *, dictionary: torch.Tensor | None = None,
                  parameters: torch.Tensor | None = None, query_chunk_size: int = 65536,
@@ -64,8 +181,8 @@ class DictionaryMatcher:
                  prune: float = 5e-3, device: torch.device | str | None = None) -> None:
         if acquisition is not None:
             raise NotImplementedError("simulate the dictionary first and pass dictionary=")
-        if groups is not None:
-            raise NotImplementedError("group matching is not built")
+        if groups is not None and groups < 1:
+            raise ValueError(f"groups must be positive, got {groups}")
         if query_chunk_size < 1 or dictionary_chunk_size < 1:
             raise ValueError("chunk sizes must be positive")
         if not 1 <= top_k <= 8:
@@ -75,6 +192,9 @@ class DictionaryMatcher:
         self.query_chunk_size = int(query_chunk_size)
         self.dictionary_chunk_size = int(dictionary_chunk_size)
         self.top_k = int(top_k)
+        self.groups = None if groups is None else int(groups)
+        self.prune = float(prune)
+        self.grouping: Grouping | None = None
         self.device = engine.require_cuda(torch.device(device) if device is not None else None)
         self.dictionary = None
         if dictionary is not None:
@@ -116,6 +236,8 @@ class DictionaryMatcher:
         stored = torch.zeros((rows, screen.shape[1]), dtype=torch.float16, device=self.device)
         stored[pos] = screen
         self._screen_atoms = stored
+        self.grouping = (None if self.groups is None
+                         else Grouping.fit(d, min(self.groups, d.shape[0])))
         if parameters is None:
             self.parameter_values = None
         else:
@@ -157,6 +279,11 @@ class DictionaryMatcher:
         for chunk in flat.split(self.query_chunk_size):
             V = chunk.shape[0]
             s_hat, _ = _normalized(chunk)
+            if self.grouping is not None:
+                ix, sc = _search_groups(s_hat, self.grouping, self.top_k, self.prune)
+                scores.append(sc)
+                indices.append(ix)
+                continue
             queries = self._queries(s_hat)
             cand_s = torch.empty((V, m), dtype=torch.float32, device=self.device)
             cand_i = torch.empty((V, m), dtype=torch.int32, device=self.device)
