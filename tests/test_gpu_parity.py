@@ -82,6 +82,52 @@ def test_config0_workload(cuda):
         assert max_rel(jac.numpy()[:, k].real, ref[:, k]) <= JACOBIAN_TOL
 
 
+def test_dictionary_workload_at_full_size(cuda):
+    """The dictionary workload at its full size -- 262,144 grid atoms (T1
+    geomspace(100, 4000, 128) x T2 geomspace(5, 500, 64) x B1 linspace(0.6,
+    1.4, 32)), the 880-pulse schedule, nstates 20, Jacobian (T1, T2, B1) in
+    one fused launch -- through properties that do not depend on its size:
+    1,024 atoms spread over the grid against the FP64 oracle; the same atoms
+    swept alone, bitwise equal to their rows of the full launch at the same
+    launch shape; the signal against the forward-only kernel's."""
+    import torchsim_gb300 as ts
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    axes = (np.geomspace(100, 4000, 128), np.geomspace(5, 500, 64), np.linspace(0.6, 1.4, 32))
+    g1, g2, g3 = (x.ravel().astype(np.float32) for x in np.meshgrid(*axes, indexing="ij"))
+    A = g1.size
+    flip = mrf_schedule()
+    T1, T2, B1 = (torch.from_numpy(x).to(cuda) for x in (g1, g2, g3))
+    names = ("T1", "T2", "B1")
+    rng = np.random.default_rng(11)
+    pick = np.unique(np.concatenate([np.linspace(0, A - 1, 768).astype(np.int64),
+                                     rng.integers(0, A, 256)]))
+    idx = torch.from_numpy(pick).to(cuda)
+
+    sig, jac = ts.mrf_sim(torch.from_numpy(flip), 10.0, T1, T2, B1=B1, states=20, diff=names)
+    assert sig.shape == (A, 880) and jac.shape == (A, 3, 880)
+    s, j = sig[idx].cpu().numpy(), jac[idx].cpu().numpy()
+    del sig, jac
+    ev = mrf_events(flip, 10.0)
+    p = packed_from_events(ev, g1[pick], g2[pick], 20, b1=g3[pick])
+    assert max_rel(s.real, -O.forward(p, "f64", threads=O.cpu_threads())) <= SIGNAL_TOL
+    ref = oracle_jacobian(p, names)
+    for k in range(3):
+        assert max_rel(j[:, k].real, ref[:, k]) <= JACOBIAN_TOL, names[k]
+
+    program = program_for(ev, cuda)
+    shape = (5, 4, 4, 5)  # the register-budget shape the full launch picks
+    full = engine.tissue_maps(cuda, A, T1, T2, None, B1, None)
+    fs, fj = engine.forward_tangents(program, full, 20, names, launch=shape)
+    alone = engine.tissue_maps(cuda, len(pick), T1[idx], T2[idx], None, B1[idx], None)
+    a_s, a_j = engine.forward_tangents(program, alone, 20, names, launch=shape)
+    assert torch.equal(fs[idx], a_s) and torch.equal(fj[idx], a_j)
+    plain = engine.forward(program, full, 20)
+    got, want = fs.cpu().numpy(), plain.cpu().numpy()
+    assert np.abs(want).max() > 0 and max_rel(got, want) <= SIGNAL_TOL
+
+
 def test_prepared_repeated_mrf_all_columns(cuda, golden):
     import torchsim_gb300 as ts
 
