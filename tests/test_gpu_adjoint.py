@@ -146,6 +146,52 @@ def test_adjoint_launch_shapes(cuda, shape, mode):
         assert max_rel(got, ref[name]) <= GRAD_TOL, (shape, mode, name)
 
 
+def test_adjoint_workload_at_full_size(cuda):
+    """The sequence-optimisation workload at its full size -- 16,384 voxels,
+    600 pulses (flip U(5, 70) deg, TR U(8, 15) ms), 20 states, trajectory
+    mode -- through properties that do not depend on its size: the tissue
+    gradients of 512 voxels spread over the batch against the FP64 oracle run
+    on those voxels alone, and each event's gradient equal to the sum of the
+    two half batches' (the loss is a sum over voxels)."""
+    from torchsim_gb300 import engine
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    rng = np.random.default_rng(5)
+    V, S = 16384, 20
+    flips = rng.uniform(5, 70, 600).astype(np.float32)
+    trs = rng.uniform(8, 15, 600).astype(np.float32)
+    ev = mrf_events(flips, trs)
+    prog = program_for(ev, cuda)
+    t1, t2, b1 = draw_tissue(3, V)
+    seed = rng.standard_normal((V, ev.outputs)).astype(np.complex64)
+
+    def run(rows):
+        n = len(rows)
+        tissue = engine.tissue_maps(cuda, n, t1[rows], t2[rows], None, b1[rows], None)
+        c, ck, _ = engine.adjoint_plan(prog, n, S, None, 1)
+        assert c == 1
+        ckpt = torch.empty(ck // 4, dtype=torch.float32, device=cuda)
+        engine.forward_checkpointed(prog, tissue, S, c, ckpt)
+        grads = {k: torch.zeros(n, device=cuda) for k in ("t1_ms", "t2_ms", "b1")}
+        for k in ("flip_rad", "duration_s"):
+            grads[k] = torch.zeros((1, ev.events), device=cuda)
+        engine.adjoint(prog, tissue, S, torch.from_numpy(seed[rows]).to(cuda), ckpt, c, grads)
+        return {k: v.cpu().numpy() for k, v in grads.items()}
+
+    rows = np.arange(V)
+    full = run(rows)
+    sample = np.unique(np.concatenate([np.linspace(0, V - 1, 384).astype(np.int64),
+                                       rng.integers(0, V, 128)]))
+    ref = O.adjoint(packed_from_events(ev, t1[sample], t2[sample], S, b1=b1[sample]),
+                    -seed[sample].real, "f64")
+    for name in ("t1_ms", "t2_ms", "b1"):
+        assert max_rel(full[name][sample], ref[name]) <= GRAD_TOL, name
+    low, high = run(rows[: V // 2]), run(rows[V // 2:])
+    for name in ("flip_rad", "duration_s"):
+        assert np.abs(full[name]).max() > 0, name
+        assert max_rel(full[name], low[name] + high[name]) <= 1e-5, name
+
+
 def test_adjoint_against_central_differences(cuda):
     """Config-3 shapes in small: 600 pulses, nstates 20; central differences
     (h = 1e-3 deg / ms) of the FP64 oracle's loss on sampled coordinates."""
