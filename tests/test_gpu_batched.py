@@ -72,6 +72,48 @@ def test_sequence_alone_equals_in_the_mix(cuda):
     assert torch.equal(alone.signal(0), batch.signal(5))
 
 
+def test_batched_workload_at_full_size(cuda):
+    """The uneven-CPMG workload at its full size -- 512 sequences (ETL
+    U{8..64}, refocusing U(100, 180) deg, ESP U(5, 15) ms, phases 90 deg,
+    round(exp(U(ln 1e3, ln 6.4e4))) voxels each, nstates 2 x ETL), one
+    persistent launch at 16 orders per lane, 2 warps, 8 blocks per SM --
+    through properties that do not depend on its size: up to 64 voxels of
+    every 16th sequence against the FP64 oracle, and three sequences launched
+    alone bitwise equal to their rows of the full launch."""
+    from torchsim_gb300.batching import BatchEntry, SequenceBatch
+    from torchsim_gb300.sequence import fse_events
+
+    rng = np.random.default_rng(2)
+    entries = []
+    for _ in range(512):
+        etl = int(rng.integers(8, 65))
+        flips = rng.uniform(100, 180, etl).astype(np.float32)
+        ev = fse_events(flips, float(rng.uniform(5, 15)), phases_deg=90.0)
+        v = int(round(np.exp(rng.uniform(np.log(1e3), np.log(6.4e4)))))
+        entries.append(BatchEntry(ev, 2 * etl, rng.uniform(300, 3000, v).astype(np.float32),
+                                  rng.uniform(10, 300, v).astype(np.float32),
+                                  rng.uniform(0.7, 1.3, v).astype(np.float32)))
+    batch = SequenceBatch(entries, cuda)
+    assert sum(e.t1.size for e in entries) > 7_000_000
+    shape = (16, 2, 8)
+    batch.out.fill_(float("nan"))
+    batch.launch(shape)
+    torch.cuda.synchronize()
+    for s in range(0, 512, 16):
+        e = entries[s]
+        rows = np.unique(np.linspace(0, e.t1.size - 1, 64).astype(np.int64))
+        ref = O.forward(packed_from_events(e.events, e.t1[rows], e.t2[rows], e.states,
+                                           b1=e.b1[rows]), "f64")
+        got = batch.signal(s)[torch.from_numpy(rows).to(cuda)].cpu().numpy()
+        assert not got.real.any()
+        assert max_rel(got.imag, ref) <= 1e-5, s
+    for s in (0, 255, 511):
+        alone = SequenceBatch([entries[s]], cuda)
+        alone.launch(shape)
+        torch.cuda.synchronize()
+        assert torch.equal(alone.signal(0), batch.signal(s)), s
+
+
 def test_autotuner_picks_a_working_shape(cuda, tmp_path, monkeypatch):
     monkeypatch.setenv("TORCHSIM_GB300_CACHE", str(tmp_path / "tuning.json"))
     batch = make_batch(cuda, seed=3, etls=(8, 16), voxels=(50, 200))
