@@ -32,7 +32,7 @@ extern "C" {
 enum {
     TSG_OK = 0,
     TSG_ERR_ARGUMENT = -1,    /* bad sizes or null pointers: the reference's ValueError */
-    TSG_ERR_UNSUPPORTED = -2, /* outside the real-subspace single-pool subset */
+    TSG_ERR_UNSUPPORTED = -2, /* outside the served subset (single pool, instant RF) */
     TSG_ERR_CUDA = -3,        /* a CUDA runtime call failed */
     TSG_ERR_CAPACITY = -4     /* a size beyond a stated maximum */
 };
