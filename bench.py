@@ -177,6 +177,22 @@ def traffic_per_launch() -> float | None:
     return None
 
 
+def job_seconds(local_seconds: float, dist, device) -> float:
+    """The job's time for N replicas: the slowest rank's (max over ranks)."""
+    if dist is None:
+        return local_seconds
+    import torch
+
+    t = torch.tensor([local_seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_step: float, steps: int, world: int, seconds: float) -> float:
+    """Whole-job throughput: the units every rank processed over the job's time."""
+    return units_per_step * steps * world / seconds
+
+
 def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     import torch
 
@@ -232,13 +248,9 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends, strict=True)]
-    total_s = sum(step_ms) * 1e-3
-    if dist is not None:
-        t = torch.tensor([total_s], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = job_seconds(sum(step_ms) * 1e-3, dist, device)
     updates = float(atoms) * PULSES * STATES
-    value = updates * args.steps * world / total_s
+    value = job_value(updates, args.steps, world, total_s)
     kernel_s = total_s / args.steps
 
     # Plain form: the reference's call pattern on the GPU -- one forward pass,
