@@ -868,8 +868,9 @@ class EpgVjpFunction(torch.autograd.Function):
     curvature of ``<w, J v>``), both from one forward-with-trajectory and one
     reverse of the second-order sweep. This is the reference's
     ``_NativeEpgVjp.backward`` (``_run_packed_vjp_jvp`` with the gradients'
-    cotangents as the direction, sequence/_accelerators.py:1597-1735). Zero-duration events, folded into the op before them, carry no
-    duration gradient of either order."""
+    cotangents as the direction, sequence/_accelerators.py:1597-1735).
+    Zero-duration events, folded into the op before them, carry no duration
+    gradient of either order."""
 
     @staticmethod
     def forward(ctx, program, states, launch, c, ckpt, tissue, want, grad_out, t1, t2, m0, b1,
@@ -907,7 +908,9 @@ class EpgVjpFunction(torch.autograd.Function):
         need = ctx.needs_input_grad  # program, states, launch, c, ckpt, tissue, want, grad_out, ...
         if not direction:
             return (None,) * len(need)
-        sig, jac, traj, ws = second_forward(program, tissue, states, [direction], launch=launch_of(ctx))
+        # The second-order sweeps pick their own launch shape (the first-order
+        # shape of the forward is not one of theirs).
+        sig, jac, traj, ws = second_forward(program, tissue, states, [direction])
         curvature = {}
         V = tissue.voxels
         ev_shape = (program.trains, program.events.events)
@@ -916,13 +919,8 @@ class EpgVjpFunction(torch.autograd.Function):
                 shape = ev_shape if name in ("flip_rad", "duration_s") else (V,)
                 curvature[name] = torch.zeros(shape, dtype=torch.float32, device=dev)
         second_reverse(program, tissue, states, [direction], grad_out.detach()[:, None, :], traj, ws,
-                       curvature=curvature, launch=launch_of(ctx))
+                       curvature=curvature)
         out = [None] * 7
         out.append(jac[:, 0] if need[7] else None)
         out += [curvature.get(n) for n in VJP_NAMES]
         return tuple(out)
-
-
-def launch_of(ctx):
-    """The second-order sweeps pick their own launch shape."""
-    return None
