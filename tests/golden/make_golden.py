@@ -514,6 +514,39 @@ def case_double_backward(ts, rec) -> dict:
     return out
 
 
+def case_grouping(ts, rec) -> dict:
+    """The reference's group matching (estimators/_grouped.py) on a
+    deterministic family of complex decays: the greedy clustering into 24
+    groups, the representatives, the surviving groups of noisy signals at
+    three thresholds and the top-3 grouped match."""
+    import torch
+    from torchsim.estimators._grouped import Grouping, match_in_groups
+
+    t = torch.linspace(0.01, 3.0, 60, dtype=torch.float64)
+    r1 = torch.linspace(0.3, 5.0, 20, dtype=torch.float64)
+    r2 = torch.linspace(1.0, 30.0, 25, dtype=torch.float64)
+    g1, g2 = torch.meshgrid(r1, r2, indexing="ij")
+    atoms = (1 - 2 * torch.exp(-t * g1.reshape(-1, 1))) * torch.exp(-t * g2.reshape(-1, 1) / 10)
+    atoms = atoms.to(torch.complex64) * (1 + 0.5j)
+    grouping = Grouping.fit(atoms, 24)
+    gen = torch.Generator().manual_seed(7)
+    picked = atoms[::13]
+    noise = torch.randn(picked.shape, generator=gen, dtype=torch.complex64)
+    signals = picked + 0.01 * float(atoms.abs().max()) * noise
+    unit = signals / torch.linalg.vector_norm(signals, dim=-1, keepdim=True)
+    out = {"atoms": _np(atoms), "signals": _np(signals),
+           "members": np.concatenate([_np(m) for m in grouping.members]),
+           "sizes": np.array(grouping.sizes, np.int64),
+           "representative": _np(grouping.representative),
+           "condition": np.float64(grouping.condition)}
+    for prune in (0.0, 5e-3, 0.2):
+        out[f"survivors_{prune:g}"] = _np(grouping.survivors(unit, prune))
+    indices, scores = match_in_groups(unit, grouping, 3, 5e-3)
+    out["match_indices"] = _np(indices)
+    out["match_scores"] = _np(scores)
+    return out
+
+
 def _accelerators_of(ts):
     from torchsim.sequence import _accelerators
 
@@ -552,7 +585,7 @@ def case_gn(ts, rec) -> dict:
 
 
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
-         "mrf_second", "complex_adjoint", "double_backward")
+         "mrf_second", "complex_adjoint", "double_backward", "grouping")
 
 
 def main() -> None:
@@ -575,7 +608,7 @@ def main() -> None:
                      ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn),
                      ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
                      ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint),
-                     ("double_backward", case_double_backward)):
+                     ("double_backward", case_double_backward), ("grouping", case_grouping)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

@@ -1,9 +1,11 @@
-"""Group matching's clustering on the host (no GPU): the reference's
+"""Group matching on the host (no GPU): the reference's
 estimators/_grouped.py contract, checked the way its tests/estimators/
-test_grouped.py checks it, on a synthetic two-parameter family of decays."""
+test_grouped.py checks it on a synthetic two-parameter family of decays, and
+pinned to the reference's own outputs on a committed fixture."""
 
 from __future__ import annotations
 
+import numpy as np
 import pytest
 import torch
 
@@ -102,3 +104,32 @@ def test_correlate_is_blind_to_complex_scale(family):
     real = unit.real / torch.linalg.vector_norm(unit.real, dim=-1, keepdim=True)
     both = correlate(turned, real)
     assert both.shape == (5, family.shape[0]) and bool((both >= 0).all())
+
+
+def test_grouping_matches_the_reference(golden):
+    """The reference's own Grouping.fit, survivors and match_in_groups on the
+    same family (tests/golden/grouping.npz, made by tests/golden/
+    make_golden.py from estimators/_grouped.py): the same groups, the same
+    representatives, the same surviving groups at three thresholds and the
+    same top-3 grouped match."""
+    from torchsim_gb300.matching import _search_groups
+
+    d = golden("grouping")
+    atoms = torch.from_numpy(d["atoms"])
+    grouping = Grouping.fit(atoms, 24)
+    assert list(grouping.sizes) == d["sizes"].tolist()
+    offsets = np.concatenate([[0], np.cumsum(d["sizes"])])
+    for g, members in enumerate(grouping.members):
+        want = d["members"][offsets[g]:offsets[g + 1]]
+        assert sorted(members.tolist()) == sorted(want.tolist()), g
+    torch.testing.assert_close(grouping.representative, torch.from_numpy(d["representative"]),
+                               rtol=1e-5, atol=1e-6)
+    assert grouping.condition == pytest.approx(float(d["condition"]), rel=1e-4)
+    signals = torch.from_numpy(d["signals"])
+    unit = signals / torch.linalg.vector_norm(signals, dim=-1, keepdim=True)
+    for prune in (0.0, 5e-3, 0.2):
+        got = grouping.survivors(unit, prune).numpy()
+        assert np.array_equal(got, d[f"survivors_{prune:g}"]), prune
+    indices, scores = _search_groups(unit, grouping, 3, 5e-3)
+    assert np.array_equal(indices.numpy(), d["match_indices"])
+    np.testing.assert_allclose(scores.numpy(), d["match_scores"], rtol=1e-5, atol=1e-6)
