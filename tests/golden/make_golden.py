@@ -547,6 +547,38 @@ def case_grouping(ts, rec) -> dict:
     return out
 
 
+def case_design_loop(ts, rec) -> dict:
+    """The reference's design layer on a pure-torch cost (optim/_design.py):
+    crlb of real and complex Jacobians (and the infinite answer where the
+    Fisher matrix is singular), and SequenceDesign.minimize with two bounded
+    parameter vectors, one with per-element limits, for 25 Adam steps."""
+    import torch
+    from torchsim.optim import Bounded, SequenceDesign, crlb
+
+    gen = torch.Generator().manual_seed(3)
+    real = torch.randn((5, 3, 40), generator=gen)
+    cplx = torch.randn((5, 3, 40), generator=gen, dtype=torch.complex64)
+    singular = real.clone()
+    singular[2, 1] = singular[2, 0]
+    flip0 = torch.linspace(10.0, 60.0, 12)
+    tr0 = torch.full((12,), 11.0)
+    target = torch.rand(12, generator=gen) * 0.8 + 0.1
+    upper = torch.linspace(40.0, 70.0, 12)
+
+    def cost(flip, tr):
+        return ((torch.sin(torch.deg2rad(flip)) - target) ** 2).sum() + 1e-3 * (tr - 9.0).square().sum()
+
+    design = SequenceDesign(cost, flip=Bounded(flip0, 5.0, upper), tr=Bounded(tr0, 8.0, 15.0))
+    result = design.minimize(iterations=25, learning_rate=0.05)
+    return {"real": _np(real), "complex": _np(cplx), "singular": _np(singular),
+            "crlb_real": _np(crlb(real, noise_variance=0.5)),
+            "crlb_complex": _np(crlb(cplx, noise_variance=0.5)),
+            "crlb_singular": _np(crlb(singular, singular="infinite")),
+            "flip0": _np(flip0), "tr0": _np(tr0), "target": _np(target), "upper": _np(upper),
+            "loss": _np(result.loss), "flip": _np(result.parameters["flip"]),
+            "tr": _np(result.parameters["tr"])}
+
+
 def _accelerators_of(ts):
     from torchsim.sequence import _accelerators
 
@@ -585,7 +617,7 @@ def case_gn(ts, rec) -> dict:
 
 
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
-         "mrf_second", "complex_adjoint", "double_backward", "grouping")
+         "mrf_second", "complex_adjoint", "double_backward", "grouping", "design_loop")
 
 
 def main() -> None:
@@ -608,7 +640,8 @@ def main() -> None:
                      ("fse_cpmg", case_fse), ("mrf_adjoint", case_adjoint), ("gn_mrf", case_gn),
                      ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
                      ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint),
-                     ("double_backward", case_double_backward), ("grouping", case_grouping)):
+                     ("double_backward", case_double_backward), ("grouping", case_grouping),
+                     ("design_loop", case_design_loop)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

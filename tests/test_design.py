@@ -66,3 +66,35 @@ def test_crlb_matches_the_inverse_fisher():
         crlb(singular)
     with pytest.raises(ValueError):
         crlb(torch.zeros(4))
+
+
+def test_design_layer_matches_the_reference(golden):
+    """The reference's own crlb and SequenceDesign loop on a pure-torch cost
+    (tests/golden/design_loop.npz, made by tests/golden/make_golden.py from
+    optim/_design.py): the bounds of real and complex Jacobians, the infinite
+    answer of a singular one, and 25 Adam steps over two bounded vectors
+    (one with per-element limits) -- every step's loss and the final values."""
+    import numpy as np
+
+    d = golden("design_loop")
+    for name in ("real", "complex"):
+        got = crlb(torch.from_numpy(d[name]), noise_variance=0.5).numpy()
+        np.testing.assert_allclose(got, d[f"crlb_{name}"], rtol=1e-5)
+    got = crlb(torch.from_numpy(d["singular"]), singular="infinite").numpy()
+    want = d["crlb_singular"]
+    assert np.array_equal(np.isinf(got), np.isinf(want))
+    finite = np.isfinite(want)
+    np.testing.assert_allclose(got[finite], want[finite], rtol=1e-5)
+
+    target = torch.from_numpy(d["target"])
+
+    def cost(flip, tr):
+        return ((torch.sin(torch.deg2rad(flip)) - target) ** 2).sum() + 1e-3 * (tr - 9.0).square().sum()
+
+    design = SequenceDesign(cost, flip=Bounded(torch.from_numpy(d["flip0"]), 5.0,
+                                               torch.from_numpy(d["upper"])),
+                            tr=Bounded(torch.from_numpy(d["tr0"]), 8.0, 15.0))
+    result = design.minimize(iterations=25, learning_rate=0.05)
+    np.testing.assert_allclose(result.loss.numpy(), d["loss"], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(result.parameters["flip"].numpy(), d["flip"], rtol=1e-5)
+    np.testing.assert_allclose(result.parameters["tr"].numpy(), d["tr"], rtol=1e-5)
