@@ -579,6 +579,30 @@ def case_design_loop(ts, rec) -> dict:
             "tr": _np(result.parameters["tr"])}
 
 
+def case_bounds(ts, rec) -> dict:
+    """The reference's variable transforms (_bounds.py): to_free of values
+    inside two-sided, lower-only, upper-only and absent bounds, including
+    values at the very edges (clamped), and to_natural back."""
+    import torch
+    from torchsim._bounds import to_free, to_natural
+
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, None), "M0": (None, 5.0)}
+    names = ("T1", "T2", "M0", "B1")
+    gen = torch.Generator().manual_seed(5)
+    natural = torch.stack([
+        torch.cat([50.0 + 4950.0 * torch.rand(60, generator=gen, dtype=torch.float64),
+                   torch.tensor([50.0, 5000.0, 50.0 + 1e-9], dtype=torch.float64)]),
+        torch.cat([2.0 + torch.exp(6 * torch.randn(60, generator=gen, dtype=torch.float64)),
+                   torch.tensor([2.0, 2.0 + 1e-9, 1e6], dtype=torch.float64)]),
+        torch.cat([5.0 - torch.exp(3 * torch.randn(60, generator=gen, dtype=torch.float64)),
+                   torch.tensor([5.0, -1e3, 5.0 - 1e-9], dtype=torch.float64)]),
+        torch.randn(63, generator=gen, dtype=torch.float64),
+    ], dim=-1)
+    free = to_free(natural, bounds, names)
+    return {"natural": _np(natural), "free": _np(free),
+            "back": _np(to_natural(free, bounds, names))}
+
+
 def _accelerators_of(ts):
     from torchsim.sequence import _accelerators
 
@@ -617,7 +641,7 @@ def case_gn(ts, rec) -> dict:
 
 
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
-         "mrf_second", "complex_adjoint", "double_backward", "grouping", "design_loop")
+         "mrf_second", "complex_adjoint", "double_backward", "grouping", "design_loop", "bounds")
 
 
 def main() -> None:
@@ -641,7 +665,7 @@ def main() -> None:
                      ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
                      ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint),
                      ("double_backward", case_double_backward), ("grouping", case_grouping),
-                     ("design_loop", case_design_loop)):
+                     ("design_loop", case_design_loop), ("bounds", case_bounds)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

@@ -105,3 +105,20 @@ def test_engine_facade_defaults_and_labels():
         eng.simulate(mrf, {"T1": 1000.0, "T2": 80.0}, record="odd")
     with pytest.raises(ValueError):
         eng.simulate(mrf, {"T1": 1000.0})
+
+
+def test_free_variables_match_the_reference(golden):
+    """The reference's own to_free (_bounds.py:113-160) on values inside
+    two-sided, lower-only, upper-only and absent bounds, edges included
+    (tests/golden/bounds.npz, made by tests/golden/make_golden.py)."""
+    import numpy as np
+
+    from torchsim_gb300.recon import to_free
+
+    d = golden("bounds")
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, None), "M0": (None, 5.0)}
+    got = to_free(torch.from_numpy(d["natural"]), bounds, ("T1", "T2", "M0", "B1")).numpy()
+    np.testing.assert_allclose(got, d["free"], rtol=1e-12, atol=1e-12)
+    # And the reference's inverse takes them back (inside the edge clamps).
+    inside = np.abs(d["back"] - d["natural"]) <= 1e-6 * np.maximum(1.0, np.abs(d["natural"]))
+    assert inside.mean() > 0.95
