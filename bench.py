@@ -944,59 +944,53 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:  
 # ---- CPU baselines ----------------------------------------------------------
 
 
-def _reference_module():
-    """The reference's own compiled CPU kernel (oracle/_ref), if it loads here."""
-    import importlib.util
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu's, else /proc/cpuinfo's, else the
+    platform's machine type)."""
+    import platform
+    import subprocess
 
-    for path in sorted((ROOT / "oracle" / "_ref").glob("_epg_cpu*.so")):
-        try:
-            spec = importlib.util.spec_from_file_location("_epg_cpu", path)
-            module = importlib.util.module_from_spec(spec)
-            spec.loader.exec_module(module)
-            return module
-        except (ImportError, OSError):
-            continue
-    return None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip() + f" ({platform.machine()})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.machine()
 
 
 def cpu_run(sample: int, threads: int):
     """Forward + one tangent pass per Jacobian column (the reference's call
-    pattern) over the first `sample` atoms of the grid. Returns (seconds, kind)."""
+    pattern, `torch.func.jvp` per property) over the first `sample` atoms of the
+    grid. Runs the reference's own compiled CPU kernel where a build for this
+    machine exists, else the oracle's FP32 port, whose forward is the
+    reference's per-atom kernel and whose tangents are its eight-atom lane
+    kernel (the layout the reference picks for these runs), bitwise the
+    reference's results. Returns (seconds, kind)."""
+    from oracle import oracle as O
     from torchsim_gb300.sequence import mrf_events
 
     t1, t2, b1 = (a[:sample].copy() for a in dictionary_grid())
     ev = mrf_events(mrf_schedule(), 10.0)
-    ref = _reference_module()
-    if ref is not None:
-        E = ev.events
-        zeros = np.zeros(sample, np.float32)
-        ones = np.ones(sample, np.float32)
-        tissue = [t1, t2, ones, b1, zeros, zeros, ones, *([zeros] * 10)]
-        events = [np.ascontiguousarray(ev.duration[0]), ev.kind, np.ascontiguousarray(ev.flip[0]),
-                  np.ascontiguousarray(ev.phase[0]), ev.action, ev.output_index,
-                  np.zeros(E, np.int32), np.zeros(E, np.float32), np.zeros(E, np.float32)]
-        out_r = np.zeros((sample, PULSES), np.float32)
-        out_i = np.zeros((sample, PULSES), np.float32)
-        features = 8  # transmit only: m0 and inversion at identity
-        common = (sample, 1, E, STATES, PULSES, threads, 1, 0.0, 0.0, 1, 1, 0, 1.0, 0, 1.0, 0,
-                  features, 0, 0, 0)
-        t0 = time.perf_counter()
-        ref.simulate([a.ctypes.data for a in (*tissue, *events, out_r, out_i)] + [0] * 13, *common)
-        for col in (0, 1, 3):
-            tan = [zeros] * 17 + [np.zeros(E, np.float32)] * 3
-            tan = list(tan)
-            tan[col] = ones
-            ref.simulate_jvp([a.ctypes.data for a in (*tissue, *events, *tan, out_r, out_i)]
-                             + [0] * 13, *common)
-        return time.perf_counter() - t0, "reference"
-    from oracle import oracle as O
-
     p = O.Packed(t1, t2, ev.duration, ev.kind, ev.flip, ev.action, ev.output_index, STATES, b1=b1)
+    ref = O.reference_module()
     t0 = time.perf_counter()
+    if ref is not None:
+        O.reference_forward(ref, p, threads)
+        for column in (0, 1, 3):  # T1, T2, B1 tissue slots
+            O.reference_jvp(ref, p, column, threads)
+        return time.perf_counter() - t0, "reference"
     O.forward(p, "f32", threads=threads)
     for key in ("t1_ms", "t2_ms", "b1"):
         O.tangent(p, "f32", threads=threads, **{key: 1.0})
     return time.perf_counter() - t0, "port"
+
+
+PORT_NOTE = ("the oracle's FP32 port: the reference's compiled kernel is built only where its "
+             "sources are, and no build for this host's architecture exists here; the port "
+             "runs the reference's own kernel layouts (per-atom forward, eight-atom lane "
+             "tangents) and reproduces its results bit for bit")
 
 
 def cpu_baseline(sample: int) -> dict:
@@ -1004,10 +998,13 @@ def cpu_baseline(sample: int) -> dict:
 
     threads = O.cpu_threads()
     seconds, kind = cpu_run(sample, threads)
-    return {"value": float(sample) * PULSES * STATES / seconds, "unit": "updates/s",
-            "cores": threads, "kind": kind,
+    line = {"value": float(sample) * PULSES * STATES / seconds, "unit": "updates/s",
+            "cores": threads, "kind": kind, "cpu": cpu_model(),
             "sample": f"first {sample} of the {ATOMS} grid atoms, forward + 3 tangent passes "
                       f"(the reference's per-column call pattern), {seconds:.2f} s"}
+    if kind == "port":
+        line["why_port"] = PORT_NOTE
+    return line
 
 
 def run_reference(args, rank: int) -> dict | None:
@@ -1042,8 +1039,10 @@ def run_reference(args, rank: int) -> dict | None:
         "data": "synthetic (seeded grid of the named shape)",
         "config": config({"sample_atoms_per_step": args.cpu_sample}),
         "cpu_baseline": {"value": value, "unit": "updates/s", "cores": threads, "kind": kind,
+                         "cpu": cpu_model(),
                          "sample": f"{args.cpu_sample} of {ATOMS} atoms per step, forward + "
-                                   "3 tangent passes"},
+                                   "3 tangent passes",
+                         **({"why_port": PORT_NOTE} if kind == "port" else {})},
         "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }

@@ -8,10 +8,14 @@
 # for bit. It needs only the CPython headers; the reference's cmake project is
 # not used.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The reference checkout is the argument, else $TORCHSIM_REFERENCE, else the
+# container's read-only checkout at /root/reference. Where none of them holds
+# the sources (a host without the checkout), nothing is built and the CPU
+# baseline runs the oracle's port.
 set -euo pipefail
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${TORCHSIM_REFERENCE:-/root/reference}}"
 src="$ref/src/torchsim/_epg_cpu.cpp"
 if [[ ! -f "$src" ]]; then
     echo "reference sources not found at $ref; nothing built" >&2

@@ -19,6 +19,7 @@
  *   shift_adjoint         shift_real_adjoint               5950-5971
  *   run_forward           simulate_real_range              3041-3128
  *   run_tangent           simulate_real_jvp_range          3136-3285
+ *   run_tangent_lanes     simulate_real_jvp_atom_lane_range 3503-3695
  *   run_adjoint           simulate_real_vjp_range          5985-6232
  *   run_second            simulate_real_vjp_jvp_range      7028-7330
  *                         (dual arithmetic 346-365, 407-418, 768-775, 6964-6967)
@@ -299,6 +300,164 @@ static void run_tangent(const oracle_case* c, const oracle_direction* d,
             } else if (a & A_SHIFT_AFTER) {
                 shift(plus, minus, S);
                 shift(dp_, dm_, S);
+            }
+        }
+    }
+    free(buf);
+}
+
+/* The same tangent with eight atoms of one train side by side
+ * (_epg_cpu.cpp:3286-3500 lane helpers, 3503-3695 the kernel): the layout the
+ * reference's CPU kernel picks for any run with eight atoms or more on the
+ * real subspace (_epg_cpu.cpp:10957-10965), so that the timed CPU baseline runs
+ * at the reference's speed. Orders are stored [order][lane]; every per-atom
+ * quantity is a lane vector, every event value a splat. The lane vector is
+ * GCC's generic vector extension, lowered to whatever SIMD the host has (two
+ * 128-bit NEON registers on aarch64, one AVX register on x86). A partial block
+ * repeats its first atom into the idle lanes, which are not written back.
+ * The derivative factors are formed in the kernel's own order
+ * (t1_scale = 1000*dT1/T1^2, then e1' = e1*(dt*t1_scale - r1*ddt)), so the FP32
+ * variant matches the reference's lane kernel, which rounds differently from
+ * the per-atom one above. Work items are (train, block of eight atoms),
+ * train-major. */
+#define OLANES 8
+typedef REAL lanes_t __attribute__((vector_size(sizeof(REAL) * OLANES)));
+/* The same vector at the alignment of one element: the state planes are
+ * addressed eight elements at a time from a plain array. */
+typedef REAL lanes_at __attribute__((vector_size(sizeof(REAL) * OLANES), aligned(sizeof(REAL))));
+
+static inline lanes_t lanes_ld(const REAL* p) { return *(const lanes_at*)p; }
+static inline void lanes_st(REAL* p, lanes_t v) { *(lanes_at*)p = v; }
+static inline lanes_t lanes_all(REAL x) {
+    lanes_t v;
+    for (int l = 0; l < OLANES; ++l) v[l] = x;
+    return v;
+}
+
+static void shift_lanes(REAL* plus, REAL* minus, int64_t states) {
+    for (int64_t s = 0; s + 1 < states; ++s) lanes_st(minus + s * OLANES, lanes_ld(minus + (s + 1) * OLANES));
+    lanes_st(minus + (states - 1) * OLANES, lanes_all(LIT(0.0)));
+    for (int64_t s = states - 1; s > 0; --s) lanes_st(plus + s * OLANES, lanes_ld(plus + (s - 1) * OLANES));
+    lanes_st(plus, -lanes_ld(minus));
+}
+
+/* One property for the eight lanes of the block starting at `first`; a null
+ * pointer (or an undeclared feature) reads as `identity`. */
+static lanes_t gather8(const float* p, int present, REAL identity, int64_t first, int64_t active) {
+    lanes_t v;
+    for (int l = 0; l < OLANES; ++l) v[l] = (present && p) ? (REAL)p[first + (l < active ? l : 0)] : identity;
+    return v;
+}
+
+static void run_tangent_lanes(const oracle_case* c, const oracle_direction* d,
+                              int64_t begin, int64_t end, REAL* out_real, REAL* out_imag) {
+    const int64_t S = c->state_count;
+    const int64_t W = S * OLANES;
+    const int64_t blocks = (c->atom_count + OLANES - 1) / OLANES;
+    REAL* buf = (REAL*)aligned_alloc(64, sizeof(REAL) * (size_t)(6 * W));
+    REAL *plus = buf, *minus = buf + W, *lon = buf + 2 * W;
+    REAL *dplus = buf + 3 * W, *dminus = buf + 4 * W, *dlon = buf + 5 * W;
+    const lanes_t half = lanes_all(LIT(0.5)), one = lanes_all(LIT(1.0));
+    for (int64_t work = begin; work < end; ++work) {
+        const int64_t train = work / blocks;
+        const int64_t first = (work % blocks) * OLANES;
+        const int64_t active = c->atom_count - first < OLANES ? c->atom_count - first : OLANES;
+        const int64_t ebase = train * c->event_count;
+        memset(buf, 0, sizeof(REAL) * (size_t)(6 * W));
+        lanes_st(lon, one);
+        const lanes_t t1 = gather8(c->t1_ms, 1, LIT(1.0), first, active);
+        const lanes_t t2 = gather8(c->t2_ms, 1, LIT(1.0), first, active);
+        const lanes_t dt1 = gather8(d->t1_ms, 1, LIT(0.0), first, active);
+        const lanes_t dt2 = gather8(d->t2_ms, 1, LIT(0.0), first, active);
+        const lanes_t b1 = gather8(c->b1, 1, LIT(1.0), first, active);
+        const lanes_t db1 = gather8(d->b1, c->b1 != NULL, LIT(0.0), first, active);
+        const lanes_t m0 = gather8(c->m0, 1, LIT(1.0), first, active);
+        const lanes_t dm0 = gather8(d->m0, 1, LIT(0.0), first, active);
+        const lanes_t flipz = -gather8(c->inversion, 1, LIT(1.0), first, active);
+        const lanes_t dflipz = -gather8(d->inversion, c->inversion != NULL, LIT(0.0), first, active);
+        const lanes_t r1 = lanes_all(LIT(1000.0)) / t1;
+        const lanes_t r2 = lanes_all(LIT(1000.0)) / t2;
+        const lanes_t s1 = lanes_all(LIT(1000.0)) * dt1 / (t1 * t1);
+        const lanes_t s2 = lanes_all(LIT(1000.0)) * dt2 / (t2 * t2);
+        for (int64_t e = 0; e < c->event_count; ++e) {
+            const REAL dt = (REAL)c->duration_s[ebase + e];
+            const REAL ddt = d->duration_s ? (REAL)d->duration_s[ebase + e] : LIT(0.0);
+            lanes_t e1, e2;
+            for (int l = 0; l < OLANES; ++l) {
+                e1[l] = EXP(-r1[l] * dt);
+                e2[l] = EXP(-r2[l] * dt);
+            }
+            const lanes_t e1t = e1 * (dt * s1 - r1 * ddt);
+            const lanes_t e2t = e2 * (dt * s2 - r2 * ddt);
+            for (int64_t s = 0; s < S; ++s) {
+                REAL* o = buf + s * OLANES;
+                const lanes_t p = lanes_ld(o), m = lanes_ld(o + W), z = lanes_ld(o + 2 * W);
+                lanes_st(o + 3 * W, lanes_ld(o + 3 * W) * e2 + p * e2t);
+                lanes_st(o, p * e2);
+                lanes_st(o + 4 * W, lanes_ld(o + 4 * W) * e2 + m * e2t);
+                lanes_st(o + W, m * e2);
+                lanes_st(o + 5 * W, lanes_ld(o + 5 * W) * e1 + z * e1t);
+                lanes_st(o + 2 * W, z * e1);
+            }
+            lanes_st(lon, lanes_ld(lon) + (one - e1));
+            lanes_st(dlon, lanes_ld(dlon) - e1t);
+            const uint8_t a = c->action[e];
+            if (a & A_PRE_SHIFT) {
+                shift_lanes(plus, minus, S);
+                shift_lanes(dplus, dminus, S);
+            }
+            if (c->kind[e] == 1) {
+                if (a & A_INVERSION) {
+                    for (int64_t s = 0; s < S; ++s) {
+                        REAL* o = buf + s * OLANES;
+                        const lanes_t z = lanes_ld(o + 2 * W);
+                        lanes_st(o + 5 * W, lanes_ld(o + 5 * W) * flipz + z * dflipz);
+                        lanes_st(o + 2 * W, z * flipz);
+                    }
+                } else {
+                    const REAL fl = (REAL)c->flip_rad[ebase + e];
+                    const REAL dfl = d->flip_rad ? (REAL)d->flip_rad[ebase + e] : LIT(0.0);
+                    lanes_t co, si, at;
+                    for (int l = 0; l < OLANES; ++l) {
+                        const REAL alpha = fl * b1[l];
+                        co[l] = COS(alpha);
+                        si[l] = SIN(alpha);
+                        at[l] = dfl * b1[l] + fl * db1[l];
+                    }
+                    const lanes_t ch = half * (one + co), sh = half * (one - co), hs = half * si;
+                    const lanes_t cot = -(si * at), sit = co * at;
+                    const lanes_t cht = half * cot, sht = -(half * cot), hst = half * sit;
+                    for (int64_t s = 0; s < S; ++s) {
+                        REAL* o = buf + s * OLANES;
+                        const lanes_t p = lanes_ld(o), m = lanes_ld(o + W), z = lanes_ld(o + 2 * W);
+                        const lanes_t dp = lanes_ld(o + 3 * W), dm = lanes_ld(o + 4 * W),
+                                      dz = lanes_ld(o + 5 * W);
+                        lanes_st(o + 3 * W, ch * dp + cht * p + sh * dm + sht * m - si * dz - sit * z);
+                        lanes_st(o + 4 * W, sh * dp + sht * p + ch * dm + cht * m + si * dz + sit * z);
+                        lanes_st(o + 5 * W, hs * dp + hst * p - hs * dm - hst * m + co * dz + cot * z);
+                        lanes_st(o, ch * p + sh * m - si * z);
+                        lanes_st(o + W, sh * p + ch * m + si * z);
+                        lanes_st(o + 2 * W, hs * p - hs * m + co * z);
+                    }
+                }
+            } else if (c->kind[e] == 2 && (a & A_RECORD)) {
+                for (int64_t l = 0; l < active; ++l) {
+                    const int64_t idx = (train * c->atom_count + first + l) * c->output_count
+                                        + c->output_index[e];
+                    out_real[idx] = LIT(0.0);
+                    out_imag[idx] = dm0[l] * plus[l] + m0[l] * dplus[l];
+                }
+            }
+            if (a & A_POST_SHIFT) {
+                shift_lanes(plus, minus, S);
+                shift_lanes(dplus, dminus, S);
+            }
+            if (a & A_SPOIL_AFTER) {
+                memset(plus, 0, sizeof(REAL) * (size_t)(2 * W));
+                memset(dplus, 0, sizeof(REAL) * (size_t)(2 * W));
+            } else if (a & A_SHIFT_AFTER) {
+                shift_lanes(plus, minus, S);
+                shift_lanes(dplus, dminus, S);
             }
         }
     }
@@ -1067,6 +1226,12 @@ static void* tangent_job(void* p) {
     return NULL;
 }
 
+static void* tangent_lanes_job(void* p) {
+    job* j = (job*)p;
+    run_tangent_lanes(j->c, j->d, j->begin, j->end, j->out_real, j->out_imag);
+    return NULL;
+}
+
 static void* complex_job(void* p) {
     job* j = (job*)p;
     run_forward_complex(j->c, j->o, j->begin, j->end, j->out_real, j->out_imag);
@@ -1084,7 +1249,9 @@ static void run_threads(void* (*fn)(void*), const oracle_case* c,
 
 static void run_threads_o(void* (*fn)(void*), const oracle_case* c, const oracle_direction* d,
                           const oracle_offaxis* o, REAL* out_real, REAL* out_imag, int threads) {
-    const int64_t work = c->atom_count * c->train_count;
+    const int64_t work = fn == tangent_lanes_job
+                             ? c->train_count * ((c->atom_count + OLANES - 1) / OLANES)
+                             : c->atom_count * c->train_count;
     if (threads < 1) threads = 1;
     if (threads > 256) threads = 256;
     if (work < threads) threads = work > 0 ? (int)work : 1;
@@ -1117,6 +1284,14 @@ void NAME(oracle_forward)(const oracle_case* c, REAL* out_real, REAL* out_imag,
 void NAME(oracle_tangent)(const oracle_case* c, const oracle_direction* d,
                           REAL* out_real, REAL* out_imag, int threads) {
     run_threads(tangent_job, c, d, out_real, out_imag, threads);
+}
+
+/* The tangent in the reference's eight-atom lane layout (run_tangent_lanes);
+ * its threads split the (train, atom block) items into contiguous ranges, as
+ * the reference's pool does (_epg_cpu.cpp:10910-10921). */
+void NAME(oracle_tangent_lanes)(const oracle_case* c, const oracle_direction* d,
+                                REAL* out_real, REAL* out_imag, int threads) {
+    run_threads(tangent_lanes_job, c, d, out_real, out_imag, threads);
 }
 
 void NAME(oracle_forward_complex)(const oracle_case* c, const oracle_offaxis* o,

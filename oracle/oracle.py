@@ -209,13 +209,22 @@ def forward_complex(p: Packed, precision: str = "f64", threads: int = 1) -> np.n
     return real + 1j * imag
 
 
-def tangent(p: Packed, precision: str = "f64", threads: int = 1, **direction) -> np.ndarray:
+def tangent(p: Packed, precision: str = "f64", threads: int = 1, lanes: bool | None = None,
+            **direction) -> np.ndarray:
     """One forward-mode tangent of the recorded samples' imaginary plane.
 
     ``direction`` names any of ``t1_ms, t2_ms, m0, b1, inversion`` (per atom)
     and ``duration_s, flip_rad`` (per event or per train and event). Follows
-    ``simulate_real_jvp_range`` (src/torchsim/_epg_cpu.cpp:3136-3285).
+    ``simulate_real_jvp_range`` (src/torchsim/_epg_cpu.cpp:3136-3285), or with
+    ``lanes=True`` the eight-atom lane kernel (``simulate_real_jvp_atom_lane_range``,
+    :3503-3695); the two round differently in FP32. ``lanes=None`` picks as the
+    reference's dispatch does for the real subspace (:10957-10965): the lane
+    kernel whenever the run has eight atoms or more. (The reference's train-lane
+    kernel, for fewer than eight atoms but eight trains or more, is not restated;
+    such runs take the per-atom kernel here.)
     """
+    if lanes is None:
+        lanes = p.atom_count >= 8
     dtype, _ = _dtype(precision)
     keep: list = []
     c = _case(p, keep)
@@ -236,7 +245,7 @@ def tangent(p: Packed, precision: str = "f64", threads: int = 1, **direction) ->
         raise ValueError(f"unknown tangent directions {sorted(direction)}")
     real = np.zeros(_shape(p), dtype=dtype)
     imag = np.zeros(_shape(p), dtype=dtype)
-    fn = getattr(_library(), f"oracle_tangent_{precision}")
+    fn = getattr(_library(), f"oracle_tangent{'_lanes' if lanes else ''}_{precision}")
     fn(ctypes.byref(c), ctypes.byref(d), ctypes.c_void_p(real.ctypes.data),
        ctypes.c_void_p(imag.ctypes.data), ctypes.c_int(threads))
     return imag
@@ -357,6 +366,90 @@ def second(p: Packed, seed_imag: np.ndarray, precision: str = "f64",
             for n in SECOND_ORDER[5:]:
                 side[n] = side[n][0]
     return sides[0], sides[1]
+
+
+REFERENCE_DIR = HERE / "_ref"
+
+
+def reference_module():
+    """The reference's own compiled CPU kernel (``_epg_cpu``, built by
+    ``oracle/build_ref.sh`` from the reference's sources into ``oracle/_ref``),
+    or None where no build for this machine exists."""
+    import importlib.util
+    import sysconfig
+
+    suffix = sysconfig.get_config_var("EXT_SUFFIX") or ".so"
+    path = REFERENCE_DIR / f"_epg_cpu{suffix}"
+    if not path.exists():
+        return None
+    try:
+        spec = importlib.util.spec_from_file_location("_epg_cpu", path)
+        module = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(module)
+    except (ImportError, OSError):
+        return None
+    return module
+
+
+# The reference's feature mask (_epg_cpu.cpp:95-100): which optional tissue
+# maps a call declares; an undeclared map reads as its identity.
+_TRANSMIT, _DENSITY, _INVERTING = 1 << 3, 1 << 4, 1 << 5
+
+
+def _reference_call(p: Packed, keep: list, threads: int):
+    """The 17 tissue and 9 event pointers of ``_parameters.py``'s packed order,
+    two output planes, and the scalar arguments of ``_epg_cpu.simulate``
+    (``_epg_cpu.cpp:10740-10788``) for a single-pool instant-RF real-axis run."""
+    A = p.atom_count
+    E = p.event_count
+    zeros = np.zeros(A, np.float32)
+    ones = np.ones(A, np.float32)
+    features = 0
+    tissue = [_f32(p.t1_ms), _f32(p.t2_ms)]
+    for value, bit in ((p.m0, _DENSITY), (p.b1, _TRANSMIT)):
+        tissue.append(ones if value is None else _f32(value))
+        features |= 0 if value is None else bit
+    tissue += [zeros, zeros]  # B1 phase, B0: the real axis
+    tissue.append(ones if p.inversion is None else _f32(p.inversion))
+    features |= 0 if p.inversion is None else _INVERTING
+    tissue += [zeros] * 10  # diffusion, flow and pools: absent
+    shape = (p.train_count, E)
+    events = [_f32(np.broadcast_to(p.duration_s, shape)), np.ascontiguousarray(p.kind, np.int32),
+              _f32(np.broadcast_to(p.flip_rad, shape)), np.zeros(shape, np.float32),
+              np.ascontiguousarray(p.action, np.uint8),
+              np.ascontiguousarray(p.output_index, np.int32), np.zeros(E, np.int32),
+              np.zeros(E, np.float32), np.zeros(E, np.float32)]
+    keep += tissue + events
+    scalars = (A, p.train_count, E, int(p.state_count), p.output_count, threads, 1, 0.0, 0.0,
+               1, 1, 0, 1.0, 0, 1.0, 0, features, 0, 0, 0)
+    return tissue, events, scalars
+
+
+def reference_forward(ref, p: Packed, threads: int = 1) -> np.ndarray:
+    """The imaginary output plane of the reference's ``simulate``."""
+    keep: list = []
+    tissue, events, scalars = _reference_call(p, keep, threads)
+    real = np.zeros(_shape(p), np.float32)
+    imag = np.zeros(_shape(p), np.float32)
+    ref.simulate([a.ctypes.data for a in (*tissue, *events, real, imag)] + [0] * 13, *scalars)
+    return imag
+
+
+def reference_jvp(ref, p: Packed, column: int, threads: int = 1) -> np.ndarray:
+    """The imaginary tangent plane of the reference's ``simulate_jvp``
+    (``_epg_cpu.cpp:11017-11148``) along one tissue property, a one-hot
+    direction on tissue slot ``column`` (0 T1, 1 T2, 2 M0, 3 B1, 6 inversion)."""
+    keep: list = []
+    tissue, events, scalars = _reference_call(p, keep, threads)
+    tangents = [np.zeros(p.atom_count, np.float32) for _ in range(17)]
+    tangents[column] = np.ones(p.atom_count, np.float32)
+    tangents += [np.zeros((p.train_count, p.event_count), np.float32) for _ in range(3)]
+    keep += tangents
+    real = np.zeros(_shape(p), np.float32)
+    imag = np.zeros(_shape(p), np.float32)
+    ref.simulate_jvp([a.ctypes.data for a in (*tissue, *events, *tangents, real, imag)]
+                     + [0] * 13, *scalars)
+    return imag
 
 
 def cpu_threads() -> int:

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Run in a container that has the reference checkout (default /root/reference)
+Run in a container that has the reference checkout (the argument, else
+$TORCHSIM_REFERENCE, else /root/reference)
 and a C++ compiler:
 
     python tests/golden/make_golden.py [REFERENCE_ROOT] [CASE ...]
@@ -646,7 +647,8 @@ CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0"
 
 def main() -> None:
     args = sys.argv[1:]
-    root = Path(args[0] if args and not args[0] in CASES else "/root/reference")
+    root = Path(args[0] if args and args[0] not in CASES
+                else os.environ.get("TORCHSIM_REFERENCE", "/root/reference"))
     wanted = [a for a in args if a in CASES] or list(CASES)
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     ts = _import_reference(root)

@@ -51,6 +51,10 @@ def packed_complex_from_golden(d, prefix: str = "") -> O.Packed:
     return p
 
 
+reference_module = O.reference_module
+reference_jvp = O.reference_jvp
+
+
 def max_rel(actual, expected) -> float:
     """max |a - e| / max |e|, the normalisation of the reference's CUDA parity
     tests (tests/sequence/test_cuda_parity.py:137-138)."""

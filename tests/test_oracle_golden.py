@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.helpers import max_rel, packed_complex_from_golden, packed_from_golden
+from tests.helpers import (max_rel, packed_complex_from_golden, packed_from_golden,
+                           reference_jvp, reference_module)
 
 FORWARD_CASES = ["mrf880", "mrf_prep", "fse_cpmg"]
 KEYS = {"T1": "t1_ms", "T2": "t2_ms", "B1": "b1", "M0": "m0", "inv_efficiency": "inversion"}
@@ -33,13 +34,60 @@ def test_fp64_oracle_matches_reference(golden, name):
 
 @pytest.mark.parametrize("name", ["mrf880", "mrf_prep"])
 def test_oracle_tangents_match_reference_jacobian(golden, name):
+    """The FP32 port picks the reference's kernel by atom count (eight atoms or
+    more: the eight-atom lane kernel) and reproduces its Jacobian bit for bit:
+    mrf880 has 8 atoms (lane kernel), mrf_prep 5 (per-atom kernel)."""
     d = golden(name)
     p = packed_from_golden(d)
     for col, prop in enumerate(d["jacobian_names"]):
         ref = -d["jacobian"][:, col].real  # the API returns 1j * (i * tangent)
-        for precision, tol in (("f32", 1e-6), ("f64", 5e-6)):
-            t = O.tangent(p, precision, **{KEYS[str(prop)]: 1.0})
-            assert max_rel(t, ref) < tol, (prop, precision)
+        t = O.tangent(p, "f32", **{KEYS[str(prop)]: 1.0})
+        assert np.array_equal(t, ref), prop
+        assert max_rel(O.tangent(p, "f64", **{KEYS[str(prop)]: 1.0}), ref) < 5e-6, prop
+
+
+def test_lane_and_per_atom_tangents_agree():
+    """The two FP32 layouts differ only in rounding, on a ragged atom count
+    (a partial block of eight) and two trains."""
+    rng = np.random.default_rng(3)
+    atoms, events = 21, 120
+    flip = np.deg2rad(rng.uniform(5, 70, (2, events))).astype(np.float32)
+    kind = np.ones(events, np.int32)
+    kind[1::2] = 2
+    action = np.where(kind == 2, 32 | 16, 0).astype(np.uint8)
+    out_index = np.where(kind == 2, np.cumsum(kind == 2) - 1, -1).astype(np.int32)
+    duration = np.full((2, events), 5e-3, np.float32)
+    t1 = rng.uniform(300, 2000, atoms).astype(np.float32)
+    p = O.Packed(t1, (0.1 * t1).astype(np.float32), duration, kind, flip, action, out_index, 12,
+                 b1=rng.uniform(0.8, 1.2, atoms).astype(np.float32))
+    for key in ("t1_ms", "t2_ms", "b1", "flip_rad", "duration_s"):
+        a = O.tangent(p, "f32", lanes=True, threads=3, **{key: 1.0})
+        b = O.tangent(p, "f32", lanes=False, **{key: 1.0})
+        c = O.tangent(p, "f64", **{key: 1.0})
+        assert max_rel(a, c) < 2e-5 and max_rel(b, c) < 2e-5, key
+        assert max_rel(a, b) < 2e-5, key
+
+
+def test_lane_tangent_is_bitwise_the_reference_kernel():
+    """Against the reference's own compiled CPU kernel (built from its sources
+    where they lie into oracle/_ref), on the dictionary sequence at 45 atoms (a
+    partial block), through its ``simulate_jvp`` entry point."""
+    ref = reference_module()
+    if ref is None:
+        pytest.skip("the reference's CPU kernel is not built here")
+    from torchsim_gb300.sequence import mrf_events
+
+    rng = np.random.default_rng(5)
+    atoms = 45
+    flip = np.concatenate([np.linspace(5, 60, 100), np.linspace(60, 2, 100)]).astype(np.float32)
+    ev = mrf_events(flip, 10.0)
+    t1 = np.exp(rng.uniform(np.log(100), np.log(3000), atoms)).astype(np.float32)
+    t2 = np.minimum(np.exp(rng.uniform(np.log(10), np.log(300), atoms)), 0.999 * t1).astype(np.float32)
+    b1 = rng.uniform(0.8, 1.2, atoms).astype(np.float32)
+    p = O.Packed(t1, t2, ev.duration, ev.kind, ev.flip, ev.action, ev.output_index, 16, b1=b1)
+    for col, key in ((0, "t1_ms"), (1, "t2_ms"), (3, "b1")):
+        expected = reference_jvp(ref, p, col)
+        assert np.array_equal(O.tangent(p, "f32", threads=4, **{key: 1.0}), expected), key
 
 
 def test_public_signal_is_minus_raw_plane(golden):
