@@ -840,8 +840,10 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:  
     draw_t1 = np.exp(rng.uniform(np.log(100), np.log(3000), 4096))
     draw_t2 = np.exp(rng.uniform(np.log(10), np.log(300), 4096))
     draw_m0 = rng.uniform(0.5, 1.5, 4096)
-    est = NonlinearLeastSquares(None, bounds=bounds).fit(
-        parameters=torch.tensor(np.stack([draw_t1, draw_t2, draw_m0], 1)))
+    from torchsim_gb300 import MRFSimulator
+
+    est = NonlinearLeastSquares(MRFSimulator(flip=mrf_schedule(), TR=10.0, states=10),
+                                bounds=bounds).fit(T1=draw_t1, T2=draw_t2, M0=draw_m0)
     start = est._start
     gaps = rng.exponential(1.0 / rate, requests)
     arrivals = np.cumsum(gaps) - gaps[0]
@@ -874,8 +876,8 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:  
 
     warm = GNServer(program, 10, bounds, start, loop, budget_bytes=2 << 30, device=device)
     warm.serve([MapRequest(made[0][0][:4096], made[0][1][:4096], id=0)], realtime=False)
-    loop.minimize(program, made[0][0][:4096], start, bounds, 10, b1=made[0][1][:4096])
-    PlainGaussNewton(TrustRegion(), max_iterations=10).minimize(
+    loop.minimize_program(program, made[0][0][:4096], start, bounds, 10, b1=made[0][1][:4096])
+    PlainGaussNewton(TrustRegion(), max_iterations=10).minimize_program(
         program, made[0][0][:4096], start, bounds, 10, b1=made[0][1][:4096])
     torch.cuda.synchronize()
 

@@ -19,21 +19,153 @@ def rel(a, b):
 
 
 def test_gn_matches_reference_nlls(cuda, golden):
-    """The reference's NonlinearLeastSquares (LM, 20 steps) on noisy MRF."""
+    """The reference's NonlinearLeastSquares (LM, 20 steps) on noisy MRF,
+    called as the reference's fixture called it: B1 measured separately,
+    drawn over in fit() and given to map()."""
     from torchsim_gb300 import MRFSimulator
-    from torchsim_gb300.recon import GaussNewton, NonlinearLeastSquares, TrustRegion
+    from torchsim_gb300.recon import NonlinearLeastSquares
 
     d = golden("gn_mrf")
     bounds = {k: tuple(d["bounds"][i]) for i, k in enumerate(("T1", "T2", "M0"))}
-    est = NonlinearLeastSquares(MRFSimulator(flip=d["flip_deg"], TR=10.0, states=10), bounds=bounds,
-                                loop=GaussNewton(TrustRegion(), max_iterations=20))
-    est.fit(parameters=torch.from_numpy(d["start"][None, :]))
+    est = NonlinearLeastSquares(MRFSimulator(flip=torch.from_numpy(d["flip_deg"]), TR=10.0,
+                                             states=10), bounds=bounds)
+    est.fit(T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), known={"B1": (0.8, 1.2)},
+            seed=0)
+    assert torch.equal(est._start, torch.from_numpy(d["start"]))
     maps = est.map(torch.from_numpy(d["measured"]).to(cuda), known={"B1": torch.from_numpy(d["b1"])})
     for name, key in (("T1", "map_t1"), ("T2", "map_t2"), ("M0", "map_m0")):
+        assert maps[name].device == torch.device(cuda)
         assert rel(maps[name].cpu().numpy(), d[key]) <= 2e-3, name
     # The reference converged all 16 within its 20 steps, the last on its
     # 20th; with FP64 normal equations a slow voxel may need one more.
     assert est.unconverged <= 1
+
+
+def test_nlls_call_of_the_mapping_stack_verbatim(golden):
+    """The call stack's own form: NonlinearLeastSquares(MRFSimulator(...)
+    .bind(B1=...), bounds=...).fit(...).map(signals), host tensors in and
+    out; the same maps as the reference's estimator on the fixture."""
+    from torchsim_gb300 import MRFSimulator
+    from torchsim_gb300.recon import NonlinearLeastSquares
+
+    d = golden("gn_mrf")
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
+    maps = NonlinearLeastSquares(
+        MRFSimulator(flip=torch.from_numpy(d["flip_deg"]), TR=10.0, states=10).bind(
+            B1=torch.from_numpy(d["b1"])),
+        bounds=bounds,
+    ).fit(T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), seed=0).map(
+        torch.from_numpy(d["measured"]))
+    for name, key in (("T1", "map_t1"), ("T2", "map_t2"), ("M0", "map_m0")):
+        assert maps[name].device.type == "cpu"
+        assert rel(maps[name].numpy(), d[key]) <= 2e-3, name
+
+
+def test_block_route_agrees_with_fused_route(cuda):
+    """The same operator through the reference's block loop (Jacobian blocks
+    from the fused forward + tangents sweep, damped step by Cholesky) and
+    through the fused device route."""
+    from torchsim_gb300 import MRFSimulator
+    from torchsim_gb300.recon import GaussNewton, ModelOperator, TrustRegion
+    from tests.helpers import mrf_schedule
+
+    _, sig, (t1, t2, m0, b1) = _signals(cuda, 256, 6)
+    sim = MRFSimulator(flip=mrf_schedule(), TR=10.0, states=10).bind(
+        B1=torch.from_numpy(b1).to(cuda))
+    op = ModelOperator(sim, "T1", "T2", "M0", bounds=BOUNDS, amplitude=False)
+    start = op.initial((256,), T1=1000.0, T2=80.0, M0=1.0).to(cuda)
+    loop = GaussNewton(TrustRegion(), max_iterations=10)
+    fused = loop.minimize(op, sig, start)
+    blocks = loop._minimize_blocks(op, sig, start)
+    a, b = op.split(fused.x), op.split(blocks.x)
+    for name in ("T1", "T2", "M0"):
+        e = ((a[name] - b[name]).abs() / b[name].abs()).cpu().numpy()
+        assert np.median(e) <= 1e-4 and np.quantile(e, 0.95) <= 1e-2, name
+    assert fused.cost.ndim == 1 and blocks.cost.ndim == 1
+    assert float(blocks.cost[-1]) <= float(blocks.cost[0])
+    np.testing.assert_allclose(float(fused.cost[-1]), float(blocks.cost[-1]), rtol=1e-3)
+
+
+def test_model_operator_products_and_blocks(cuda):
+    """jacobian against central differences of A; <J d, v> = <d, J^H v>;
+    the amplitude's columns are the model itself, times 1 and times i; the
+    block route honours a per-voxel B1 map through select()."""
+    from torchsim_gb300 import MRFSimulator
+    from torchsim_gb300.recon import ModelOperator
+    from tests.helpers import draw_tissue, mrf_schedule
+
+    t1, t2, b1 = draw_tissue(9, 64)
+    sim = MRFSimulator(flip=mrf_schedule()[:200], TR=10.0, states=10).bind(
+        B1=torch.from_numpy(b1).to(cuda))
+    op = ModelOperator(sim, "T1", "T2", bounds={"T1": (50.0, 5000.0), "T2": (2.0, None)},
+                       scale={"T2": 2.0})
+    x = op.initial((64,), T1=torch.from_numpy(t1), T2=torch.from_numpy(t2),
+                   amplitude=0.8 - 0.3j).to(cuda)
+    blocks = op.jacobian(x)
+    assert blocks.shape == (64, 4, 200)
+    signal = op.A(x)
+    np.testing.assert_allclose(blocks[:, 2].cpu().numpy(), (signal / (0.8 - 0.3j)).cpu().numpy(),
+                               rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(blocks[:, 3].cpu().numpy(),
+                               (1j * signal / (0.8 - 0.3j)).cpu().numpy(), rtol=1e-5, atol=1e-7)
+    for c in range(2):
+        h = 1e-2
+        dx = torch.zeros_like(x)
+        dx[:, c] = h
+        fd = (op.A(x + dx) - op.A(x - dx)) / (2 * h)
+        assert rel(blocks[:, c].cpu().numpy(), fd.cpu().numpy()) <= 2e-3, c
+    g = torch.Generator(device=cuda).manual_seed(0)
+    d = torch.randn(x.shape, device=cuda, generator=g)
+    v = torch.complex(torch.randn(signal.shape, device=cuda, generator=g),
+                      torch.randn(signal.shape, device=cuda, generator=g))
+    left = (op.A_jvp(x, d).conj() * v).real.sum()
+    right = (d * op.A_vjp(x, v)).sum()
+    assert abs(float(left - right)) <= 1e-4 * abs(float(left))
+    keep = torch.arange(64, device=cuda) % 3 == 0
+    np.testing.assert_allclose(op.select(keep).A(x[keep]).cpu().numpy(),
+                               signal[keep].cpu().numpy(), rtol=1e-6, atol=1e-7)
+
+
+def test_nlls_uncertainty(cuda, golden):
+    """map(uncertainty=True): the standard deviation the stated noise leaves
+    on each map (the inverse Fisher diagonal at the answer); zero without
+    noise."""
+    from torchsim_gb300 import MRFSimulator
+    from torchsim_gb300.design import crlb
+    from torchsim_gb300.recon import NonlinearLeastSquares
+
+    d = golden("gn_mrf")
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
+    b1 = torch.from_numpy(d["b1"]).to(cuda)
+    sim = MRFSimulator(flip=torch.from_numpy(d["flip_deg"]), TR=10.0, states=10).bind(B1=b1)
+    sigma = 0.01
+    est = NonlinearLeastSquares(sim, bounds=bounds).fit(
+        T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), noise_std=sigma, seed=0)
+    maps, spread = est.map(torch.from_numpy(d["measured"]).to(cuda), uncertainty=True)
+    _, jac = sim.jacobian(["T1", "T2", "M0"], T1=maps["T1"], T2=maps["T2"], M0=maps["M0"])
+    expected = crlb(jac / sigma, singular="infinite").sqrt()
+    for k, name in enumerate(("T1", "T2", "M0")):
+        assert torch.all(spread[name] > 0)
+        assert rel(spread[name].cpu().numpy(), expected[:, k].cpu().numpy()) <= 1e-5, name
+    quiet = NonlinearLeastSquares(sim, bounds=bounds).fit(
+        T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), seed=0)
+    _, none = quiet.map(torch.from_numpy(d["measured"]).to(cuda), uncertainty=True)
+    assert all(bool((v == 0).all()) for v in none.values())
+
+
+def test_natural_of_matches_the_reference_inverse(cuda, golden):
+    """The device inverse of the bounds (tsg_gn_natural, FP64) on the
+    reference's own free variables gives the reference's to_natural
+    (tests/golden/bounds.npz)."""
+    from torchsim_gb300.recon import config_of, natural_of
+
+    dd = golden("bounds")
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, None), "M0": (None, 5.0)}
+    config = config_of(bounds, 1e-2, 1e-8, 1e-8, 8)
+    u = torch.from_numpy(dd["free"][:, :3]).to(cuda)
+    got = natural_of(u, config).double().cpu().numpy()
+    want = dd["back"][:, :3]
+    np.testing.assert_allclose(got, want, rtol=2e-7, atol=1e-5)
 
 
 def _signals(cuda, V, seed, noise=True, pulses=None):
@@ -61,7 +193,7 @@ def test_gn_noiseless_recovery(cuda):
 
     prog, sig, (t1, t2, m0, b1) = _signals(cuda, 500, 1, noise=False)
     start = torch.tensor([1000.0, 80.0, 1.0])
-    sol = GaussNewton(TrustRegion(), max_iterations=40).minimize(
+    sol = GaussNewton(TrustRegion(), max_iterations=40).minimize_program(
         prog, sig, start, BOUNDS, 10, b1=torch.from_numpy(b1))
     x = sol.x.cpu().numpy()
     for k, truth in enumerate((t1, t2, m0)):
@@ -75,9 +207,10 @@ def test_fused_and_plain_forms_agree(cuda):
     prog, sig, (t1, t2, m0, b1) = _signals(cuda, 300, 2)
     start = torch.tensor([1000.0, 80.0, 1.0])
     b1t = torch.from_numpy(b1)
-    fused = GaussNewton(TrustRegion(), max_iterations=10).minimize(prog, sig, start, BOUNDS, 10, b1=b1t)
-    plain = PlainGaussNewton(TrustRegion(), max_iterations=10).minimize(prog, sig, start, BOUNDS, 10,
-                                                                       b1=b1t)
+    fused = GaussNewton(TrustRegion(), max_iterations=10).minimize_program(
+        prog, sig, start, BOUNDS, 10, b1=b1t)
+    plain = PlainGaussNewton(TrustRegion(), max_iterations=10).minimize_program(
+        prog, sig, start, BOUNDS, 10, b1=b1t)
     for k in range(3):
         a, b = fused.x[:, k].cpu().numpy(), plain.x[:, k].cpu().numpy()
         assert np.median(np.abs(a - b) / np.abs(b)) <= 1e-3, k

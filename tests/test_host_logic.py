@@ -56,16 +56,105 @@ def test_bounds_round_trip():
 
 
 def test_nlls_start_is_median_and_checked():
+    from torchsim_gb300 import MRFSimulator
     from torchsim_gb300.recon import NonlinearLeastSquares
 
-    est = NonlinearLeastSquares(None, bounds={"T1": (50.0, 5000.0), "T2": (2.0, 1000.0),
-                                              "M0": (0.0, 5.0)})
-    params = torch.tensor([[100.0, 10.0, 1.0], [300.0, 30.0, 2.0], [200.0, 20.0, 3.0]])
-    est.fit(parameters=params)
+    sim = MRFSimulator(flip=[10.0, 20.0], TR=10.0)
+    est = NonlinearLeastSquares(sim, bounds={"T1": (50.0, 5000.0), "T2": (2.0, 1000.0),
+                                             "M0": (0.0, 5.0)})
+    est.fit(T1=[100.0, 300.0, 200.0], T2=[10.0, 30.0, 20.0], M0=[1.0, 2.0, 3.0])
     assert est._start.tolist() == [200.0, 20.0, 2.0]
-    bad = NonlinearLeastSquares(None, bounds={"T1": (50.0, 150.0)})
+    assert est.unknown == ("T1", "T2", "M0") and est.known == ()
     with pytest.raises(ValueError):
-        bad.fit(parameters=params)
+        NonlinearLeastSquares(sim, bounds={"T1": (50.0, 150.0)}).fit(
+            T1=[100.0, 300.0, 200.0], T2=[10.0, 30.0, 20.0], M0=[1.0, 2.0, 3.0])
+    with pytest.raises(ValueError):
+        NonlinearLeastSquares(sim, bounds={"B1": (0.5, 1.5)}).fit(T1=(100.0, 3000.0))
+    with pytest.raises(ValueError):
+        est.fit(T1=(100.0, 3000.0), known={"T1": (100.0, 200.0)})
+    with pytest.raises(RuntimeError):
+        NonlinearLeastSquares(None).fit(T1=(100.0, 3000.0))
+    with pytest.raises(RuntimeError):
+        NonlinearLeastSquares(sim).map(torch.zeros(3, 2, dtype=torch.complex64))
+
+
+def test_nlls_start_is_the_references(golden):
+    """fit() draws the training parameters with the reference's generator and
+    order (unknowns, then the measured properties; estimators/_mapping.py:
+    339-361) and starts at their median: the reference's own start on the
+    gn_mrf fixture, bit for bit."""
+    from torchsim_gb300 import MRFSimulator
+    from torchsim_gb300.recon import NonlinearLeastSquares
+
+    d = golden("gn_mrf")
+    sim = MRFSimulator(flip=torch.from_numpy(d["flip_deg"]), TR=10.0, states=10)
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
+    est = NonlinearLeastSquares(sim, bounds=bounds).fit(
+        T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), known={"B1": (0.8, 1.2)}, seed=0)
+    assert torch.equal(est._start, torch.from_numpy(d["start"]))
+    bound = NonlinearLeastSquares(sim.bind(B1=torch.from_numpy(d["b1"])), bounds=bounds).fit(
+        T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), seed=0)
+    assert torch.equal(bound._start, torch.from_numpy(d["start"]))
+
+
+def test_bind_holds_values_on_a_copy():
+    from torchsim_gb300 import MRFSimulator
+
+    sim = MRFSimulator(flip=[10.0, 20.0], TR=10.0, states=8)
+    held = sim.bind(B1=torch.tensor([0.9, 1.1]), T1=1000.0, states=12)
+    assert "B1" not in sim.protocol and sim.protocol["states"] == 8
+    assert set(held.bound) == {"B1", "T1"} and held.protocol["states"] == 12
+    assert held.protocol["flip"] == [10.0, 20.0]
+    assert "T2" in held.exposes and held.accepts == held.exposes
+
+
+def test_model_operator_host_logic():
+    """ModelOperator's channels, its start (a value per unknown, the middle of
+    a two-sided bound, the amplitude) and split() back, on the host."""
+    from torchsim_gb300 import MRFSimulator
+    from torchsim_gb300.recon import ModelOperator
+
+    sim = MRFSimulator(flip=[10.0, 20.0], TR=10.0)
+    op = ModelOperator(sim, "T1", "T2", bounds={"T1": (50.0, 5000.0), "T2": (2.0, None)},
+                       scale={"T2": 4.0})
+    assert op.channels == 4 and op.names == ("T1", "T2", "amplitude.real", "amplitude.imag")
+    x = op.initial((5,), T2=torch.linspace(10.0, 90.0, 5), amplitude=2.0 - 1.0j)
+    assert x.shape == (5, 4)
+    back = op.split(x)
+    torch.testing.assert_close(back["T1"], torch.full((5,), 2525.0), rtol=1e-5, atol=0)
+    torch.testing.assert_close(back["T2"], torch.linspace(10.0, 90.0, 5), rtol=1e-5, atol=0)
+    assert torch.equal(back["amplitude"], torch.full((5,), 2.0 - 1.0j))
+    with pytest.raises(ValueError):
+        ModelOperator(sim)
+    with pytest.raises(ValueError):
+        ModelOperator(sim, "T1", bounds={"T2": (1.0, 2.0)})
+    with pytest.raises(ValueError):
+        op.initial((2,))  # T2 has no two-sided bound
+    with pytest.raises(ValueError):
+        op.initial((2,), T1=50.0, T2=10.0)  # on the bound
+    with pytest.raises(ValueError):
+        op.split(torch.zeros(2, 3))
+
+
+def test_natural_and_chain_factor_match_the_reference(golden):
+    """to_natural on the reference's free variables gives the reference's own
+    to_natural output (_bounds.py:77-105), and widen is its derivative."""
+    import numpy as np
+
+    from torchsim_gb300.recon import to_natural, widen
+
+    d = golden("bounds")
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, None), "M0": (None, 5.0)}
+    names = ("T1", "T2", "M0", "B1")
+    free = torch.from_numpy(d["free"])
+    np.testing.assert_allclose(to_natural(free, bounds, names).numpy(), d["back"], rtol=1e-12,
+                               atol=1e-12)
+    u = free.clone().requires_grad_(True)
+    to_natural(u, bounds, names).sum().backward()
+    # torch's softplus takes its linear branch above 20, where its derivative
+    # is 1 rather than sigmoid(u) = 1 - O(1e-9).
+    np.testing.assert_allclose(widen(bounds, names, free).numpy(), u.grad.numpy(), rtol=1e-9,
+                               atol=1e-300)
 
 
 def test_autotune_cache(tmp_path, monkeypatch):

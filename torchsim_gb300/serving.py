@@ -264,7 +264,7 @@ def serve_plain(program: Program, states: int, bounds: dict, start: torch.Tensor
             continue
         req = pending.popleft()
         req.admitted = time.perf_counter() - t0
-        sol = loop.minimize(program, req.measured, start, bounds, states, b1=req.b1)
+        sol = loop.minimize_program(program, req.measured, start, bounds, states, b1=req.b1)
         torch.cuda.synchronize()
         req.maps = {name: sol.x[:, k] for k, name in enumerate(UNKNOWN)}
         req.completed = time.perf_counter() - t0

@@ -16,6 +16,7 @@ kernel pass together with the signal.
 
 from __future__ import annotations
 
+import copy
 from collections.abc import Sequence
 from dataclasses import dataclass
 from typing import Any
@@ -82,6 +83,35 @@ class _EpgSimulator:
 
     def __init__(self, **protocol: Any) -> None:
         self.protocol = dict(protocol)
+
+    # -- what is held (model/_state_machine.py:560-640) --------------------
+    @property
+    def exposes(self) -> tuple[str, ...]:
+        """The tissue properties this simulator takes."""
+        return tuple(self.properties)
+
+    accepts = exposes
+
+    @property
+    def bound(self) -> dict[str, Any]:
+        """The tissue properties fixed on this simulator (a value or a map)."""
+        return {k: v for k, v in self.protocol.items() if k in self.properties}
+
+    def bind(self, **values: Any) -> _EpgSimulator:
+        """This simulator with more fixed on it: properties (a measured B1
+        map, a known T1), protocol arguments or settings (``states``)
+        alike, held for every later call (``Simulator.bind``,
+        ``model/_state_machine.py:576-594``). A copy; this one is unchanged."""
+        held = copy.copy(self)
+        held.protocol = {**self.protocol, **values}
+        return held
+
+    def to(self, device: torch.device | str) -> _EpgSimulator:
+        """A copy with every tensor it holds on ``device``."""
+        held = copy.copy(self)
+        held.protocol = {k: (v.to(device) if isinstance(v, torch.Tensor) else v)
+                         for k, v in self.protocol.items()}
+        return held
 
     # -- to be provided by a sequence ------------------------------------
     def events(self, **protocol: Any) -> PackedEvents:  # pragma: no cover - abstract
