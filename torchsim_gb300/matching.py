@@ -8,12 +8,14 @@ scale (proton density and receive phase), its size and the atoms' parameter
 values.
 
 The search is one tensor-core kernel per chunk of voxels
-(``tsg_match_screen``): fp16 products (normalized values, 11-bit significand)
-accumulated in FP32 in tensor memory, with the selection of each voxel's best
-32 atoms fused into the epilogue, so the voxel x atom score matrix never
-exists. The candidates are then rescored exactly in FP32 against the complex
-signals (``tsg_match_rescore``) and the top k kept, so the fp16 screen only
-narrows which atoms are compared exactly.
+(``tsg_match_screen``): fp16 products accumulated in FP32 in tensor memory,
+with the selection of each voxel's best 32 atoms fused into the epilogue, so
+the voxel x atom score matrix never exists. Each atom enters the screen as two
+fp16 rows (its value and the rounding remainder), so the screen's scores carry
+the atoms to ~22 bits and only the query's rounding, which shifts near-parallel
+atoms alike, is left. The candidates are then rescored exactly in FP32 against
+the complex signals (``tsg_match_rescore``) and the top k kept, so the screen
+only narrows which atoms are compared exactly.
 
 Group matching (``groups``) is the reference's option for dictionaries too
 large to search exhaustively (``estimators/_grouped.py``; Cauley, Setsompop,
@@ -224,7 +226,19 @@ class DictionaryMatcher:
             self._screen_atoms, self._complex_atoms = im, False
         else:
             self._screen_atoms, self._complex_atoms = torch.cat((re, im), dim=1), True
-        screen = _pad8(self._screen_atoms).to(torch.float16)
+        # Each screen atom is a pair of fp16 rows, hi and lo = (atom - hi),
+        # side by side along the contraction: the query meets both, so its
+        # product is <q, atom> with the atom carried to ~22 bits. What rounding
+        # is left is the query's own, and that error is common to every atom
+        # of a voxel: <q - s, d1 - d2> is tiny for two nearly parallel atoms,
+        # so the screen ranks neighbours of a dense dictionary the way the
+        # exact scores do. Values are scaled by sqrt(contrasts) first so that
+        # the lo parts stay clear of fp16's subnormal range.
+        self._screen_scale = float(self._screen_atoms.shape[1]) ** 0.5
+        scaled = self._screen_atoms * self._screen_scale
+        hi = scaled.to(torch.float16)
+        lo = (scaled - hi.float()).to(torch.float16)
+        screen = torch.cat((_pad8(hi), _pad8(lo)), dim=1)
         # The kernel reads atom i from row pos(i) (bit 1 of i moved to bit 5,
         # bits 2-5 down by one, within blocks of 64) of a matrix padded to a
         # multiple of 64 rows, so neighbouring atoms fall in different
@@ -257,7 +271,8 @@ class DictionaryMatcher:
         else:
             a, b = s.real, s.imag
         rows = torch.stack((a, b), dim=1).reshape(2 * s.shape[0], -1)
-        return _pad8(rows).to(torch.float16).contiguous()
+        rows = _pad8(rows * self._screen_scale).to(torch.float16)
+        return torch.cat((rows, rows), dim=1).contiguous()
 
     @torch.no_grad()
     def match(self, signals: torch.Tensor) -> MatchResult:
