@@ -282,9 +282,10 @@ int tsg_epg_adjoint(const tsg_program* program, const tsg_tissue* tissue, int64_
  * until the process exits; the entry point calls no cudaMalloc, cudaFree or
  * other allocating routine. A problem whose scratch exceeds the array is
  * rejected with TSG_ERR_CAPACITY (tsg_epg_adjoint_plan gives the sizes).
- * The first call on a device resolves the array's device address on that
- * device (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the one array: calls whose work overlaps on the
+ * The first call on a device (and the first after the device's context is
+ * replaced, e.g. by cudaDeviceReset) resolves the array's device address in
+ * the current context (cudaGetSymbolAddress); make that first call before
+ * any stream capture. All calls share the one array: calls whose work overlaps on the
  * GPU (other streams, other host threads) race on it and must be ordered by
  * the caller. Nothing a previous call left in it is read. */
 int tsg_epg_adjoint_noalloc(const tsg_program* program, const tsg_tissue* tissue,

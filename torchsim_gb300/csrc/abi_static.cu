@@ -10,6 +10,8 @@
 // (the state checkpoints and the per-warp gradient partials) in one
 // file-scope device array of fixed size, so it calls no cudaMalloc,
 // cudaFree or allocating routine of any library.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "tsg_internal.h"
@@ -34,21 +36,56 @@ static __device__ __align__(256) unsigned char g_scratch[kStaticScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_address[kMaxDevices] = {};
 
-// Resolves the array's address on the current device, once per device.
+// The array's address as resolved in one context of a device. A module (and
+// so the array) lives in a context: after cudaDeviceReset, or in another
+// context on the same device, the array is loaded again elsewhere, so an
+// address is reused only while the context it was resolved in is current.
+struct Resolved {
+    CUcontext context;
+    void* address;
+};
+Resolved g_resolved[kMaxDevices] = {};
+
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+
+// The driver's cuCtxGetCurrent, through the runtime's entry-point query (the
+// library links only the CUDA runtime).
+CtxGetCurrent context_query() {
+    static CtxGetCurrent fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return CtxGetCurrent(nullptr);
+        return reinterpret_cast<CtxGetCurrent>(p);
+    }();
+    return fn;
+}
+
+// Resolves the array's address for the current device and context, once per
+// context (cudaGetSymbolAddress also makes the device's primary context
+// current on a thread that has none yet).
 int scratch_address(void** out) {
     int device = 0;
     TSG_CUDA(cudaGetDevice(&device));
     if (device < 0 || device >= kMaxDevices) return fail(TSG_ERR_CAPACITY, "device index beyond 64");
+    CtxGetCurrent query = context_query();
+    if (query == nullptr) return fail(TSG_ERR_CUDA, "cuCtxGetCurrent is unavailable");
     std::lock_guard<std::mutex> guard(g_setup_mutex);
-    if (g_scratch_address[device] == nullptr) {
+    CUcontext context = nullptr;
+    if (query(&context) != CUDA_SUCCESS) return fail(TSG_ERR_CUDA, "cuCtxGetCurrent failed");
+    Resolved& slot = g_resolved[device];
+    if (context == nullptr || slot.address == nullptr || slot.context != context) {
         void* ptr = nullptr;
         cudaError_t err = cudaGetSymbolAddress(&ptr, g_scratch);
         if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(scratch)");
-        g_scratch_address[device] = ptr;
+        if (query(&context) != CUDA_SUCCESS || context == nullptr)
+            return fail(TSG_ERR_CUDA, "no current context after resolving the scratch array");
+        slot = Resolved{context, ptr};
     }
-    *out = g_scratch_address[device];
+    *out = slot.address;
     return TSG_OK;
 }
 
