@@ -278,34 +278,41 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
                  "form": "forward + one forward-and-tangent pass per column (T1, T2, B1)"}
         del one
 
-    # End to end through the public API: pinned host tissue in, pinned host
-    # signal and Jacobian out, copies inside the timed region.
+    # End to end through the public API: the call a user makes with host
+    # tensors, torchsim_gb300.mrf_sim(flip, TR, T1, T2, B1=..., diff=(T1, T2,
+    # B1), states=20) on CPU tensors, returning the signal and Jacobian as CPU
+    # tensors; the tissue upload, the sweep and the copies back (chunked, each
+    # overlapping the next chunk's sweep) are inside the timed region.
     e2e = None
     if rank == 0 and not args.skip_e2e:
-        host_t = [torch.from_numpy(a).pin_memory() for a in (t1, t2, b1)]
-        host_sig = torch.empty((atoms, PULSES), dtype=torch.complex64).pin_memory()
-        host_jac = torch.empty((atoms, 3, PULSES), dtype=torch.complex64).pin_memory()
+        import torchsim_gb300 as ts
 
-        host_maps = engine.TissueMaps(host_t[0], host_t[1], None, host_t[2], None)
+        host_flip = torch.from_numpy(flip)
+        host_t = [torch.from_numpy(a) for a in (t1, t2, b1)]
 
         def e2e_step():
-            engine.forward_tangents_host(program, host_maps, STATES, names, host_sig, host_jac,
-                                         chunks=16, launch=launch, device=device)
+            return ts.mrf_sim(host_flip, 10.0, host_t[0], host_t[1], B1=host_t[2],
+                              diff=names, states=STATES)
 
-        e2e_step()
+        out = e2e_step()
+        assert out[0].device.type == "cpu" and out[1].shape == (atoms, 3, PULSES)
+        d2h = int(out[0].numel() * 8 + out[1].numel() * 8)
+        del out
         torch.cuda.synchronize()
         n_e2e = max(1, min(args.steps, 5))
         t0 = time.perf_counter()
         for _ in range(n_e2e):
-            e2e_step()
+            out = e2e_step()
+            del out
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / n_e2e
         e2e = {"value": updates / e2e_s, "unit": "updates/s", "ms_per_step": e2e_s * 1e3,
-               "h2d_bytes_per_step": 3 * atoms * 4,
-               "d2h_bytes_per_step": int(host_sig.numel() * 8 + host_jac.numel() * 8),
-               "api": "engine.forward_tangents_host: pinned host tissue in, pinned host signal "
-                      "and Jacobian out, 16 voxel chunks whose copies overlap the next sweep"}
-        del host_sig, host_jac
+               "h2d_bytes_per_step": 3 * atoms * 4 + PULSES * 4,
+               "d2h_bytes_per_step": d2h,
+               "api": "torchsim_gb300.mrf_sim(flip, 10.0, T1, T2, B1=B1, diff=('T1','T2','B1'), "
+                      "states=20) with CPU tensors in and out (the public call): tissue upload, "
+                      "fused sweep in chunks of ~64 MB of output, each chunk's copy to page-locked "
+                      "host memory overlapping the next chunk's sweep"}
 
     if rank != 0:
         return None

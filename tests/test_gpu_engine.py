@@ -84,3 +84,23 @@ def test_host_pipeline_matches_the_device_pass(cuda):
     with pytest.raises(ValueError):
         engine.forward_tangents_host(prog, host, 12, names, torch.empty_like(sig_h, device="cpu"),
                                      jac_h, device=cuda)
+
+
+def test_host_tensor_calls_match_device_calls(cuda):
+    """mrf_sim with CPU tensors sweeps in chunks whose copies back overlap
+    the next chunk (here 3 chunks of the Jacobian call) and returns CPU
+    tensors bitwise equal to the device call's results."""
+    import torchsim_gb300 as ts
+    from tests.helpers import draw_tissue, mrf_schedule
+
+    t1, t2, b1 = (torch.from_numpy(a) for a in draw_tissue(21, 8192))
+    flip = torch.from_numpy(mrf_schedule())
+    for diff in (None, ("T1", "T2", "B1")):
+        host = ts.mrf_sim(flip, 10.0, t1, t2, B1=b1, diff=diff, states=12)
+        dev = ts.mrf_sim(flip.to(cuda), 10.0, t1.to(cuda), t2.to(cuda), B1=b1.to(cuda),
+                         diff=diff, states=12)
+        host = host if isinstance(host, tuple) else (host,)
+        dev = dev if isinstance(dev, tuple) else (dev,)
+        for h, d in zip(host, dev, strict=True):
+            assert h.device.type == "cpu"
+            assert torch.equal(h, d.cpu())

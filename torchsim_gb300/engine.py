@@ -286,6 +286,66 @@ def forward_tangents_host(program: Program, tissue: TissueMaps, states: int,
     return sig_host, jac_host
 
 
+def sweep_to_host(program: Program, tissue: TissueMaps, states: int, names: Sequence[str] = (),
+                  *, chunks: int | None = None, launch=None):
+    """Signal (and Jacobian columns ``names``) of device-resident tissue,
+    delivered in host memory: what a call with host tensors returns. The
+    voxels go in chunks; each is swept (the fused pass of
+    :func:`forward_tangents`, or :func:`forward`) into one of two device
+    buffers and copied to page-locked host memory on a second stream while
+    the next chunk is swept, so the device-to-host copy, which bounds such a
+    call, overlaps the compute. Returns ``(signal (voxels, P), jacobian
+    (voxels, k, P) or None)`` complex64 CPU tensors once the copies are done.
+    """
+    if program.trains != 1:
+        raise ValueError("the host pipeline takes single-train programs")
+    device = tissue.t1.device
+    V, P, k = tissue.voxels, program.outputs, len(names)
+    sig_host = torch.empty((V, P), dtype=torch.complex64, pin_memory=True)
+    jac_host = torch.empty((V, k, P), dtype=torch.complex64, pin_memory=True) if k else None
+    if V == 0:
+        return sig_host, jac_host
+    if chunks is None:
+        # Pieces of ~64 MB of output, at most 16: small calls take one.
+        chunks = max(1, min(16, (V * (1 + k) * P * 8) >> 26))
+    chunks = max(1, min(int(chunks), V))
+    step = (V + chunks - 1) // chunks
+    compute = torch.cuda.current_stream(device)
+    copy = torch.cuda.Stream(device)
+    slots = min(2, chunks)
+    sig_d = [torch.empty((step, P), dtype=torch.complex64, device=device) for _ in range(slots)]
+    jac_d = [torch.empty((step, k, P), dtype=torch.complex64, device=device) if k else None
+             for _ in range(slots)]
+    freed = [None] * slots
+    for c, a in enumerate(range(0, V, step)):
+        b = min(a + step, V)
+        slot = c % slots
+        if freed[slot] is not None:
+            compute.wait_event(freed[slot])
+        sub = TissueMaps(*[None if x is None else x[a:b] for x in
+                           (tissue.t1, tissue.t2, tissue.m0, tissue.b1, tissue.inv)])
+        sig = sig_d[slot][: b - a]
+        jac = None if jac_d[slot] is None else jac_d[slot][: b - a]
+        if k:
+            forward_tangents(program, sub, states, names, sig_out=sig, jac_out=jac, launch=launch)
+        else:
+            forward(program, sub, states, out=sig, launch=launch)
+        done = torch.cuda.Event()
+        done.record(compute)
+        copy.wait_event(done)
+        with torch.cuda.stream(copy):
+            sig_host[a:b].copy_(sig, non_blocking=True)
+            if k:
+                jac_host[a:b].copy_(jac, non_blocking=True)
+            freed[slot] = torch.cuda.Event()
+            freed[slot].record(copy)
+    for x in (*sig_d, *jac_d, tissue.t1, tissue.t2, tissue.m0, tissue.b1, tissue.inv):
+        if x is not None:
+            x.record_stream(copy)
+    copy.synchronize()
+    return sig_host, jac_host
+
+
 # (lanes per voxel, orders per lane) instantiated per kernel family, as in the
 # sweep tables of csrc/sweep_*.cu.
 FAMILY_SHAPES = {

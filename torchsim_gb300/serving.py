@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 
 import torch
 
-from .recon import UNKNOWN, GaussNewton, VoxelPool, fixed_shape, natural_of, to_free
+from .recon import UNKNOWN, GaussNewton, TrustRegion, VoxelPool, fixed_shape, natural_of, to_free
 from .sequence import Program
 
 
@@ -104,7 +104,7 @@ class GNServer:
         self.program = program
         self.states = int(states)
         self.bounds = dict(bounds)
-        self.loop = loop if loop is not None else GaussNewton(max_iterations=10)
+        self.loop = loop if loop is not None else GaussNewton(TrustRegion(), max_iterations=10)
         self.config = self.loop.config(self.bounds)
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         # One launch shape for every iteration, whatever the live voxel count:

@@ -192,6 +192,16 @@ class _EpgSimulator:
                     jac = None if jac is None else jac.to(home)
                 return signal, jac
             program = program_for(events, dev)
+            if (home.type != "cuda" and program.trains == 1
+                    and type(self)._post is _EpgSimulator._post):
+                # Host tensors in, host tensors out: sweep in chunks whose
+                # copies back overlap the next chunk's sweep.
+                signal, jac = engine.sweep_to_host(program, tissue, states, kernel_names or ())
+                signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
+                if jac is not None:
+                    jac = (jac.reshape(*batch, *jac.shape[-2:]) if batch
+                           else jac.reshape(jac.shape[-2:]))
+                return signal, jac
             if kernel_names:
                 signal, jac = engine.forward_tangents(program, tissue, states, kernel_names)
             else:
