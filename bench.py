@@ -177,6 +177,57 @@ def traffic_per_launch() -> float | None:
     return None
 
 
+def host_link(torch, device, d2h_bytes: int, size: int = 2 << 30) -> dict:
+    """Device-to-host copy bandwidth of this machine (2 GB, best of 4) into
+    page-locked memory allocated while the process runs on the CPUs of each
+    NUMA node in turn, and into pageable memory; and the time the e2e call's
+    copies need at the best of them (the host link's bound on that call)."""
+    import glob
+
+    nodes = {}
+    for path in sorted(glob.glob("/sys/devices/system/node/node[0-9]*")):
+        cpus = set()
+        for part in open(path + "/cpulist").read().strip().split(","):
+            if part:
+                a, _, b = part.partition("-")
+                cpus |= set(range(int(a), int(b or a) + 1))
+        nodes[int(path.rsplit("node", 1)[1])] = cpus
+    src = torch.empty(size, dtype=torch.uint8, device=device)
+    src.fill_(1)
+
+    def rate(host):
+        best = 0.0
+        for _ in range(4):
+            s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record()
+            host.copy_(src, non_blocking=True)
+            e0.record()
+            e0.synchronize()
+            best = max(best, size / (s0.elapsed_time(e0) * 1e-3) / 1e9)
+        return best
+
+    out = {"numa_nodes": len(nodes)}
+    mine = os.sched_getaffinity(0)
+    for node, cpus in nodes.items():
+        if not cpus & mine:
+            continue
+        os.sched_setaffinity(0, cpus & mine)
+        try:
+            buf = torch.empty(size, dtype=torch.uint8, pin_memory=True)
+            buf.fill_(0)
+            out[f"pinned_node{node}_gbs"] = rate(buf)
+            del buf
+        finally:
+            os.sched_setaffinity(0, mine)
+    buf = torch.empty(size, dtype=torch.uint8)
+    buf.fill_(0)
+    out["pageable_gbs"] = rate(buf)
+    del buf, src
+    best = max(v for k, v in out.items() if k.endswith("_gbs"))
+    out["e2e_copy_bound_ms"] = d2h_bytes / (best * 1e9) * 1e3
+    return out
+
+
 def job_seconds(local_seconds: float, dist, device) -> float:
     """The job's time for N replicas: the slowest rank's (max over ranks)."""
     if dist is None:
@@ -309,6 +360,7 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         e2e = {"value": updates / e2e_s, "unit": "updates/s", "ms_per_step": e2e_s * 1e3,
                "h2d_bytes_per_step": 3 * atoms * 4 + PULSES * 4,
                "d2h_bytes_per_step": d2h,
+               "host_link": host_link(torch, device, d2h),
                "api": "torchsim_gb300.mrf_sim(flip, 10.0, T1, T2, B1=B1, diff=('T1','T2','B1'), "
                       "states=20) with CPU tensors in and out (the public call): tissue upload, "
                       "fused sweep in chunks of ~64 MB of output, each chunk's copy to page-locked "
