@@ -185,6 +185,29 @@ int tsg_program_plan(const float* duration_s, const int32_t* kind, const float* 
 int tsg_program_info(const tsg_program* program, int64_t* train_count, int64_t* op_count,
                      int64_t* output_count, int64_t* event_count);
 
+/* Rebinding a compiled program to new event values on the device, with no
+ * host round trip (the role of the reference's affine rebinding of packed
+ * buffers, model/_binding.py:94-268, for the pulse program): every op of
+ * `program` takes its relaxation dt and its rotation flip from its source
+ * events in `duration_s` and `flip_rad` (DEVICE, train_count*event_count),
+ * and is written, with the template's micro-step codes and records, to
+ * `device_ops` (DEVICE, train_count*op_count ops of 16 bytes). The new
+ * durations must be zero wherever the template's were (those events were
+ * folded into the op before them); a zero where the template had a
+ * relaxation is exact, since a zero-length relaxation is the identity.
+ * Stream-ordered. */
+int tsg_program_rebind(const tsg_program* program, const float* duration_s,
+                       const float* flip_rad, void* device_ops, void* stream);
+/* A program handle over `device_ops` (rebound by tsg_program_rebind) that
+ * borrows the template's structure and event source map; it must not
+ * outlive the template or the op array, and tsg_program_destroy frees only
+ * the handle. Allocates no device memory. */
+int tsg_program_view(const tsg_program* program, void* device_ops, tsg_program** out);
+/* out[i] = x[0] + ... + x[i], added left to right in float32 with one
+ * rounding per addition (DEVICE buffers, one thread): the reference's
+ * sequential float32 clock cursor (simulators/mrf.py:46-77) on the device. */
+int tsg_sequential_sum(const float* x, int64_t n, float* out, void* stream);
+
 /* ---- device-resident kernels ------------------------------------------- */
 
 /* Complex forward (one pool, instant RF): RF and receiver phases of the

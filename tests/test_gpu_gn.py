@@ -14,7 +14,7 @@ BOUNDS = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
 
 
 def rel(a, b):
-    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    a, b = np.asarray(a, np.complex128), np.asarray(b, np.complex128)
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 

@@ -107,6 +107,9 @@ SIGNATURES: dict[str, tuple] = {
                                 _i64]),
     "tsg_program_info": (_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                                 ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "tsg_program_rebind": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "tsg_program_view": (_int, [_vp, _vp, ctypes.POINTER(_vp)]),
+    "tsg_sequential_sum": (_int, [_vp, _i64, _vp, _vp]),
     "tsg_epg_forward": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _int, _vp, _vp,
                                ctypes.POINTER(Launch), _vp]),
     "tsg_epg_forward_complex": (_int, [_vp, ctypes.POINTER(Tissue), ctypes.POINTER(Offaxis), _i64,

@@ -265,10 +265,90 @@ extern "C" int tsg_program_plan(const float* duration_s, const int32_t* kind,
 
 extern "C" int tsg_program_destroy(tsg_program* program) {
     if (!program) return TSG_OK;
-    cudaFree(program->d_ops);
-    cudaFree(program->d_src);
-    cudaFree(program->d_phase);
+    if (!program->view) {
+        cudaFree(program->d_ops);
+        cudaFree(program->d_src);
+        cudaFree(program->d_phase);
+    }
     delete program;
+    return TSG_OK;
+}
+
+// ---- programs rebound on the device -----------------------------------------
+
+namespace tsg {
+namespace {
+
+// Every op of the template takes its dt from its relaxation's source event
+// and its flip from its rotation's source event in the new per-event buffers;
+// codes, records and sources are the template's.
+__global__ void rebind_kernel(const Op* __restrict__ tmpl, const OpSource* __restrict__ src,
+                              int64_t ops, int64_t events, int64_t total,
+                              const float* __restrict__ duration, const float* __restrict__ flip,
+                              Op* __restrict__ out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int64_t base = (i / ops) * events;
+    Op op = tmpl[i];
+    const OpSource s = src[i];
+    if ((op.code & OP_RELAX) && s.dt_event >= 0) op.dt = duration[base + s.dt_event];
+    if (op_rf(op.code) == RF_ROTATE && s.rf_event >= 0) op.flip = flip[base + s.rf_event];
+    out[i] = op;
+}
+
+// x[0], x[0]+x[1], ... summed left to right in float32, one rounding per
+// addition, as a sequential loop on the host does.
+__global__ void sequential_sum_kernel(const float* __restrict__ x, int64_t n,
+                                      float* __restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    float acc = 0.f;
+    for (int64_t i = 0; i < n; ++i) {
+        acc = i == 0 ? x[0] : __fadd_rn(acc, x[i]);
+        out[i] = acc;
+    }
+}
+
+}  // namespace
+}  // namespace tsg
+
+extern "C" int tsg_program_view(const tsg_program* tmpl, void* device_ops, tsg_program** out) {
+    if (!out) return fail(TSG_ERR_ARGUMENT, "null output handle");
+    *out = nullptr;
+    if (!tmpl) return fail(TSG_ERR_ARGUMENT, "null program");
+    if (tmpl->host.op.size() && !device_ops) return fail(TSG_ERR_ARGUMENT, "null op array");
+    auto* prog = new tsg_program();
+    prog->host = tmpl->host;
+    prog->d_ops = static_cast<Op*>(device_ops);
+    prog->d_src = tmpl->d_src;
+    prog->d_phase = tmpl->d_phase;
+    prog->device = tmpl->device;
+    prog->view = true;
+    *out = prog;
+    return TSG_OK;
+}
+
+extern "C" int tsg_program_rebind(const tsg_program* tmpl, const float* duration_s,
+                                  const float* flip_rad, void* device_ops, void* stream) {
+    if (!tmpl) return fail(TSG_ERR_ARGUMENT, "null program");
+    const int64_t total = int64_t(tmpl->host.op.size());
+    if (total == 0) return TSG_OK;
+    if (!duration_s || !flip_rad || !device_ops)
+        return fail(TSG_ERR_ARGUMENT, "null rebind buffer");
+    const int threads = 256;
+    rebind_kernel<<<unsigned((total + threads - 1) / threads), threads, 0,
+                    static_cast<cudaStream_t>(stream)>>>(
+        tmpl->d_ops, tmpl->d_src, tmpl->host.ops, tmpl->host.events, total, duration_s, flip_rad,
+        static_cast<Op*>(device_ops));
+    TSG_CUDA(cudaGetLastError());
+    return TSG_OK;
+}
+
+extern "C" int tsg_sequential_sum(const float* x, int64_t n, float* out, void* stream) {
+    if (n < 0) return fail(TSG_ERR_ARGUMENT, "negative length");
+    if (n == 0) return TSG_OK;
+    if (!x || !out) return fail(TSG_ERR_ARGUMENT, "null buffer");
+    sequential_sum_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(x, n, out);
+    TSG_CUDA(cudaGetLastError());
     return TSG_OK;
 }
 

@@ -76,6 +76,9 @@ struct tsg_program {
     tsg::OpSource* d_src = nullptr;
     float2* d_phase = nullptr;  // null unless built with event phases
     int device = 0;
+    // A view (tsg_program_view) borrows its template's source map and phases
+    // and the caller's op array; destroying it frees none of them.
+    bool view = false;
 };
 
 namespace tsg {

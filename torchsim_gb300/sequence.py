@@ -374,3 +374,112 @@ def program_for(events: PackedEvents, device: torch.device | None = None,
                 _cache.pop(next(iter(_cache)))
             _cache[key] = hit
     return hit
+
+
+# ---- programs rebound on the device ------------------------------------------
+
+
+class ProgramView:
+    """A pulse program whose op values live in a device tensor rebound from
+    device-resident event values (``tsg_program_rebind``), sharing its
+    template's structure and event source map (``tsg_program_view``). It
+    stands wherever a :class:`Program` does and keeps the template and the
+    op array alive."""
+
+    def __init__(self, template: Program, ops: torch.Tensor) -> None:
+        handle = _native.ctypes.c_void_p()
+        _native.check(_native.library().tsg_program_view(template.handle, ops.data_ptr(),
+                                                          _native.ctypes.byref(handle)))
+        self.handle = handle
+        self.template = template
+        self.ops_buffer = ops
+        self.events = template.events
+        self.phased = False
+        self.trains = template.trains
+        self.ops = template.ops
+        self.outputs = template.outputs
+
+    def __del__(self) -> None:
+        handle = getattr(self, "handle", None)
+        if handle is not None and handle.value:
+            try:
+                _native.library().tsg_program_destroy(handle)
+            except Exception:  # pragma: no cover - interpreter shutdown
+                pass
+            self.handle = None
+
+
+def rebind(template: Program, duration: torch.Tensor, flip: torch.Tensor) -> ProgramView:
+    """``template`` with every op's dt and flip taken from the device event
+    buffers ``duration`` (s) and ``flip`` (rad), ``(trains, events)`` float32,
+    by one kernel on the current stream. ``duration`` must be zero wherever
+    the template's events were (they are folded into the op before them)."""
+    duration = duration.to(torch.float32).contiguous()
+    flip = flip.to(torch.float32).contiguous()
+    ops = torch.empty((max(template.trains * template.ops, 1), 4), dtype=torch.float32,
+                      device=duration.device)
+    _native.check(_native.library().tsg_program_rebind(
+        template.handle, duration.data_ptr(), flip.data_ptr(), ops.data_ptr(),
+        torch.cuda.current_stream(duration.device).cuda_stream))
+    return ProgramView(template, ops)
+
+
+def sequential_sum(x: torch.Tensor) -> torch.Tensor:
+    """Running sums of a float32 device vector added left to right, one
+    rounding per addition (``np.cumsum(..., dtype=float32)``), on the device."""
+    x = x.to(torch.float32).contiguous()
+    out = torch.empty_like(x)
+    _native.check(_native.library().tsg_sequential_sum(
+        x.data_ptr(), x.numel(), out.data_ptr(), torch.cuda.current_stream(x.device).cuda_stream))
+    return out
+
+
+_templates: dict[tuple, Program] = {}
+
+
+def mrf_stream_on_device(flip_deg: torch.Tensor, TR_ms: Any, TI_ms: float,
+                         device: torch.device) -> tuple[ProgramView, torch.Tensor, torch.Tensor]:
+    """The MRF train of :func:`mrf_events` (one playing, TI a number, zero
+    phases) built from device-resident flips and TRs without leaving the
+    device: the played flips and the clock's intervals by the same float32
+    arithmetic as the host builder (the cursor by :func:`sequential_sum`), and
+    the program by rebinding a template compiled once per (pulses, TI) with
+    :func:`rebind`. Returns ``(program, flip (1, events), duration (1,
+    events))``, the last two the packed event buffers on the device."""
+    angles = torch.deg2rad(torch.atleast_1d(flip_deg.detach()).to(device))
+    if angles.ndim != 1:
+        raise ValueError("flip must be one angle per repetition")
+    n = int(angles.numel())
+    if n < 2:
+        raise ValueError("the device builder takes two pulses or more")
+    if isinstance(TR_ms, torch.Tensor):
+        tr = TR_ms.detach().to(device)
+    elif isinstance(TR_ms, (int, float)):
+        tr = torch.full((), float(TR_ms), dtype=torch.float32, device=device)
+    else:
+        tr = torch.as_tensor(np.asarray(TR_ms, np.float32)).to(device)
+    tr = tr.to(angles.dtype)
+    tr = tr.reshape(()).expand(n) if tr.numel() == 1 else tr
+    if tr.shape != angles.shape:
+        raise ValueError(f"expected one value per event or a single one, got {tuple(tr.shape)} "
+                         f"against {tuple(angles.shape)}")
+    s32 = (tr * 1e-3).to(torch.float32)
+    ti = float(TI_ms) * 1e-3
+    key = (n, ti, device.index)
+    template = _templates.get(key)
+    if template is None:
+        template = program_for(mrf_events(np.full(n, 10.0, np.float32),
+                                          np.full(n, 10.0, np.float32), TI_ms=float(TI_ms)),
+                               device)
+        _templates[key] = template
+    start = torch.full((1,), float(np.float32(ti)), dtype=torch.float32, device=device)
+    cursor = sequential_sum(torch.cat((start, s32)))
+    starts = cursor[:n] * np.float32(1e6)
+    starts[:1].fill_(float(np.float32(1e6 * ti)))  # a fill, not a host-to-device copy
+    stamps = torch.cat((starts.new_zeros(1), starts.repeat_interleave(4)))
+    duration = (torch.diff(stamps, prepend=stamps.new_zeros(1)) * 1e-6).to(torch.float32)
+    played = (2.0 * torch.pi * torch.abs(angles.to(torch.float32) * _HARD_PULSE_AREA))
+    flip = torch.zeros(1 + 4 * n, dtype=torch.float32, device=device)
+    flip[1::4] = played
+    program = rebind(template, duration[None], flip[None])
+    return program, flip[None], duration[None]

@@ -26,7 +26,7 @@ import torch
 
 from . import engine
 from .sequence import (POST_SHIFT, PRE_SHIFT, SHIFT_AFTER, PackedEvents, fse_events, mrf_events,
-                       mrf_gradient_map, played_flip_torch, program_for)
+                       mrf_gradient_map, mrf_stream_on_device, played_flip_torch, program_for)
 
 
 def _tensorish(value: Any) -> bool:
@@ -117,6 +117,12 @@ class _EpgSimulator:
     def events(self, **protocol: Any) -> PackedEvents:  # pragma: no cover - abstract
         raise NotImplementedError
 
+    def _device_stream(self, protocol: dict[str, Any], repetitions: int, device: torch.device):
+        """``(program, flip events, duration events)`` built on the device
+        from device-resident protocol values, or None where the stream is
+        built on the host."""
+        return None
+
     def _kernel_maps(self, held: dict[str, Any]) -> dict[str, Any]:
         return {
             "T1": held.get("T1"),
@@ -148,7 +154,9 @@ class _EpgSimulator:
         home = _home(values)
         dev = engine.require_cuda(torch.device(device) if device is not None else
                                   (home if home.type == "cuda" else None))
-        events = self.events(repetitions=repetitions, **protocol)
+        on_device = self._device_stream(protocol, repetitions, dev)
+        events = (on_device[0].events if on_device is not None
+                  else self.events(repetitions=repetitions, **protocol))
         complex_path = _leaves_real_subspace(events, held)
         batch = _batch(held)
         voxels = _numel(batch)
@@ -191,7 +199,7 @@ class _EpgSimulator:
                     signal = signal.to(home)
                     jac = None if jac is None else jac.to(home)
                 return signal, jac
-            program = program_for(events, dev)
+            program = on_device[0] if on_device is not None else program_for(events, dev)
             if (home.type != "cuda" and program.trains == 1
                     and type(self)._post is _EpgSimulator._post):
                 # Host tensors in, host tensors out: sweep in chunks whose
@@ -248,7 +256,9 @@ class _EpgSimulator:
         dev = engine.require_cuda(torch.device(device) if device is not None else
                                   (home if home.type == "cuda" else None))
         plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in protocol.items()}
-        events = self.events(repetitions=repetitions, **plain)
+        on_device = self._device_stream(plain, repetitions, dev)
+        events = (on_device[0].events if on_device is not None
+                  else self.events(repetitions=repetitions, **plain))
         complex_path = _leaves_real_subspace(events, held)
         if complex_path and names:
             raise NotImplementedError(
@@ -283,11 +293,15 @@ class _EpgSimulator:
             return flat(value, optional=False)
 
         with torch.cuda.device(dev):
-            program = program_for(events, dev, phased=complex_path)
-            flip_ev = torch.from_numpy(events.flip).to(dev)
-            dur_ev = torch.from_numpy(events.duration).to(dev)
-            phase_ev = torch.from_numpy(
-                np.array(np.broadcast_to(events.phase, events.duration.shape), np.float32)).to(dev)
+            if on_device is not None and not complex_path:
+                program, flip_ev, dur_ev = on_device
+                phase_ev = torch.zeros_like(flip_ev)
+            else:
+                program = program_for(events, dev, phased=complex_path)
+                flip_ev = torch.from_numpy(events.flip).to(dev)
+                dur_ev = torch.from_numpy(events.duration).to(dev)
+                phase_ev = torch.from_numpy(np.array(
+                    np.broadcast_to(events.phase, events.duration.shape), np.float32)).to(dev)
             flip_ev, dur_ev, phase_ev = self._event_gradients(protocol, events, flip_ev, dur_ev,
                                                               repetitions, phase_ev)
             tissue = (flat(maps["T1"], True, False), flat(maps["T2"], True, False),
@@ -329,6 +343,21 @@ class _EpgSimulator:
         return signal, jac
 
 
+_gradient_maps: dict[tuple, dict[str, torch.Tensor]] = {}
+
+
+def _gradient_map_on(pulses: int, repetitions: int, device: torch.device) -> dict[str, torch.Tensor]:
+    """:func:`mrf_gradient_map` as device index tensors, uploaded once per
+    (pulses, repetitions, device) so that a design step uploads nothing."""
+    key = (pulses, repetitions, str(device))
+    hit = _gradient_maps.get(key)
+    if hit is None:
+        hit = {k: torch.from_numpy(v).to(device)
+               for k, v in mrf_gradient_map(pulses, repetitions).items()}
+        _gradient_maps[key] = hit
+    return hit
+
+
 class MRFSimulator(_EpgSimulator):
     """Inversion-prepared unbalanced-SSFP MR fingerprinting
     (``simulators/mrf.py:17-84``): protocol ``flip`` (deg), ``TR`` (ms),
@@ -344,27 +373,43 @@ class MRFSimulator(_EpgSimulator):
     def events(self, *, flip, TR, TI=0.0, phases=0.0, repetitions=1) -> PackedEvents:
         return mrf_events(flip, TR, TI_ms=TI, phases_deg=phases, repetitions=repetitions)
 
+    def _device_stream(self, protocol, repetitions, device):
+        """Flips or TRs resident on the device: the stream and its program
+        are rebound there (:func:`mrf_stream_on_device`), so a design loop
+        that moves them pays no host round trip and no compile per step. One
+        playing, TI a number, zero phases and two pulses or more."""
+        flip, tr = protocol.get("flip"), protocol.get("TR")
+        if not any(isinstance(v, torch.Tensor) and v.device.type == "cuda" for v in (flip, tr)):
+            return None
+        if repetitions != 1 or set(protocol) - {"flip", "TR", "TI", "phases"}:
+            return None
+        ti, phases = protocol.get("TI", 0.0), protocol.get("phases", 0.0)
+        if _tensorish(ti) or _tensorish(phases) or float(phases) != 0.0:
+            return None
+        if not isinstance(flip, torch.Tensor) or flip.numel() < 2:
+            return None
+        return mrf_stream_on_device(flip, tr, float(ti), device)
+
     def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions, phase_ev=None):
         flip = protocol.get("flip")
         tr = protocol.get("TR")
         ti = protocol.get("TI", 0.0)
         n = int(torch.atleast_1d(torch.as_tensor(
             flip.detach() if isinstance(flip, torch.Tensor) else np.asarray(flip))).numel())
-        where = mrf_gradient_map(n, repetitions)
         dev = flip_ev.device
+        where = _gradient_map_on(n, repetitions, dev)
         if isinstance(flip, torch.Tensor) and flip.requires_grad:
             played = played_flip_torch(torch.atleast_1d(flip).to(dev))
             delta = (played - played.detach()).expand(repetitions, n).reshape(-1)
-            idx = torch.from_numpy(where["flip"].reshape(-1)).to(dev)
-            flip_ev = flip_ev.index_add(1, idx, delta[None])
+            flip_ev = flip_ev.index_add(1, where["flip"].reshape(-1), delta[None])
         if isinstance(tr, torch.Tensor) and tr.requires_grad:
             spacing = torch.atleast_1d(tr).to(dev, torch.float32).expand(n) * 1e-3
-            pairs = torch.from_numpy(where["tr"]).to(dev)
+            pairs = where["tr"]
             delta = (spacing - spacing.detach())[pairs[:, 1]]
             dur_ev = dur_ev.index_add(1, pairs[:, 0], delta[None])
         if isinstance(ti, torch.Tensor) and ti.requires_grad:
             t = ti.to(dev, torch.float32).reshape(()) * 1e-3
-            idx = torch.from_numpy(where["ti"]).to(dev)
+            idx = where["ti"]
             dur_ev = dur_ev.index_add(1, idx, (t - t.detach()).expand(idx.numel())[None])
         if isinstance(protocol.get("phases"), torch.Tensor) and protocol["phases"].requires_grad:
             raise NotImplementedError("MRFSimulator: gradients w.r.t. phases are not built")
