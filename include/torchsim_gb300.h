@@ -91,6 +91,16 @@ typedef struct {
     const float* flip_rad;
 } tsg_direction;
 
+/* The complex path's further forward-mode directions (DEVICE pointers,
+ * nullable): per atom the transmit phase (radians) and off-resonance (Hz),
+ * per (train, event) the phase (of a pulse, or of an ADC's receiver). The
+ * reference's b1_phase, b0 and phase tangent slots (_epg_cpu.cpp:11071). */
+typedef struct {
+    const float* b1_phase_rad;
+    const float* b0_hz;
+    const float* phase_rad;
+} tsg_offaxis_direction;
+
 /* The complex path's further gradients (DEVICE pointers, nullable): per
  * atom the transmit phase and off-resonance, per (train, event) the phase
  * (of a pulse, or of an ADC's receiver). */
@@ -317,6 +327,21 @@ int tsg_epg_adjoint_noalloc(const tsg_program* program, const tsg_tissue* tissue
                             const tsg_launch* launch, void* stream);
 /* TSG_STATIC_SCRATCH_BYTES, as built into the library. */
 int64_t tsg_static_scratch_bytes(void);
+
+/* One general forward-mode direction on the complex path: the tangent of
+ * the recorded sample along per-atom T1, T2, M0, B1, inversion (direction),
+ * B1phase and B0 (offaxis_direction) and per-event duration, flip
+ * (direction) and phase (offaxis_direction) at once. Replaces the complex
+ * simulate_jvp_range (_epg_cpu.cpp:2470-3005) for one pool and instant RF.
+ * A direction along a property the tissue does not declare (a null m0, b1,
+ * inversion, B1phase or B0 map) is ignored, as the reference's feature mask
+ * has it. Output layouts as tsg_epg_forward_complex. `program` from
+ * tsg_program_create_phased. Stream-ordered; up to 128 states. */
+int tsg_epg_tangent_complex(const tsg_program* program, const tsg_tissue* tissue,
+                            const tsg_offaxis* offaxis, int64_t atom_count, int64_t state_count,
+                            const tsg_direction* direction,
+                            const tsg_offaxis_direction* offaxis_direction, int layout,
+                            float* out_a, float* out_b, const tsg_launch* launch, void* stream);
 
 /* ---- the complex path's first-order adjoint ----------------------------- */
 
@@ -561,7 +586,11 @@ int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, int64_t atom_
 
 /* _epg_cpu.simulate_jvp (src/torchsim/_epg_cpu.cpp:11017-11148): 26 packed
  * buffers, 20 tangents (the differentiable inputs, FLOAT_INPUTS order of
- * sequence/_parameters.py:206), two output planes, 13 tail slots (61). */
+ * sequence/_parameters.py:206: 17 tissue, then duration, flip, phase), two
+ * output planes, 13 tail slots (61). real_axis == 1 runs the real-subspace
+ * tangent (simulate_real_jvp_range); any other value the complex one
+ * (tsg_epg_tangent_complex, simulate_jvp_range), which also follows the
+ * B1phase, B0 and event phase directions. Synchronous. */
 int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count, int64_t atom_count,
                          int64_t train_count, int64_t event_count, int64_t state_count,
                          int64_t output_count, int real_axis, int features);

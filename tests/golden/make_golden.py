@@ -292,6 +292,65 @@ def case_mrf_offaxis(ts, rec) -> dict:
     return out
 
 
+def case_complex_jvp(ts, rec) -> dict:
+    """Forward-mode tangents on the complex path, as the reference's own
+    _run_packed_jvp computes them (its complex simulate_jvp_range): an MRF
+    train with RF phases, per-voxel B0, B1phase, M0 and inversion efficiency,
+    differentiated along each tissue property the public Jacobian offers
+    (one call each) and along one direction in flip, TR and phase at once.
+    Each recorded call keeps its packed buffers, tangents and result."""
+    import torch
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(12)
+    n, pulses = 6, 50
+    t1, t2, b1 = draw_tissue(rng, n)
+    b0 = rng.uniform(-40, 40, n).astype(np.float32)
+    b1p = rng.uniform(-0.5, 0.5, n).astype(np.float32)
+    m0 = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    inv = rng.uniform(0.85, 1.0, n).astype(np.float32)
+    flip = rng.uniform(5, 70, pulses).astype(np.float32)
+    tr = rng.uniform(8, 15, pulses).astype(np.float32)
+    phases = rng.uniform(-40, 40, pulses).astype(np.float32)
+    values = {"T1": torch.from_numpy(t1), "T2": torch.from_numpy(t2),
+              "B1": torch.from_numpy(b1), "B0": torch.from_numpy(b0),
+              "B1phase": torch.from_numpy(b1p), "M0": torch.from_numpy(m0),
+              "inv_efficiency": torch.from_numpy(inv)}
+    sim = MRFSimulator(TI=15.0, states=12)
+    protocol = {"flip": torch.from_numpy(flip), "TR": torch.from_numpy(tr),
+                "phases": torch.from_numpy(phases)}
+    rec.clear()
+    names = ("T1", "T2", "B1", "M0", "inv_efficiency", "B0", "B1phase")
+    _, jac = sim.jacobian(names, **protocol, **values)
+    directions = {"flip": rng.standard_normal(pulses).astype(np.float32),
+                  "TR": rng.standard_normal(pulses).astype(np.float32) * 0.5,
+                  "phases": rng.standard_normal(pulses).astype(np.float32) * 5}
+
+    def played(f, r, p):
+        return sim.simulate(flip=f, TR=r, phases=p, **values)
+
+    _, along = torch.func.jvp(
+        played, (protocol["flip"], protocol["TR"], protocol["phases"]),
+        tuple(torch.from_numpy(directions[k]) for k in ("flip", "TR", "phases")))
+    calls = [c for c in rec.calls if c["route"] == "_run_packed_jvp"]
+    out = {"jacobian": _np(jac), "jacobian_names": np.array(names), "along": _np(along),
+           "states": np.int64(12), "calls": np.int64(len(calls)), "flip_deg": flip, "tr_ms": tr,
+           "phases_deg": phases, "ti_ms": np.float32(15.0), "t1": t1, "t2": t2, "b1": b1,
+           "b0": b0, "b1_phase": b1p, "m0": m0, "inv": inv,
+           **{f"direction_{k}": v for k, v in directions.items()}}
+    for k, call in enumerate(calls):
+        args = call["args"]
+        out.update(_packed(call, f"c{k}_"))
+        for j, value in enumerate(args[2]):
+            out[f"c{k}_tissue_tangent_{j}"] = _np(value)
+        for j, value in enumerate(args[3]):
+            out[f"c{k}_event_tangent_{j}"] = _np(value)
+        axis = args[7] if len(args) > 7 else call["kwargs"].get("real_axis")
+        out[f"c{k}_real_axis"] = np.int64(-1 if axis is None else axis)
+        out[f"c{k}_result"] = _np(call["result"])
+    return out
+
+
 def case_adjoint(ts, rec) -> dict:
     import torch
     from torchsim.simulators import MRFSimulator
@@ -642,6 +701,7 @@ def case_gn(ts, rec) -> dict:
 
 
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
+         "complex_jvp",
          "mrf_second", "complex_adjoint", "double_backward", "grouping", "design_loop", "bounds")
 
 
@@ -667,7 +727,8 @@ def main() -> None:
                      ("fse_phase0", case_fse_phase0), ("mrf_offaxis", case_mrf_offaxis),
                      ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint),
                      ("double_backward", case_double_backward), ("grouping", case_grouping),
-                     ("design_loop", case_design_loop), ("bounds", case_bounds)):
+                     ("design_loop", case_design_loop), ("bounds", case_bounds),
+                     ("complex_jvp", case_complex_jvp)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

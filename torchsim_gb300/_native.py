@@ -44,6 +44,10 @@ class Offaxis(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("b1_phase_rad", "b0_hz")]
 
 
+class OffaxisDirection(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("b1_phase_rad", "b0_hz", "phase_rad")]
+
+
 class OffaxisGradients(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("b1_phase_rad", "b0_hz", "phase_rad")]
 
@@ -124,6 +128,10 @@ SIGNATURES: dict[str, tuple] = {
                                         _vp, _vp, _vp, _vp, ctypes.POINTER(Launch), _vp]),
     "tsg_epg_tangent": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, ctypes.POINTER(Direction),
                                _vp, _vp, ctypes.POINTER(Launch), _vp]),
+    "tsg_epg_tangent_complex": (_int, [_vp, ctypes.POINTER(Tissue), ctypes.POINTER(Offaxis), _i64,
+                                       _i64, ctypes.POINTER(Direction),
+                                       ctypes.POINTER(OffaxisDirection), _int, _vp, _vp,
+                                       ctypes.POINTER(Launch), _vp]),
     "tsg_epg_forward_checkpointed": (_int, [_vp, ctypes.POINTER(Tissue), _i64, _i64, _int, _vp,
                                             _vp, _vp, _int, ctypes.POINTER(Launch), _vp]),
     "tsg_epg_adjoint_plan": (_int, [_vp, _i64, _i64, ctypes.POINTER(Launch), _int,

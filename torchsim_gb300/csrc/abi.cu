@@ -710,23 +710,29 @@ extern "C" int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count
     constexpr int64_t expected = PACKED_COUNT + FLOAT_COUNT + 2 + TAIL_COUNT;
     if (atom_count < 0 || train_count < 1 || event_count < 0 || state_count < 1 || output_count < 0)
         return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
+    // Off the real subspace (real_axis != 1) the complex tangent kernel runs,
+    // as the reference's dispatch_jvp picks simulate_jvp_range there
+    // (_epg_cpu.cpp:10957-10980).
     int rc = check_subset(pointers, pointer_count, expected, PACKED_COUNT + FLOAT_COUNT + 2,
-                          atom_count, real_axis, features, train_count);
+                          atom_count, real_axis, features, train_count, true);
     if (rc) return rc;
+    const bool complex_path = real_axis != 1;
     std::lock_guard<std::mutex> guard(g_dropin_mutex);
     void* const* tan = pointers + PACKED_COUNT;  // FLOAT_INPUTS order
     const float* duration = static_cast<const float*>(pointers[TISSUE_COUNT + 0]);
     const int32_t* kind = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 1]);
     const float* flip = static_cast<const float*>(pointers[TISSUE_COUNT + 2]);
+    const float* phase = static_cast<const float*>(pointers[TISSUE_COUNT + 3]);
     const uint8_t* action = static_cast<const uint8_t*>(pointers[TISSUE_COUNT + 4]);
     const int32_t* oindex = static_cast<const int32_t*>(pointers[TISSUE_COUNT + 5]);
     const float* dur_tangent = static_cast<const float*>(tan[TISSUE_COUNT + 0]);
     float* out_real = static_cast<float*>(pointers[PACKED_COUNT + FLOAT_COUNT]);
     float* out_imag = static_cast<float*>(pointers[PACKED_COUNT + FLOAT_COUNT + 1]);
     if (!out_real || !out_imag) return fail(TSG_ERR_ARGUMENT, "null output plane");
+    if (complex_path && event_count > 0 && !phase) return fail(TSG_ERR_ARGUMENT, "null phase buffer");
     tsg_program* prog = nullptr;
-    rc = tsg_program_create(duration, kind, flip, action, oindex, train_count, event_count, 0,
-                            dur_tangent, &prog);
+    rc = create_program(duration, kind, flip, complex_path ? phase : nullptr, action, oindex,
+                        train_count, event_count, 0, dur_tangent, &prog);
     if (rc) return rc;
     if (prog->host.outputs > output_count) {
         tsg_program_destroy(prog);
@@ -736,19 +742,28 @@ extern "C" int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count
     std::vector<void*> owned;
     const size_t abytes = size_t(atom_count) * sizeof(float);
     const size_t ebytes = size_t(train_count) * size_t(event_count) * sizeof(float);
-    void *t1, *t2, *m0 = nullptr, *b1 = nullptr, *inv = nullptr;
-    void *g[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void *t1, *t2, *m0 = nullptr, *b1 = nullptr, *inv = nullptr, *b1p = nullptr, *b0 = nullptr;
+    // Tangents: t1, t2, m0, b1, inversion; duration, flip; b1 phase, b0, phase.
+    void* g[10] = {};
     void *dr, *di;
     rc = upload(pointers[0], abytes, owned, &t1, s);
     if (!rc) rc = upload(pointers[1], abytes, owned, &t2, s);
     if (!rc && (features & F_DENSITY)) rc = upload(pointers[2], abytes, owned, &m0, s);
     if (!rc && (features & F_TRANSMIT)) rc = upload(pointers[3], abytes, owned, &b1, s);
     if (!rc && (features & F_INVERTING)) rc = upload(pointers[6], abytes, owned, &inv, s);
-    // Tangents: t1, t2, m0, b1 (index 3), inversion (6); duration, flip.
+    if (!rc && complex_path && (features & F_OFF_AXIS)) {
+        rc = upload(pointers[4], abytes, owned, &b1p, s);
+        if (!rc) rc = upload(pointers[5], abytes, owned, &b0, s);
+    }
     const int tissue_idx[5] = {0, 1, 2, 3, 6};
     for (int k = 0; k < 5 && !rc; ++k) rc = upload(tan[tissue_idx[k]], abytes, owned, &g[k], s);
     if (!rc) rc = upload(tan[TISSUE_COUNT + 0], ebytes, owned, &g[5], s);
     if (!rc) rc = upload(tan[TISSUE_COUNT + 1], ebytes, owned, &g[6], s);
+    if (!rc && complex_path) {
+        rc = upload(tan[4], abytes, owned, &g[7], s);
+        if (!rc) rc = upload(tan[5], abytes, owned, &g[8], s);
+        if (!rc) rc = upload(tan[TISSUE_COUNT + 2], ebytes, owned, &g[9], s);
+    }
     const size_t obytes = size_t(train_count) * size_t(atom_count) * size_t(output_count) * 4;
     if (!rc) rc = dense_device(obytes, owned, &dr, s);
     if (!rc) rc = dense_device(obytes, owned, &di, s);
@@ -765,8 +780,17 @@ extern "C" int tsg_epg_simulate_jvp(void* const* pointers, int64_t pointer_count
                           static_cast<float*>(g[4]), static_cast<float*>(g[5]),
                           static_cast<float*>(g[6])};
         prog->host.outputs = output_count;
-        rc = tsg_epg_tangent(prog, &tissue, atom_count, state_count, &dir,
-                             static_cast<float*>(dr), static_cast<float*>(di), nullptr, s);
+        if (complex_path) {
+            tsg_offaxis off{static_cast<float*>(b1p), static_cast<float*>(b0)};
+            tsg_offaxis_direction odir{static_cast<float*>(g[7]), static_cast<float*>(g[8]),
+                                       static_cast<float*>(g[9])};
+            rc = tsg_epg_tangent_complex(prog, &tissue, &off, atom_count, state_count, &dir,
+                                         &odir, TSG_LAYOUT_PLANES, static_cast<float*>(dr),
+                                         static_cast<float*>(di), nullptr, s);
+        } else {
+            rc = tsg_epg_tangent(prog, &tissue, atom_count, state_count, &dir,
+                                 static_cast<float*>(dr), static_cast<float*>(di), nullptr, s);
+        }
     }
     if (!rc && obytes) {
         cudaError_t e1 = cudaMemcpyAsync(out_real, dr, obytes, cudaMemcpyDeviceToHost, s);

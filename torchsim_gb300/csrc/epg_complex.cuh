@@ -117,6 +117,25 @@ __device__ __forceinline__ Pulse pulse_of(float d00, float d22, float a, float b
     return u;
 }
 
+// A pulse (or a derivative of one) from its entries: t00, t22, A = t01,
+// B = t12 and C = t21, with t10 = conj(A), t02 = conj(B), t20 = conj(C).
+__device__ __forceinline__ Pulse pulse_raw(float d00, float d22, float ar, float ai, float br,
+                                           float bi, float cr, float ci) {
+    Pulse u;
+    u.t00 = dup(d00);
+    u.t22 = dup(d22);
+    u.A_r = dup(ar);
+    u.A_i = dup(ai);
+    u.nA_i = dup(-ai);
+    u.B_r = dup(br);
+    u.B_i = dup(bi);
+    u.nB_i = dup(-bi);
+    u.C_r = dup(cr);
+    u.C_i = dup(ci);
+    u.nC_i = dup(-ci);
+    return u;
+}
+
 // (P, M, Z) -> pulse applied to (pr..zi); written to the six outputs.
 __device__ __forceinline__ void apply(const Pulse& u, float2 pr, float2 pi, float2 mr, float2 mi,
                                       float2 zr, float2 zi, float2& opr, float2& opi, float2& omr,

@@ -152,16 +152,70 @@ def forward_complex(program: Program, tissue: TissueMaps, states: int, offaxis=N
     return out
 
 
-def forward_tangents_complex(program: Program, tissue: TissueMaps, states: int,
-                             names: Sequence[str], offaxis=None, *, launch=None):
-    """Complex-path signal and Jacobian columns ``names`` (T1, T2, B1, M0) in
-    one pass: ``(signal (rows, P), jacobian (rows, k, P))`` complex64 holding
-    ``1j * m0 F+[0] e^{-i phase}`` and its derivatives."""
+# Columns of the complex path carried by the general tangent kernel (one
+# launch each), beside the fused T1/T2/B1/M0 sweep: the property's slot in
+# the direction structs.
+COMPLEX_DIRECTIONS = {"inv_efficiency": ("direction", "inversion"),
+                      "B0": ("offaxis", "b0_hz"), "B1phase": ("offaxis", "b1_phase_rad")}
+
+
+def tangent_complex(program: Program, tissue: TissueMaps, states: int, offaxis=None, *,
+                    direction: dict | None = None, offaxis_direction: dict | None = None,
+                    out: torch.Tensor | None = None, launch=None) -> torch.Tensor:
+    """One general direction on the complex path (``tsg_epg_tangent_complex``):
+    ``direction`` keys ``t1_ms, t2_ms, m0, b1, inversion`` (per voxel) and
+    ``duration_s, flip_rad`` (per train and event); ``offaxis_direction``
+    keys ``b1_phase_rad, b0_hz`` (per voxel) and ``phase_rad`` (per train and
+    event); device tensors. Returns the tangent of the recorded samples,
+    complex64 ``(trains*voxels, outputs)``, as ``1j`` times the tangent of
+    ``m0 F+[0] e^{-i phase}`` (the public MRF value's derivative)."""
     if not program.phased:
         raise ValueError("the complex kernel needs a program built with its event phases")
-    mask, columns = plan_tangents(names)
-    if columns[3] >= 0:
-        raise NotImplementedError("no inversion-efficiency column on the complex path")
+    keep = []
+
+    def ptr(v):
+        if v is None:
+            return None
+        v = v.to(torch.float32).contiguous()
+        keep.append(v)
+        return v.data_ptr()
+
+    d = _native.Direction(*[ptr((direction or {}).get(n)) for n in
+                            ("t1_ms", "t2_ms", "m0", "b1", "inversion", "duration_s",
+                             "flip_rad")])
+    od = _native.OffaxisDirection(*[ptr((offaxis_direction or {}).get(n)) for n in
+                                    ("b1_phase_rad", "b0_hz", "phase_rad")])
+    rows = program.trains * tissue.voxels
+    if out is None:
+        out = torch.empty((rows, program.outputs), dtype=torch.complex64,
+                          device=tissue.t1.device)
+    t = tissue.struct()
+    off = offaxis if offaxis is not None else _native.Offaxis(None, None)
+    _native.check(_native.library().tsg_epg_tangent_complex(
+        program.handle, ctypes.byref(t), ctypes.byref(off), tissue.voxels, states, ctypes.byref(d),
+        ctypes.byref(od), _native.LAYOUT_COMPLEX_IJ, out.data_ptr(), None,
+        _native.launch_shape(launch), _stream()))
+    return out
+
+
+def forward_tangents_complex(program: Program, tissue: TissueMaps, states: int,
+                             names: Sequence[str], offaxis=None, *, launch=None):
+    """Complex-path signal and Jacobian columns ``names``:
+    ``(signal (rows, P), jacobian (rows, k, P))`` complex64 holding
+    ``1j * m0 F+[0] e^{-i phase}`` and its derivatives. T1, T2, B1 and M0
+    come out of ONE fused pass with the signal; inv_efficiency, B0 and
+    B1phase each take one launch of the general tangent kernel (B0 and
+    B1phase need their maps in ``offaxis``, zero maps where absent)."""
+    if not program.phased:
+        raise ValueError("the complex kernel needs a program built with its event phases")
+    names = list(names)
+    for name in names:
+        if name not in DIFFERENTIABLE and name not in COMPLEX_DIRECTIONS:
+            raise ValueError(f"{name!r} does not carry a derivative on this path; choose from "
+                             f"{sorted({*DIFFERENTIABLE, *COMPLEX_DIRECTIONS})}")
+    if len(set(names)) != len(names):
+        raise ValueError("a property is named twice")
+    fused = [n for n in names if n in ("T1", "T2", "B1", "M0")]
     rows = program.trains * tissue.voxels
     k = len(names)
     device = tissue.t1.device
@@ -169,11 +223,28 @@ def forward_tangents_complex(program: Program, tissue: TissueMaps, states: int,
     jac = torch.empty((rows, k, program.outputs), dtype=torch.complex64, device=device)
     t = tissue.struct()
     off = offaxis if offaxis is not None else _native.Offaxis(None, None)
-    cols = (ctypes.c_int32 * 5)(*columns)
-    _native.check(_native.library().tsg_epg_forward_tangents_complex(
-        program.handle, ctypes.byref(t), ctypes.byref(off), tissue.voxels, states, mask, cols, k,
-        _native.LAYOUT_COMPLEX_IJ, sig.data_ptr(), None, jac.data_ptr(), None,
-        _native.launch_shape(launch), _stream()))
+    if fused:
+        mask, _ = plan_tangents(fused)
+        columns = [-1] * 5
+        for name in fused:
+            columns[DIFFERENTIABLE[name][1]] = names.index(name)
+        cols = (ctypes.c_int32 * 5)(*columns)
+        _native.check(_native.library().tsg_epg_forward_tangents_complex(
+            program.handle, ctypes.byref(t), ctypes.byref(off), tissue.voxels, states, mask, cols,
+            k, _native.LAYOUT_COMPLEX_IJ, sig.data_ptr(), None, jac.data_ptr(), None,
+            _native.launch_shape(launch), _stream()))
+    else:
+        forward_complex(program, tissue, states, offaxis, out=sig, launch=launch)
+    ones = torch.ones(tissue.voxels, dtype=torch.float32, device=device)
+    for col, name in enumerate(names):
+        if name in fused:
+            continue
+        group, key = COMPLEX_DIRECTIONS[name]
+        onehot = {key: ones}
+        jac[:, col] = tangent_complex(
+            program, tissue, states, offaxis, launch=launch,
+            direction=onehot if group == "direction" else None,
+            offaxis_direction=onehot if group == "offaxis" else None)
     return sig, jac
 
 

@@ -157,7 +157,13 @@ class _EpgSimulator:
         on_device = self._device_stream(protocol, repetitions, dev)
         events = (on_device[0].events if on_device is not None
                   else self.events(repetitions=repetitions, **protocol))
-        complex_path = _leaves_real_subspace(events, held)
+        # A derivative along B0 or B1phase leaves the real subspace too, as
+        # the reference's verdict counts the tangents (_accelerators.py:3953-3966).
+        complex_path = (_leaves_real_subspace(events, held)
+                        or bool(names and {"B0", "B1phase"} & set(names)))
+        if complex_path and on_device is not None:
+            on_device = None
+            events = self.events(repetitions=repetitions, **protocol)
         batch = _batch(held)
         voxels = _numel(batch)
         maps = self._kernel_maps(held)
@@ -260,6 +266,9 @@ class _EpgSimulator:
         events = (on_device[0].events if on_device is not None
                   else self.events(repetitions=repetitions, **plain))
         complex_path = _leaves_real_subspace(events, held)
+        if complex_path and on_device is not None:
+            on_device = None
+            events = self.events(repetitions=repetitions, **plain)
         if complex_path and names:
             raise NotImplementedError(
                 "a differentiable Jacobian on the complex path (RF phases, B0, B1phase) is not "
@@ -464,7 +473,7 @@ class FSESimulator(_EpgSimulator):
         return flip_ev, dur_ev, phase_ev
 
     def _kernel_names(self, names):
-        kernel = [n for n in names if n in ("T1", "T2", "B1")]
+        kernel = [n for n in names if n in ("T1", "T2", "B1", "B0", "B1phase")]
         if "T1" not in kernel:
             kernel.append("T1")  # the recovery term depends on T1 too
         return kernel
