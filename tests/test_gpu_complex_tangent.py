@@ -116,7 +116,9 @@ def test_complex_tangent_tissue_directions_against_central_differences(cuda, gol
     assert max_rel(got, fd) <= JACOBIAN_TOL, name
 
 
-@pytest.mark.parametrize("name,group,h", [("duration_s", "direction", 2e-5),
+# Durations are ~10 ms and the relaxation and off-resonance rates reach
+# ~250 per second, so the duration step is kept to 2 us for the truncation.
+@pytest.mark.parametrize("name,group,h", [("duration_s", "direction", 2e-6),
                                           ("flip_rad", "direction", 1e-3),
                                           ("phase_rad", "offaxis", 1e-3)])
 def test_complex_tangent_event_directions_against_central_differences(cuda, golden, name,
