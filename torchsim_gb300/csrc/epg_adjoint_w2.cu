@@ -14,6 +14,7 @@ const AdjointEntry kAdjointW2[] = {
     TSG_ADJOINT_ENTRY(6, 2, 2),  TSG_ADJOINT_ENTRY(4, 5, 2),  TSG_ADJOINT_ENTRY(2, 10, 2),
     TSG_ADJOINT_ENTRY(4, 4, 2),  TSG_ADJOINT_ENTRY(6, 4, 2),  TSG_ADJOINT_ENTRY(4, 8, 2),
     TSG_ADJOINT_ENTRY(8, 8, 2),  TSG_ADJOINT_ENTRY(4, 16, 2), TSG_ADJOINT_ENTRY(4, 32, 2),
+    TSG_ADJOINT_ENTRY(10, 2, 2),
 };
 const int kAdjointW2Count = sizeof(kAdjointW2) / sizeof(kAdjointW2[0]);
 
@@ -24,6 +25,7 @@ const AdjointEntry kAdjointTrajectoryW2[] = {
     TSG_ADJOINT_TRAJECTORY_ENTRY(4, 4, 2),  TSG_ADJOINT_TRAJECTORY_ENTRY(6, 4, 2),
     TSG_ADJOINT_TRAJECTORY_ENTRY(4, 8, 2),  TSG_ADJOINT_TRAJECTORY_ENTRY(8, 8, 2),
     TSG_ADJOINT_TRAJECTORY_ENTRY(4, 16, 2), TSG_ADJOINT_TRAJECTORY_ENTRY(4, 32, 2),
+    TSG_ADJOINT_TRAJECTORY_ENTRY(10, 2, 2),
 };
 const int kAdjointTrajectoryW2Count =
     sizeof(kAdjointTrajectoryW2) / sizeof(kAdjointTrajectoryW2[0]);

@@ -14,6 +14,7 @@ const AdjointEntry kAdjointW4[] = {
     TSG_ADJOINT_ENTRY(6, 2, 4),  TSG_ADJOINT_ENTRY(4, 5, 4),  TSG_ADJOINT_ENTRY(2, 10, 4),
     TSG_ADJOINT_ENTRY(4, 4, 4),  TSG_ADJOINT_ENTRY(6, 4, 4),  TSG_ADJOINT_ENTRY(4, 8, 4),
     TSG_ADJOINT_ENTRY(8, 8, 4),  TSG_ADJOINT_ENTRY(4, 16, 4), TSG_ADJOINT_ENTRY(4, 32, 4),
+    TSG_ADJOINT_ENTRY(10, 2, 4),
 };
 const int kAdjointW4Count = sizeof(kAdjointW4) / sizeof(kAdjointW4[0]);
 
@@ -24,6 +25,7 @@ const AdjointEntry kAdjointTrajectoryW4[] = {
     TSG_ADJOINT_TRAJECTORY_ENTRY(4, 4, 4),  TSG_ADJOINT_TRAJECTORY_ENTRY(6, 4, 4),
     TSG_ADJOINT_TRAJECTORY_ENTRY(4, 8, 4),  TSG_ADJOINT_TRAJECTORY_ENTRY(8, 8, 4),
     TSG_ADJOINT_TRAJECTORY_ENTRY(4, 16, 4), TSG_ADJOINT_TRAJECTORY_ENTRY(4, 32, 4),
+    TSG_ADJOINT_TRAJECTORY_ENTRY(10, 2, 4),
 };
 const int kAdjointTrajectoryW4Count =
     sizeof(kAdjointTrajectoryW4) / sizeof(kAdjointTrajectoryW4[0]);
