@@ -396,14 +396,24 @@ extern "C" int tsg_epg_forward_checkpointed(const tsg_program* program, const ts
     a.sig_a = out_a;
     a.sig_b = out_b;
     if (layout == TSG_LAYOUT_PLANES ? !out_b : !out_a) a.sig_a = a.sig_b = nullptr;
+    tsg_launch pinned{};
     if (ops_per_checkpoint == 1) {
-        // Trajectory mode: every op's entry state as order pairs, then the
-        // recorded F+[0] values.
+        // Trajectory mode: every op's entry state, then the recorded F+[0]
+        // values. Up to 20 states the sweep runs one voxel per lane with the
+        // reverse sweep's orders and stores its registers as they are.
         const int64_t state_bytes = trajectory_state_bytes(program->host.trains, program->host.ops,
                                                            atom_count, state_count);
         a.traj = reinterpret_cast<float2*>(checkpoints);
         a.traj_rec = reinterpret_cast<float*>(reinterpret_cast<char*>(checkpoints) +
                                               align256(state_bytes));
+        const int orders = trajectory_strided_orders(state_count);
+        if (orders > 0) {
+            a.traj_strided = 1;
+            pinned.lanes_per_voxel = 1;
+            pinned.orders_per_lane = orders;
+            pinned.warps_per_block = launch_shape ? launch_shape->warps_per_block : 0;
+            launch_shape = &pinned;
+        }
     } else {
         a.ckpt = checkpoints;
         a.ckpt_every = ops_per_checkpoint;

@@ -134,11 +134,52 @@ int make_plan_with(const tsg_program* prog, int64_t atoms, int64_t states, const
     return TSG_OK;
 }
 
+// Trajectory mode up to 20 states: one voxel per lane on the strided
+// trajectory (the forward's own register order); a requested lane or order
+// count is not used, its warps per block (2 or 4) are.
+int make_strided_plan(const tsg_program* prog, int64_t atoms, int64_t states,
+                      const tsg_launch* want, AdjointPlan* plan) {
+    const int orders = trajectory_strided_orders(states);
+    const int warps = (want && want->warps_per_block == 4) ? 4 : 2;
+    if (want && want->warps_per_block > 0 && want->warps_per_block != 2 &&
+        want->warps_per_block != 4)
+        return fail(TSG_ERR_ARGUMENT, "the adjoint takes 2 or 4 warps per block");
+    const AdjointEntry* entry = adjoint_strided_entry(orders, warps);
+    if (!entry) return fail(TSG_ERR_UNSUPPORTED, "no strided trajectory kernel");
+    const int64_t ops = prog->host.ops;
+    if (ops > kTrajMaxOps)
+        return fail(TSG_ERR_CAPACITY, "trajectory mode takes at most 2048 ops; use checkpoints");
+    plan->entry = entry;
+    plan->trajectory = true;
+    plan->warps = warps;
+    plan->ops_per_checkpoint = 1;
+    plan->checkpoint_count = int(ops);
+    const int threads = 32 * warps;
+    plan->blocks = (atoms + threads - 1) / threads;
+    plan->warps_per_train = plan->blocks * warps;
+    const int64_t event_bytes = prog->host.trains * plan->warps_per_train * ops *
+                                int64_t(sizeof(float2));
+    const int64_t tissue_bytes = prog->host.trains * atoms * 5 * int64_t(sizeof(float));
+    plan->workspace_bytes = align256(event_bytes) + tissue_bytes;
+    plan->checkpoint_bytes =
+        align256(trajectory_state_bytes(prog->host.trains, ops, atoms, states)) +
+        trajectory_record_bytes(prog->host.trains, prog->host.outputs, atoms);
+    const size_t granules = size_t(trajectory_granules(orders));
+    plan->smem = size_t(kTrajRing) * threads *
+                     (sizeof(float4) + sizeof(float2) + sizeof(float4) * 3 * granules) +
+                 sizeof(float2) * size_t(threads) * (kTrajChunk + 1) + sizeof(Op) * size_t(ops);
+    if (plan->smem > 200 * 1024)
+        return fail(TSG_ERR_CAPACITY, "trajectory ring does not fit in shared memory");
+    return TSG_OK;
+}
+
 int make_plan(const tsg_program* prog, int64_t atoms, int64_t states, const tsg_launch* want,
               int ops_per_checkpoint, AdjointPlan* plan) {
     if (!prog) return fail(TSG_ERR_ARGUMENT, "null program");
     if (atoms < 0 || states < 1) return fail(TSG_ERR_ARGUMENT, "invalid EPG buffer dimensions");
     if (states > 256) return fail(TSG_ERR_CAPACITY, "more than 256 states");
+    if (ops_per_checkpoint == 1 && trajectory_strided_orders(states) > 0)
+        return make_strided_plan(prog, atoms, states, want, plan);
     const bool shaped = want && (want->lanes_per_voxel > 0 || want->orders_per_lane > 0);
     // One voxel per lane up to 20 states (measured best), two warps a block;
     // a requested segment too long for its shared memory takes the

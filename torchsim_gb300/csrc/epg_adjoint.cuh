@@ -109,6 +109,52 @@ __device__ __forceinline__ void shift_adjoint(float2 (&pb)[RP], float2 (&mb)[RP]
     }
 }
 
+// The same two shifts for one lane holding a voxel's R = 2 RP orders as
+// strided pairs (pair k = orders k and k + RP): whole pairs move, and only
+// the wrap between the halves (order RP - 1 <-> RP) and the ends move single
+// values. `kill` clears order `kill_r` (= states) as the contiguous shifts do.
+template <int RP>
+__device__ __forceinline__ void shift_fwd_strided(float2 (&p)[RP], float2 (&m)[RP], bool kill,
+                                                  int kill_r) {
+    const float m_wrap = m[0].y;  // order RP moves down to RP - 1
+    const float p_wrap = p[RP - 1].x;  // order RP - 1 moves up to RP
+#pragma unroll
+    for (int k = 0; k + 1 < RP; ++k) m[k] = m[k + 1];
+    m[RP - 1] = make_float2(m_wrap, 0.f);
+#pragma unroll
+    for (int k = RP - 1; k > 0; --k) p[k] = p[k - 1];
+    p[0] = make_float2(-m[0].x, p_wrap);
+    if (kill) {
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            if (k == kill_r) p[k].x = 0.f;
+            if (k + RP == kill_r) p[k].y = 0.f;
+        }
+    }
+}
+
+template <int RP>
+__device__ __forceinline__ void shift_adjoint_strided(float2 (&pb)[RP], float2 (&mb)[RP], bool kill,
+                                                      int kill_r) {
+    const float carry = -pb[0].x;
+    const float pb_wrap = pb[0].y;      // order RP's cotangent moves down to RP - 1
+    const float mb_wrap = mb[RP - 1].x;  // order RP - 1's moves up to RP
+#pragma unroll
+    for (int k = 0; k + 1 < RP; ++k) pb[k] = pb[k + 1];
+    pb[RP - 1] = make_float2(pb_wrap, 0.f);
+#pragma unroll
+    for (int k = RP - 1; k > 0; --k) mb[k] = mb[k - 1];
+    mb[0] = make_float2(0.f, mb_wrap);
+    if constexpr (RP > 1) mb[1].x += carry;
+    if (kill) {
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            if (k == kill_r) mb[k].x = 0.f;
+            if (k + RP == kill_r) mb[k].y = 0.f;
+        }
+    }
+}
+
 }  // namespace adjoint_detail
 
 using namespace adjoint_detail;
@@ -130,7 +176,7 @@ struct TissueGrads {
 // `rec` the F+[0] it recorded (both used on the voxel's lane 0 only).
 // Updates the cotangent (pb, mb, zb) and the voxel gradients; returns this
 // lane's (dL/dflip, dL/dduration) of the op.
-template <int RP, int L>
+template <int RP, int L, bool STRIDED = false>
 __device__ __forceinline__ float2 reverse_op(const Op& op, const float4& tr, const float2 (&p_)[RP],
                                              const float2 (&m_)[RP], const float2 (&z_)[RP],
                                              float ep, float ez, float r0, float2 (&pb)[RP],
@@ -139,11 +185,17 @@ __device__ __forceinline__ float2 reverse_op(const Op& op, const float4& tr, con
                                              TissueGrads& g, int q, bool kill, int kill_r) {
     const uint32_t code = op.code;
     const float2 neg1 = dup(-1.f);
+    auto adjoint_shift = [&](float2 (&b_p)[RP], float2 (&b_m)[RP]) {
+        if constexpr (STRIDED)
+            shift_adjoint_strided<RP>(b_p, b_m, kill, kill_r);
+        else
+            shift_adjoint<RP, L>(b_p, b_m, q, kill, kill_r);
+    };
     if (code & OP_SPOIL2) {
 #pragma unroll
         for (int k = 0; k < RP; ++k) pb[k] = mb[k] = dup(0.f);
     }
-    for (int s = 0; s < op_shift3(code); ++s) shift_adjoint<RP, L>(pb, mb, q, kill, kill_r);
+    for (int s = 0; s < op_shift3(code); ++s) adjoint_shift(pb, mb);
     if ((code & OP_RECORD) && lane0) {
         pb[0].x = fmaf(seed, v.m0, pb[0].x);
         g.m0 = fmaf(seed, rec, g.m0);
@@ -152,7 +204,7 @@ __device__ __forceinline__ float2 reverse_op(const Op& op, const float4& tr, con
 #pragma unroll
         for (int k = 0; k < RP; ++k) pb[k] = mb[k] = dup(0.f);
     }
-    for (int s = 0; s < op_shift2(code); ++s) shift_adjoint<RP, L>(pb, mb, q, kill, kill_r);
+    for (int s = 0; s < op_shift2(code); ++s) adjoint_shift(pb, mb);
     const int rf = op_rf(code);
     // The recovery term r0 sits in z at order 0 (lane 0's first slot).
     const float r0q = q == 0 ? r0 : 0.f;
@@ -209,7 +261,7 @@ __device__ __forceinline__ float2 reverse_op(const Op& op, const float4& tr, con
         g.t1 = fmaf(a1, op.dt * v.w1, g.t1);
         g_dt = -v.r2 * a2 - v.r1 * a1;
     }
-    for (int s = 0; s < op_shift1(code); ++s) shift_adjoint<RP, L>(pb, mb, q, kill, kill_r);
+    for (int s = 0; s < op_shift1(code); ++s) adjoint_shift(pb, mb);
     if (code & OP_RELAX) {
         const float2 E1 = dup(tr.z), E2 = dup(tr.w);
 #pragma unroll

@@ -154,14 +154,6 @@ __device__ __forceinline__ void rotate_pair_moved(const Rotation& c, float2& p, 
     z = fma2(dup(at), Bs, fma2(c.hsi, d, mul2(c.co, z)));
 }
 
-// The op shape of an MRF repetition and of most spoiled sequences: relax,
-// rotate, (record), one shift after, and nothing else. It takes a
-// straight-line path with the shift folded into the rotation's results.
-constexpr uint32_t kFastMask = OP_RELAX | (3u << OP_SHIFT1_SHIFT) | (3u << OP_RF_SHIFT) |
-                               (3u << OP_SHIFT2_SHIFT) | OP_SPOIL1 | (3u << OP_SHIFT3_SHIFT) |
-                               OP_SPOIL2;
-constexpr uint32_t kFastBits = OP_RELAX | (uint32_t(RF_ROTATE) << OP_RF_SHIFT) |
-                               (1u << OP_SHIFT3_SHIFT);
 // The refocusing op of a CPMG echo: relax, shift, rotate, shift, nothing
 // else; straight-line too.
 constexpr uint32_t kEchoMask = kFastMask | OP_RECORD;
@@ -253,6 +245,17 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     const Op* ops = a.ops + train * a.n_ops;
     const float2* dirs = GEN ? a.op_dir + train * a.n_ops : nullptr;
     const int64_t row = train * a.atoms + atom;
+    // Strided trajectory: this lane's granules of op 0; each op moves the
+    // pointer on by one op's worth (3 planes x granules x 32 lanes).
+    constexpr int kGran = (RP + 1) / 2;
+    float4* traj_cur = nullptr;
+    if constexpr (L == 1 && NT == 0 && !GEN && !GN) {
+        if (a.traj != nullptr && a.traj_strided)
+            traj_cur = reinterpret_cast<float4*>(a.traj) +
+                       (train * ((a.atoms + 31) >> 5) + (ac >> 5)) * int64_t(a.n_ops) *
+                           (3 * kGran * 32) +
+                       (ac & 31);
+    }
     // Output row bases, once: a record then only adds its sample index.
     // Column offsets (col * outputs) are the same for every thread.
     const int64_t sig_base = row * a.outputs;
@@ -608,7 +611,27 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                         }
                     }
                 }
-                if (a.traj != nullptr && active) {
+                if constexpr (L == 1) {
+                    if (traj_cur != nullptr) {
+                        // The registers as they are: granule g holds pairs
+                        // 2g and 2g + 1 (the last one zero for odd RP).
+                        if (active) {
+#pragma unroll
+                            for (int g = 0; g < kGran; ++g) {
+                                const float2 p1 = 2 * g + 1 < RP ? P[2 * g + 1] : dup(0.f);
+                                const float2 m1 = 2 * g + 1 < RP ? M[2 * g + 1] : dup(0.f);
+                                const float2 z1 = 2 * g + 1 < RP ? Z[2 * g + 1] : dup(0.f);
+                                traj_cur[g * 32] = make_float4(P[2 * g].x, P[2 * g].y, p1.x, p1.y);
+                                traj_cur[(kGran + g) * 32] =
+                                    make_float4(M[2 * g].x, M[2 * g].y, m1.x, m1.y);
+                                traj_cur[(2 * kGran + g) * 32] =
+                                    make_float4(Z[2 * g].x, Z[2 * g].y, z1.x, z1.y);
+                            }
+                        }
+                        traj_cur += 3 * kGran * 32;
+                    }
+                }
+                if (a.traj != nullptr && !a.traj_strided && active) {
                     // Every op's entry state as consecutive order pairs
                     // (2 pj, 2 pj + 1), in tiles of 32 atoms:
                     // [train][tile][op][plane][pair][32].

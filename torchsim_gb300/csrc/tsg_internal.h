@@ -41,6 +41,15 @@ constexpr uint32_t OP_SHIFT3_SHIFT = 9;   // bits 9-10
 constexpr uint32_t OP_SPOIL2 = 1u << 11;
 constexpr int RF_NONE = 0, RF_ROTATE = 1, RF_INVERT = 2;
 
+// The op shape of an MRF repetition and of most spoiled sequences: relax,
+// rotate, (record), one shift after, and nothing else. The sweeps take a
+// straight-line path for it with the shift folded into the rotation.
+constexpr uint32_t kFastMask = OP_RELAX | (3u << OP_SHIFT1_SHIFT) | (3u << OP_RF_SHIFT) |
+                               (3u << OP_SHIFT2_SHIFT) | OP_SPOIL1 | (3u << OP_SHIFT3_SHIFT) |
+                               OP_SPOIL2;
+constexpr uint32_t kFastBits = OP_RELAX | (uint32_t(RF_ROTATE) << OP_RF_SHIFT) |
+                               (1u << OP_SHIFT3_SHIFT);
+
 __host__ __device__ inline int op_shift1(uint32_t c) { return (c >> OP_SHIFT1_SHIFT) & 3; }
 __host__ __device__ inline int op_rf(uint32_t c) { return (c >> OP_RF_SHIFT) & 3; }
 __host__ __device__ inline int op_shift2(uint32_t c) { return (c >> OP_SHIFT2_SHIFT) & 3; }
@@ -141,6 +150,10 @@ struct SweepArgs {
     // (states + 1) / 2 pairs, and every recorded F+[0], [train][output][atom].
     float2* traj;
     float* traj_rec;
+    // Trajectory layout: 0 order pairs (2j, 2j+1) in float2 [.. pair][32];
+    // 1 the one-lane sweep's own strided pairs (k, k + RP) two at a time in
+    // float4 granules [.. granule][32] (trajectory_strided_orders).
+    int traj_strided;
     // Gauss-Newton accumulation (GN sweeps): the measured samples (complex64
     // of the API signal) at row measured_rows[atom] (or atom when null), and
     // per voxel: cost, J^T J (6, upper triangle by rows) and J^T r (3) of the
@@ -227,6 +240,9 @@ struct AdjointEntry {
 // The reverse-sweep kernels built for `warps` warps per block (2 or 4),
 // checkpointed or trajectory; null with *count = 0 for any other block size.
 const AdjointEntry* adjoint_table(int warps, bool trajectory, int* count);
+// The one-lane reverse sweep over the strided trajectory layout, for R
+// orders (10 or 20) and 2 or 4 warps per block; null if none.
+const AdjointEntry* adjoint_strided_entry(int orders, int warps);
 
 // Trajectory-mode reverse sweep: ops per event-gradient reduction, ops in
 // flight per lane (ring slots in shared memory), and the longest program it
@@ -239,7 +255,22 @@ constexpr int kTrajMaxOps = 2048;
 
 // Bytes of the adjoint's trajectory mode: entry states (whole tiles of 32
 // atoms) and recorded F+[0].
+// Trajectory mode up to 20 states runs one voxel per lane on both sides and
+// stores each op's entry state in the sweep's own register order: R orders
+// (10 up to 10 states, else 20) as strided pairs (k, k + R/2), two pairs per
+// 16-byte granule, [train][atom/32][op][plane][granule][atom%32] float4, so
+// the forward stores and the reverse sweep copies whole registers. More
+// states keep the contiguous pair layout. Returns R, or 0 for the latter.
+inline int trajectory_strided_orders(int64_t states) {
+    return states <= 10 ? 10 : (states <= 20 ? 20 : 0);
+}
+inline int trajectory_granules(int orders) { return (orders / 2 + 1) / 2; }
+
 inline int64_t trajectory_state_bytes(int64_t trains, int64_t ops, int64_t atoms, int64_t states) {
+    const int orders = trajectory_strided_orders(states);
+    if (orders > 0)
+        return trains * ((atoms + 31) / 32) * ops * 3 * trajectory_granules(orders) * 32 *
+               int64_t(sizeof(float4));
     return trains * ((atoms + 31) / 32) * ops * 3 * ((states + 1) / 2) * 32 * int64_t(sizeof(float2));
 }
 inline int64_t trajectory_record_bytes(int64_t trains, int64_t outputs, int64_t atoms) {
