@@ -165,8 +165,10 @@ int make_strided_plan(const tsg_program* prog, int64_t atoms, int64_t states,
         align256(trajectory_state_bytes(prog->host.trains, ops, atoms, states)) +
         trajectory_record_bytes(prog->host.trains, prog->host.outputs, atoms);
     const size_t granules = size_t(trajectory_granules(orders));
+    // Per ring slot: an even op's entry state, and transcendentals, seed and
+    // record of it and of the odd op after it.
     plan->smem = size_t(kTrajRing) * threads *
-                     (sizeof(float4) + sizeof(float2) + sizeof(float4) * 3 * granules) +
+                     (2 * sizeof(float4) + 2 * sizeof(float2) + sizeof(float4) * 3 * granules) +
                  sizeof(float2) * size_t(threads) * (kTrajChunk + 1) + sizeof(Op) * size_t(ops);
     if (plan->smem > 200 * 1024)
         return fail(TSG_ERR_CAPACITY, "trajectory ring does not fit in shared memory");

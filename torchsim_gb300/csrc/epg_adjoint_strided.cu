@@ -2,13 +2,16 @@
 // over the strided trajectory the one-lane forward sweep stores.
 //
 // The forward keeps a voxel's R = 2 RP orders as strided pairs (pair k =
-// orders k and k + RP) and, in trajectory mode, stores each op's entry state
-// exactly as it holds it, two pairs per 16-byte granule
-// ([train][atom/32][op][plane][granule][atom%32] float4). This sweep keeps
-// its cotangents in the same layout, so:
-//   * every op's entry state arrives by 3 x ceil(RP/2) 16-byte cp.async
-//     copies into a ring of shared-memory slots, kTrajRing - 1 ops ahead of
-//     use, from a pointer that moves back one op per step;
+// orders k and k + RP) and, in trajectory mode, stores the entry state of
+// every even op exactly as it holds it, two pairs per 16-byte granule
+// ([train][atom/32][op/2][plane][granule][atom%32] float4): half the bytes of
+// every op's state, which is what bounds both sweeps here. This sweep walks
+// the ops back in (even, odd) pairs, runs the even op forward once to get the
+// odd op's entry state, and keeps its cotangents in the same layout, so:
+//   * each stored state arrives by 3 x ceil(RP/2) 16-byte cp.async copies
+//     into a ring of shared-memory slots, kTrajRing - 1 pairs ahead of use,
+//     from a pointer that moves back one pair per step (the even state is
+//     read from the ring twice: before the re-run and for its own step);
 //   * a gradient shift moves whole pairs, and in the op shape of an MRF
 //     repetition (relax, rotate, record, one shift after) the shift's
 //     transpose is folded into the operands of the rotation's transpose: the
@@ -93,9 +96,58 @@ __device__ __forceinline__ float2 reverse_mrf_op(const Op& op, const float4& tr,
     return make_float2(gsum * v.b1, -v.r2 * a2 - v.r1 * a1);
 }
 
-// Dynamic shared memory: the transcendental ring [D][T] float4, the
-// entry-state ring [D][3][G][T] float4, the (seed, F+[0]) ring [D][T]
-// float2, per-lane event partials [T][K + 1] float2, the ops [n_ops].
+// One op forward on a strided one-lane state (relax, shifts, pulse, spoils;
+// the record leaves the state as it is): the odd op's entry state from the
+// stored even one. tr = (sin, cos, e1, e2) of the op.
+template <int RP>
+__device__ __forceinline__ void forward_op_strided(const Op& op, const float4& tr, float2 (&p)[RP],
+                                                   float2 (&m)[RP], float2 (&z)[RP], float eff,
+                                                   bool kill, int kill_r) {
+    const uint32_t code = op.code;
+    if (code & OP_RELAX) {
+        const float2 E1 = dup(tr.z), E2 = dup(tr.w);
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            p[k] = mul2(p[k], E2);
+            m[k] = mul2(m[k], E2);
+            z[k] = mul2(z[k], E1);
+        }
+        z[0].x += 1.f - tr.z;
+    }
+    for (int s = 0; s < op_shift1(code); ++s) shift_fwd_strided<RP>(p, m, kill, kill_r);
+    const int rf = op_rf(code);
+    if (rf == RF_ROTATE) {
+        const float si = tr.x, co = tr.y;
+        const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
+        const float2 hs = dup(0.5f * si), si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
+        const float2 neg1 = dup(-1.f);
+#pragma unroll
+        for (int k = 0; k < RP; ++k) {
+            const float2 pk = p[k], mk = m[k], zk = z[k];
+            p[k] = fma2(ch, pk, fma2(sh, mk, mul2(nsi2, zk)));
+            m[k] = fma2(sh, pk, fma2(ch, mk, mul2(si2, zk)));
+            z[k] = fma2(hs, fma2(neg1, mk, pk), mul2(co2, zk));
+        }
+    } else if (rf == RF_INVERT) {
+#pragma unroll
+        for (int k = 0; k < RP; ++k) z[k] = mul2(z[k], dup(-eff));
+    }
+    for (int s = 0; s < op_shift2(code); ++s) shift_fwd_strided<RP>(p, m, kill, kill_r);
+    if (code & OP_SPOIL1) {
+#pragma unroll
+        for (int k = 0; k < RP; ++k) p[k] = m[k] = dup(0.f);
+    }
+    for (int s = 0; s < op_shift3(code); ++s) shift_fwd_strided<RP>(p, m, kill, kill_r);
+    if (code & OP_SPOIL2) {
+#pragma unroll
+        for (int k = 0; k < RP; ++k) p[k] = m[k] = dup(0.f);
+    }
+}
+
+// Dynamic shared memory, per ring slot one stored (even) op and the odd op
+// after it: the transcendentals [D][2][T] float4, the entry state of the even
+// op [D][3][G][T] float4, the (seed, F+[0]) of both [D][2][T] float2; then
+// per-lane event partials [T][K + 1] float2 and the ops [n_ops].
 template <int RP, int W>
 __global__ void __launch_bounds__(32 * W) epg_adjoint_strided_kernel(const AdjointArgs a) {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -104,6 +156,7 @@ __global__ void __launch_bounds__(32 * W) epg_adjoint_strided_kernel(const Adjoi
     constexpr int D = kTrajRing;
     constexpr int R = 2 * RP;
     constexpr int G = (RP + 1) / 2;
+    static_assert(K % 2 == 0, "event groups hold whole pairs of ops");
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t warp_global = int64_t(blockIdx.x) * W + warp;
@@ -113,11 +166,12 @@ __global__ void __launch_bounds__(32 * W) epg_adjoint_strided_kernel(const Adjoi
     const int64_t ac = active ? atom : 0;
     const int S = a.states;
     const int n_ops = a.n_ops;
+    const int n_pairs = (n_ops + 1) >> 1;
 
-    float4* s_tring = reinterpret_cast<float4*>(s_raw);          // [D][T]
-    float4* s_ring = s_tring + D * T;                             // [D][3][G][T]
-    float2* s_sring = reinterpret_cast<float2*>(s_ring + D * 3 * G * T);  // [D][T]
-    float2* s_ev = s_sring + D * T;                               // [T][K + 1]
+    float4* s_tring = reinterpret_cast<float4*>(s_raw);          // [D][2][T]
+    float4* s_ring = s_tring + D * 2 * T;                         // [D][3][G][T]
+    float2* s_sring = reinterpret_cast<float2*>(s_ring + D * 3 * G * T);  // [D][2][T]
+    float2* s_ev = s_sring + D * 2 * T;                           // [T][K + 1]
     Op* s_ops = reinterpret_cast<Op*>(s_ev + T * (K + 1));        // [n_ops]
     float2* my_ev = s_ev + threadIdx.x * (K + 1);
     const float2* warp_ev = s_ev + warp * 32 * (K + 1);
@@ -157,18 +211,20 @@ __global__ void __launch_bounds__(32 * W) epg_adjoint_strided_kernel(const Adjoi
     const float* rec_col = a.traj_rec + train * a.outputs * n + ac;
     const bool lane0 = active;
 
-    // One op of this lane's granules is 3 * G * 32 float4 further on; the
-    // fetch pointer starts at the last op and moves back one op per fetch.
+    // One stored op of this lane's granules is 3 * G * 32 float4 on; the
+    // fetch pointer starts at the last pair and moves back one pair per fetch.
     constexpr int op_stride = 3 * G * 32;
     const float4* fetch_ptr = reinterpret_cast<const float4*>(a.traj) +
-                              ((train * ((n + 31) >> 5) + (ac >> 5)) * int64_t(n_ops) +
-                               (n_ops - 1)) * op_stride +
+                              ((train * ((n + 31) >> 5) + (ac >> 5)) * int64_t(n_pairs) +
+                               (n_pairs - 1)) * op_stride +
                               (ac & 31);
     const unsigned ring_base = static_cast<unsigned>(__cvta_generic_to_shared(s_ring + threadIdx.x));
     const unsigned sring_base =
         static_cast<unsigned>(__cvta_generic_to_shared(s_sring + threadIdx.x));
-    // The next op to fetch (from the last down) into ring slot `rs`.
-    int fetch_op = n_ops - 1;
+    // The next pair to fetch (from the last down) into ring slot `rs`: the
+    // even op's entry state, and for it and the odd op after it the seed,
+    // the recorded F+[0] and the transcendentals.
+    int fetch_pair = n_pairs - 1;
     auto fetch = [&](int rs) {
         const unsigned dst = ring_base + unsigned(rs * 3 * G * T) * 16u;
 #pragma unroll
@@ -177,48 +233,46 @@ __global__ void __launch_bounds__(32 * W) epg_adjoint_strided_kernel(const Adjoi
                              dst + unsigned(j * T) * 16u),
                          "l"(fetch_ptr + j * 32)
                          : "memory");
-        const Op op = s_ops[fetch_op];
-        const bool rec = lane0 && (op.code & OP_RECORD);
-        const int64_t r = rec ? op.record : 0;
-        const unsigned sdst = sring_base + unsigned(rs * T) * 8u;
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sdst),
-                     "l"(seed_row + r * seed_stride), "r"(rec ? 4 : 0)
-                     : "memory");
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sdst + 4u),
-                     "l"(rec_col + r * n), "r"(rec ? 4 : 0)
-                     : "memory");
-        float si, co;
-        sincosf(op.flip * vc.b1, &si, &co);
-        s_tring[rs * T + threadIdx.x] =
-            make_float4(si, co, expf(-vc.r1 * op.dt), expf(-vc.r2 * op.dt));
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int o = 2 * fetch_pair + h;
+            const bool here = o < n_ops;
+            const Op op = s_ops[here ? o : 2 * fetch_pair];
+            const bool rec = here && lane0 && (op.code & OP_RECORD);
+            const int64_t r = rec ? op.record : 0;
+            const unsigned sdst = sring_base + unsigned((rs * 2 + h) * T) * 8u;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sdst),
+                         "l"(seed_row + r * seed_stride), "r"(rec ? 4 : 0)
+                         : "memory");
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sdst + 4u),
+                         "l"(rec_col + r * n), "r"(rec ? 4 : 0)
+                         : "memory");
+            // The hardware approximations (|error| ~1e-6 relative for these
+            // arguments, an angle of at most a few radians and exponents of a
+            // few units): the gradient's tolerance is 1e-4, and the exact
+            // routines cost a fifth of this loop's instructions.
+            float si, co;
+            __sincosf(op.flip * vc.b1, &si, &co);
+            s_tring[(rs * 2 + h) * T + threadIdx.x] =
+                make_float4(si, co, __expf(-vc.r1 * op.dt), __expf(-vc.r2 * op.dt));
+        }
         fetch_ptr -= op_stride;
-        --fetch_op;
+        --fetch_pair;
     };
 
-    // Op o sits in ring slot (n_ops - 1 - o) % D.
+    // Pair q sits in ring slot (n_pairs - 1 - q) % D.
 #pragma unroll
     for (int j = 1; j < D; ++j) {
-        if (fetch_op >= 0) fetch(j - 1);
+        if (fetch_pair >= 0) fetch(j - 1);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
     int use_slot = 0;
     int fill_slot = D - 1;
     int group = 0;  // ops processed since the last event reduction
     const bool fast_ok = !kill;
-    // Not unrolled: a second copy of the body overflows the instruction cache.
-#pragma unroll 1
-    for (int o = n_ops - 1; o >= 0; --o) {
-        if (fetch_op >= 0) fetch(fill_slot);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        fill_slot = fill_slot + 1 == D ? 0 : fill_slot + 1;
-        const Op op = s_ops[o];
-        const uint32_t code = op.code;
-        asm volatile("cp.async.wait_group %0;\n" ::"n"(D - 1) : "memory");
-        const float4 tr = s_tring[use_slot * T + threadIdx.x];
-        const float2 sr = s_sring[use_slot * T + threadIdx.x];
-        const float4* ring = s_ring + use_slot * (3 * G * T) + threadIdx.x;
-        use_slot = use_slot + 1 == D ? 0 : use_slot + 1;
-        float2 p_[RP], m_[RP], z_[RP];
+
+    float2 p_[RP], m_[RP], z_[RP];
+    auto load_entry = [&](const float4* ring) {
 #pragma unroll
         for (int j = 0; j < G; ++j) {
             const float4 pp = ring[(0 * G + j) * T];
@@ -233,39 +287,67 @@ __global__ void __launch_bounds__(32 * W) epg_adjoint_strided_kernel(const Adjoi
                 z_[2 * j + 1] = make_float2(zz.z, zz.w);
             }
         }
-        float2 ev;
-        if (fast_ok && (code & kFastMask) == kFastBits) {
-            ev = reverse_mrf_op<RP>(op, tr, p_, m_, z_, pb, mb, zb, seed_sign * sr.x, sr.y, lane0,
-                                    vc, g);
-        } else {
-            // The pre-RF state: the entry state relaxed and shifted. Without
-            // a shift in between, the relaxation folds into reverse_op.
-            const bool relax = (code & OP_RELAX) != 0;
-            float ep = 1.f, ez = 1.f, r0 = 0.f;
-            if (relax && op_shift1(code) == 0) {
-                ep = tr.w;
-                ez = tr.z;
-                r0 = 1.f - tr.z;
-            } else if (relax) {
-                const float2 E1 = dup(tr.z), E2 = dup(tr.w);
+    };
+    // The reverse step of op `op` from its entry state in (p_, m_, z_).
+    auto reverse_at = [&](const Op& op, const float4& tr, const float2& sr) -> float2 {
+        const uint32_t code = op.code;
+        if (fast_ok && (code & kFastMask) == kFastBits)
+            return reverse_mrf_op<RP>(op, tr, p_, m_, z_, pb, mb, zb, seed_sign * sr.x, sr.y,
+                                      lane0, vc, g);
+        // The pre-RF state: the entry state relaxed and shifted. Without a
+        // shift in between, the relaxation folds into reverse_op.
+        const bool relax = (code & OP_RELAX) != 0;
+        float ep = 1.f, ez = 1.f, r0 = 0.f;
+        if (relax && op_shift1(code) == 0) {
+            ep = tr.w;
+            ez = tr.z;
+            r0 = 1.f - tr.z;
+        } else if (relax) {
+            const float2 E1 = dup(tr.z), E2 = dup(tr.w);
 #pragma unroll
-                for (int k = 0; k < RP; ++k) {
-                    p_[k] = mul2(p_[k], E2);
-                    m_[k] = mul2(m_[k], E2);
-                    z_[k] = mul2(z_[k], E1);
-                }
-                z_[0].x += 1.f - tr.z;
-                for (int s = 0; s < op_shift1(code); ++s) shift_fwd_strided<RP>(p_, m_, kill, kill_r);
-            } else {
-                for (int s = 0; s < op_shift1(code); ++s) shift_fwd_strided<RP>(p_, m_, kill, kill_r);
+            for (int k = 0; k < RP; ++k) {
+                p_[k] = mul2(p_[k], E2);
+                m_[k] = mul2(m_[k], E2);
+                z_[k] = mul2(z_[k], E1);
             }
-            ev = reverse_op<RP, 1, true>(op, tr, p_, m_, z_, ep, ez, r0, pb, mb, zb,
-                                         seed_sign * sr.x, sr.y, lane0, vc, g, 0, kill, kill_r);
+            z_[0].x += 1.f - tr.z;
+            for (int s = 0; s < op_shift1(code); ++s) shift_fwd_strided<RP>(p_, m_, kill, kill_r);
+        } else {
+            for (int s = 0; s < op_shift1(code); ++s) shift_fwd_strided<RP>(p_, m_, kill, kill_r);
         }
-        my_ev[group] = active ? ev : dup(0.f);
+        return reverse_op<RP, 1, true>(op, tr, p_, m_, z_, ep, ez, r0, pb, mb, zb,
+                                       seed_sign * sr.x, sr.y, lane0, vc, g, 0, kill, kill_r);
+    };
+
+    // Not unrolled: a second copy of the body overflows the instruction cache.
+#pragma unroll 1
+    for (int q = n_pairs - 1; q >= 0; --q) {
+        if (fetch_pair >= 0) fetch(fill_slot);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        fill_slot = fill_slot + 1 == D ? 0 : fill_slot + 1;
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(D - 1) : "memory");
+        const int o = 2 * q;
+        const Op op_even = s_ops[o];
+        const float4 tr_even = s_tring[(use_slot * 2) * T + threadIdx.x];
+        const float2 sr_even = s_sring[(use_slot * 2) * T + threadIdx.x];
+        const float4* ring = s_ring + use_slot * (3 * G * T) + threadIdx.x;
+        if (o + 1 < n_ops) {
+            // The odd op: its entry state is the even op run forward.
+            const Op op_odd = s_ops[o + 1];
+            const float4 tr_odd = s_tring[(use_slot * 2 + 1) * T + threadIdx.x];
+            const float2 sr_odd = s_sring[(use_slot * 2 + 1) * T + threadIdx.x];
+            load_entry(ring);
+            forward_op_strided<RP>(op_even, tr_even, p_, m_, z_, vc.eff, kill, kill_r);
+            const float2 ev = reverse_at(op_odd, tr_odd, sr_odd);
+            my_ev[group++] = active ? ev : dup(0.f);
+        }
+        load_entry(ring);
+        use_slot = use_slot + 1 == D ? 0 : use_slot + 1;
+        const float2 ev = reverse_at(op_even, tr_even, sr_even);
+        my_ev[group++] = active ? ev : dup(0.f);
         // Every K ops (and at the end) the warp sums its lanes' partials:
-        // entry j of the group is op o + group - j.
-        if (++group == K || o == 0) {
+        // entry j of the group is op o + group - 1 - j.
+        if (group >= K || q == 0) {
             __syncwarp();
             for (int j = lane; j < group; j += 32) {
                 float2 acc[4] = {dup(0.f), dup(0.f), dup(0.f), dup(0.f)};

@@ -245,15 +245,15 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
     const Op* ops = a.ops + train * a.n_ops;
     const float2* dirs = GEN ? a.op_dir + train * a.n_ops : nullptr;
     const int64_t row = train * a.atoms + atom;
-    // Strided trajectory: this lane's granules of op 0; each op moves the
-    // pointer on by one op's worth (3 planes x granules x 32 lanes).
+    // Strided trajectory: this lane's granules of op 0; each even op moves
+    // the pointer on by one stored op's worth (3 planes x granules x 32).
     constexpr int kGran = (RP + 1) / 2;
     float4* traj_cur = nullptr;
     if constexpr (L == 1 && NT == 0 && !GEN && !GN) {
         if (a.traj != nullptr && a.traj_strided)
             traj_cur = reinterpret_cast<float4*>(a.traj) +
-                       (train * ((a.atoms + 31) >> 5) + (ac >> 5)) * int64_t(a.n_ops) *
-                           (3 * kGran * 32) +
+                       (train * ((a.atoms + 31) >> 5) + (ac >> 5)) *
+                           int64_t((a.n_ops + 1) >> 1) * (3 * kGran * 32) +
                        (ac & 31);
     }
     // Output row bases, once: a record then only adds its sample index.
@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 256, MINB) epg_sweep_kernel(c
                     }
                 }
                 if constexpr (L == 1) {
-                    if (traj_cur != nullptr) {
+                    if (traj_cur != nullptr && ((base + i) & 1) == 0) {
                         // The registers as they are: granule g holds pairs
                         // 2g and 2g + 1 (the last one zero for odd RP).
                         if (active) {

@@ -256,11 +256,13 @@ constexpr int kTrajMaxOps = 2048;
 // Bytes of the adjoint's trajectory mode: entry states (whole tiles of 32
 // atoms) and recorded F+[0].
 // Trajectory mode up to 20 states runs one voxel per lane on both sides and
-// stores each op's entry state in the sweep's own register order: R orders
-// (10 up to 10 states, else 20) as strided pairs (k, k + R/2), two pairs per
-// 16-byte granule, [train][atom/32][op][plane][granule][atom%32] float4, so
-// the forward stores and the reverse sweep copies whole registers. More
-// states keep the contiguous pair layout. Returns R, or 0 for the latter.
+// stores the entry state of every other op (ops 0, 2, 4, ...; the reverse
+// sweep re-runs each odd op from the even one before it) in the sweep's own
+// register order: R orders (10 up to 10 states, else 20) as strided pairs
+// (k, k + R/2), two pairs per 16-byte granule,
+// [train][atom/32][op/2][plane][granule][atom%32] float4, so the forward
+// stores and the reverse sweep copies whole registers. More states keep the
+// contiguous pair layout of every op. Returns R, or 0 for the latter.
 inline int trajectory_strided_orders(int64_t states) {
     return states <= 10 ? 10 : (states <= 20 ? 20 : 0);
 }
@@ -269,8 +271,8 @@ inline int trajectory_granules(int orders) { return (orders / 2 + 1) / 2; }
 inline int64_t trajectory_state_bytes(int64_t trains, int64_t ops, int64_t atoms, int64_t states) {
     const int orders = trajectory_strided_orders(states);
     if (orders > 0)
-        return trains * ((atoms + 31) / 32) * ops * 3 * trajectory_granules(orders) * 32 *
-               int64_t(sizeof(float4));
+        return trains * ((atoms + 31) / 32) * ((ops + 1) / 2) * 3 * trajectory_granules(orders) *
+               32 * int64_t(sizeof(float4));
     return trains * ((atoms + 31) / 32) * ops * 3 * ((states + 1) / 2) * 32 * int64_t(sizeof(float2));
 }
 inline int64_t trajectory_record_bytes(int64_t trains, int64_t outputs, int64_t atoms) {
