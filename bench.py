@@ -571,7 +571,10 @@ def adjoint_section(torch, device, repeats: int = 5) -> dict:
         "ops_per_checkpoint": c,
         "checkpoint_bytes": ck,
         "forward_shape": list(fwd_shape),
-        "adjoint_shape": list(shape),
+        # Trajectory mode up to 20 states runs one voxel per lane whatever
+        # shape is requested (its warps per block are kept).
+        "adjoint_shape": ([1, 10 if S <= 10 else 20, shape[2]] if c == 1 and S <= 20
+                          else list(shape)),
         "forward_ms": fwd,
         "forward_with_checkpoints_ms": fwd_ck,
         "backward_ms": bwd,
