@@ -429,6 +429,15 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     if not args.skip_batched:
         line["batched"] = batched_section(torch, device, sequences=args.batch_sequences,
                                           shape=args.batch_shape)
+        b = line["batched"]
+        b_flops = float(b["updates"]) * 18.0  # relax 3 + rotate 15 per update
+        b_achieved = b_flops / (b["persistent_graph_ms"] * 1e-3) / 1e12
+        b["roofline"] = {"bound": "fp32", "achieved": b_achieved, "peak": peak / 1e12,
+                         "unit": "TFLOP/s", "frac": b_achieved * 1e12 / peak,
+                         "flops_per_launch": b_flops,
+                         "flop_count": "18 per update (order x echo x voxel): relaxation 3, "
+                                       "rotation 15",
+                         "peak_source": "the FP32 FMA probe of this run"}
     if not args.skip_gn:
         line["gn_server"] = gn_section(torch, device, requests=args.gn_requests)
     if not args.skip_match:

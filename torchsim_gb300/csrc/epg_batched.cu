@@ -112,7 +112,12 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
         if (q == 0) Z[0].x = 1.f;
         float last_dt = __int_as_float(0x7fffffff);
         float e1 = 1.f, e2 = 1.f;
-        const float2 neg1 = dup(-1.f);
+        // Relaxation not yet applied to the state: F+ and F- owe a factor pe2,
+        // Z owes pe1 and the recovery 1 - pe1 at order 0. A relaxation only
+        // multiplies these (a shift moves F+ and F- orders, which share the
+        // factor, and leaves Z alone, so it commutes with them); the pulse,
+        // the inversion and the record apply them in their own coefficients.
+        float pe1 = 1.f, pe2 = 1.f;
         float2* orow = out + sq.output_offset + int64_t(u.voxel_begin + local) * sq.outputs;
         for (int base = 0; base < sq.op_count; base += kBatchOpChunk) {
             const int count = min(kBatchOpChunk, sq.op_count - base);
@@ -142,27 +147,32 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                         e1 = expf(-r1 * op.dt);
                         e2 = expf(-r2 * op.dt);
                     }
-                    const float2 E1 = dup(e1), E2 = dup(e2);
-#pragma unroll
-                    for (int k = 0; k < RP; ++k) {
-                        P[k] = mul2(P[k], E2);
-                        M[k] = mul2(M[k], E2);
-                        Z[k] = mul2(Z[k], E1);
-                    }
-                    if (q == 0) Z[0].x += 1.f - e1;
+                    pe1 *= e1;
+                    pe2 *= e2;
                 };
+                // The pulse on the relaxed state (pe2 p, pe2 m, pe1 z + (1 - pe1)
+                // at order 0): the factors ride in the coefficients.
                 auto rotate = [&]() {
                     const float si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
                     const float co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
-                    const float2 ch = dup(0.5f * (1.f + co)), sh = dup(0.5f * (1.f - co));
-                    const float2 hs = dup(0.5f * si), si2 = dup(si), nsi2 = dup(-si), co2 = dup(co);
+                    const float a = 0.5f * (1.f + co) * pe2, b = 0.5f * (1.f - co) * pe2;
+                    const float c = si * pe1, h = 0.5f * si * pe2, d = co * pe1;
+                    const float2 A = dup(a), B = dup(b), C = dup(c), nC = dup(-c), H = dup(h),
+                                 nH = dup(-h), Dz = dup(d);
 #pragma unroll
                     for (int k = 0; k < RP; ++k) {
                         const float2 p = P[k], m = M[k], z = Z[k];
-                        P[k] = fma2(ch, p, fma2(sh, m, mul2(nsi2, z)));
-                        M[k] = fma2(sh, p, fma2(ch, m, mul2(si2, z)));
-                        Z[k] = fma2(hs, fma2(neg1, m, p), mul2(co2, z));
+                        P[k] = fma2(A, p, fma2(B, m, mul2(nC, z)));
+                        M[k] = fma2(B, p, fma2(A, m, mul2(C, z)));
+                        Z[k] = fma2(H, p, fma2(nH, m, mul2(Dz, z)));
                     }
+                    if (q == 0) {
+                        const float r = 1.f - pe1;
+                        P[0].x = fmaf(-si, r, P[0].x);
+                        M[0].x = fmaf(si, r, M[0].x);
+                        Z[0].x = fmaf(co, r, Z[0].x);
+                    }
+                    pe1 = pe2 = 1.f;
                 };
                 if ((code & kEchoMask) == kEchoBits) {
                     relax();
@@ -178,8 +188,13 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                 if (rf == RF_ROTATE) {
                     rotate();
                 } else if (rf == RF_INVERT) {
+                    // Z -> -(pe1 Z + (1 - pe1) at order 0); F+ and F- keep
+                    // owing pe2.
+                    const float2 f = dup(-pe1);
 #pragma unroll
-                    for (int k = 0; k < RP; ++k) Z[k] = mul2(Z[k], neg1);
+                    for (int k = 0; k < RP; ++k) Z[k] = mul2(Z[k], f);
+                    if (q == 0) Z[0].x -= 1.f - pe1;
+                    pe1 = 1.f;
                 }
                 ++g;
                 for (int s = 0; s < op_shift2(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
@@ -188,7 +203,7 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                     for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
                 }
                 if ((code & OP_RECORD) && q == 0 && active)
-                    __stcs(orow + op.record, make_float2(0.f, m0 * P[0].x));
+                    __stcs(orow + op.record, make_float2(0.f, (m0 * pe2) * P[0].x));
                 for (int s = 0; s < op_shift3(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
                 if (code & OP_SPOIL2) {
 #pragma unroll
