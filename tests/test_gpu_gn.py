@@ -246,3 +246,41 @@ def test_server_alone_equals_mix_and_respects_budget(cuda):
     with pytest.raises(ValueError):
         server.submit(MapRequest(torch.zeros((1, 200), dtype=torch.complex64,
                                              device=cuda).expand(10**6, 200)))
+
+
+def test_server_reads_the_host_once_per_iteration(cuda):
+    """A server iteration (step, evaluation, judge, retirement and the
+    completion bookkeeping) waits on the device once: the read of the
+    per-request finished counts."""
+    import os
+    import time
+    import warnings
+
+    from torchsim_gb300.serving import GNServer, MapRequest
+
+    prog, _, _ = _signals(cuda, 4, 0, pulses=200)
+    start = torch.tensor([1000.0, 80.0, 1.0])
+    server = GNServer(prog, 10, BOUNDS, start, budget_bytes=64 << 20, device=cuda)
+    for i, V in enumerate((300, 37, 640)):
+        _, sig, (_, _, _, b1) = _signals(cuda, V, 20 + i, pulses=200)
+        server.submit(MapRequest(sig, torch.from_numpy(b1).to(cuda), id=i))
+    server.admit(0.0)
+    server.step(time.perf_counter)  # first launch: loads the kernels
+    torch.cuda.synchronize()
+    reads = []
+    while server.active:
+        with warnings.catch_warnings(record=True) as caught:
+            warnings.simplefilter("always")
+            torch.cuda.set_sync_debug_mode("warn")
+            try:
+                server.step(time.perf_counter)
+            finally:
+                torch.cuda.set_sync_debug_mode("default")
+        # Synchronizing operations warn from the line that called them; the
+        # one-time notice that the debug mode is a prototype comes from
+        # torch's own module and is not a read.
+        reads.append([f"{w.filename}:{w.lineno}" for w in caught
+                      if "synchroniz" in str(w.message).lower()
+                      and os.sep + "torch" + os.sep not in w.filename])
+    assert len(reads) >= 2 and all(len(r) == 1 for r in reads), reads
+    assert server.stats.completed == 3

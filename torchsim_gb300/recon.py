@@ -342,17 +342,46 @@ class VoxelPool:
                                           stream))
         _native.check(lib.tsg_gn_judge(ctypes.byref(st), self.n, ctypes.byref(config), stream))
 
-    def retire(self) -> dict[str, torch.Tensor]:
+    def retire(self, group: torch.Tensor | None = None, groups: int = 1
+               ) -> dict[str, torch.Tensor | list[int]]:
         """Remove finished voxels; returns their owner rows, free variables,
-        costs and step counts (one host sync)."""
+        costs, step counts and limit flags, and ``counts``: how many finished,
+        per group when ``group`` gives each live voxel's group (in
+        ``range(groups)``), else one total.
+
+        One device-to-host read per call, of those counts. The rows are then
+        partitioned stably (kept rows first, each side in pool order) by two
+        prefix sums and a scatter, and every copy is sized from the counts
+        already on the host."""
         done = self.t["status"] == _native_done()
-        out = {"owner": self.t["owner"][done], "u": self.t["u"][done],
-               "cost": self.t["cost"][done], "iterations": self.t["iterations"][done],
-               "limited": (self.t["flags"][done] & 4)}
-        keep = ~done
-        for name in self.t:
-            self.t[name] = self.t[name][keep].contiguous()
-        self.n = int(self.t["rows"].numel())
+        if group is not None:
+            tally = torch.zeros(groups, dtype=torch.int64, device=self.device)
+            tally.index_add_(0, group, done.to(torch.int64))
+        else:
+            tally = done.sum(dtype=torch.int64).reshape(1)
+        counts = tally.cpu().tolist()
+        finished = int(sum(counts))
+        kept = self.n - finished
+        if finished:
+            flag = done.to(torch.int64)
+            dest = torch.where(done, torch.cumsum(flag, 0) + (kept - 1),
+                               torch.cumsum(1 - flag, 0) - 1)
+            order = torch.empty_like(dest).scatter_(
+                0, dest, torch.arange(self.n, device=self.device))
+            keep_rows, done_rows = order[:kept], order[kept:]
+        else:
+            done_rows = torch.zeros(0, dtype=torch.int64, device=self.device)
+        t = self.t
+        out = {"owner": t["owner"].index_select(0, done_rows),
+               "u": t["u"].index_select(0, done_rows),
+               "cost": t["cost"].index_select(0, done_rows),
+               "iterations": t["iterations"].index_select(0, done_rows),
+               "limited": t["flags"].index_select(0, done_rows) & 4,
+               "counts": counts}
+        if finished:
+            for name in t:
+                t[name] = t[name].index_select(0, keep_rows)
+            self.n = kept
         return out
 
 

@@ -178,12 +178,13 @@ class GNServer:
         self.stats.iterations += 1
         self.stats.launches += 3
         self.stats.voxel_iterations += live
-        out = self.pool.retire()
+        # The one host read of the iteration: finished voxels per request slot.
+        out = self.pool.retire(self.slot_of_row.index_select(0, self.pool.t["owner"]),
+                               self._next_slot)
+        counts = out["counts"]
         done: list[MapRequest] = []
-        if out["owner"].numel():
+        if sum(counts):
             self.answer_u[out["owner"]] = out["u"]
-            counts = torch.bincount(self.slot_of_row[out["owner"]], minlength=self._next_slot)
-            counts = counts.cpu().tolist()
             now = clock()
             for slot, c in enumerate(counts):
                 if c == 0:
