@@ -93,12 +93,19 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        # nvidia-smi takes a moment to start: begin the timed region only once
+        # it is sampling (at most 5 s).
+        deadline = time.perf_counter() + 5.0
+        while not self.lines and self.proc.poll() is None and time.perf_counter() < deadline:
+            time.sleep(0.01)
+        self.first = len(self.lines)
         return self
 
     def _read(self):
@@ -117,7 +124,11 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        # The samples taken while the timed region ran (the last one taken
+        # before it as well when it was shorter than the sampling period).
+        first = getattr(self, "first", 0)
+        lines = self.lines[first:] if len(self.lines) > first else self.lines[max(0, first - 1):]
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -350,14 +361,18 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
         d2h = int(out[0].numel() * 8 + out[1].numel() * 8)
         del out
         torch.cuda.synchronize()
-        n_e2e = max(1, min(args.steps, 5))
+        n_e2e = max(1, min(args.steps, 10))
+        e2e_steps = []
         t0 = time.perf_counter()
         for _ in range(n_e2e):
+            t_step = time.perf_counter()
             out = e2e_step()
             del out
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+            e2e_steps.append((time.perf_counter() - t_step) * 1e3)
         e2e_s = (time.perf_counter() - t0) / n_e2e
         e2e = {"value": updates / e2e_s, "unit": "updates/s", "ms_per_step": e2e_s * 1e3,
+               "steps_ms": e2e_steps,
                "h2d_bytes_per_step": 3 * atoms * 4 + PULSES * 4,
                "d2h_bytes_per_step": d2h,
                "host_link": host_link(torch, device, d2h),

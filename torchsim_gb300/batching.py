@@ -164,7 +164,7 @@ class SequenceBatch:
             if (-(-self.states // orders) > 32).any():
                 continue
             for warps in (2, 4, 8):
-                for per_sm in (2, 4, 8, 16):
+                for per_sm in (2, 4, 5, 6, 8, 10, 12, 16):
                     if warps * per_sm <= 64:
                         cands.append((orders, warps, per_sm))
         return cands

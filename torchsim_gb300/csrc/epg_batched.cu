@@ -22,15 +22,42 @@ __device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
+// Truncation at `states`: the slot of order `states` on the voxel's last lane
+// is cleared after every shift. `slot` (that order's index within the lane,
+// -1 when the state count fills the lanes exactly) is the same for every lane
+// of the block, which runs one sequence, so the switch is a uniform branch
+// and only the lane that `kills` clears one value.
+template <int RP>
+__device__ __forceinline__ void truncate_slot(float2 (&p)[RP], int slot, bool kills) {
+    switch (slot) {
+#define TSG_TRUNCATE_CASE(k)                                  \
+    case k:                                                   \
+        if constexpr (k < 2 * RP) {                           \
+            if constexpr (k < RP) {                           \
+                if (kills) p[k].x = 0.f;                      \
+            } else {                                          \
+                if (kills) p[(k) - RP].y = 0.f;               \
+            }                                                 \
+        }                                                     \
+        break;
+        TSG_TRUNCATE_CASE(0) TSG_TRUNCATE_CASE(1) TSG_TRUNCATE_CASE(2) TSG_TRUNCATE_CASE(3)
+        TSG_TRUNCATE_CASE(4) TSG_TRUNCATE_CASE(5) TSG_TRUNCATE_CASE(6) TSG_TRUNCATE_CASE(7)
+        TSG_TRUNCATE_CASE(8) TSG_TRUNCATE_CASE(9) TSG_TRUNCATE_CASE(10) TSG_TRUNCATE_CASE(11)
+        TSG_TRUNCATE_CASE(12) TSG_TRUNCATE_CASE(13) TSG_TRUNCATE_CASE(14) TSG_TRUNCATE_CASE(15)
+#undef TSG_TRUNCATE_CASE
+        default:
+            break;
+    }
+}
+
 // One gradient shift of the lane's strided order pairs (local order l in
 // pair l % RP, .x below RP and .y above) with a per-sequence lane count L:
 // F- moves one order down, F+ one order up, F+[0] = -F-[0] on the voxel's
-// first lane, nothing crosses a voxel's edge, and the slot of order `states`
-// (kill_k, kill_hi; kill_k -1 where the lane has none) is cleared
-// (truncation). Whole pairs move except one at each edge.
+// first lane, nothing crosses a voxel's edge, and the order `states` is
+// cleared (truncate_slot). Whole pairs move except one at each edge.
 template <int RP>
 __device__ __forceinline__ void shift_pairs(float2 (&p)[RP], float2 (&m)[RP], int q, int L,
-                                            int kill_k, bool kill_hi) {
+                                            int slot, bool kills) {
     const float in_p = __shfl_up_sync(0xffffffffu, p[RP - 1].y, 1);
     const float in_m = __shfl_down_sync(0xffffffffu, m[0].x, 1);
     const float top = (q == L - 1) ? 0.f : in_m;
@@ -43,13 +70,7 @@ __device__ __forceinline__ void shift_pairs(float2 (&p)[RP], float2 (&m)[RP], in
 #pragma unroll
     for (int k = RP - 1; k > 0; --k) p[k] = p[k - 1];
     p[0] = make_float2(bottom, p_edge);
-#pragma unroll
-    for (int k = 0; k < RP; ++k) {
-        if (k == kill_k) {
-            if (kill_hi) p[k].y = 0.f;
-            else p[k].x = 0.f;
-        }
-    }
+    truncate_slot<RP>(p, slot, kills);
 }
 
 // A refocusing op of a CPMG echo: relax, shift, rotate, shift, nothing else.
@@ -60,6 +81,8 @@ constexpr uint32_t kEchoMask = OP_RELAX | (3u << OP_SHIFT1_SHIFT) | (3u << OP_RF
                                (3u << OP_SHIFT3_SHIFT) | OP_SPOIL2;
 constexpr uint32_t kEchoBits = OP_RELAX | (1u << OP_SHIFT1_SHIFT) |
                                (uint32_t(RF_ROTATE) << OP_RF_SHIFT) | (1u << OP_SHIFT2_SHIFT);
+// The recording op of a CPMG echo: relax and record, nothing else.
+constexpr uint32_t kRecordBits = OP_RELAX | OP_RECORD;
 
 }  // namespace
 
@@ -102,10 +125,10 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
         const float r1 = 1000.f / t1;
         const float r2 = 1000.f / t2;
         const int S = sq.states;
-        const int kill_r = S - q * R;
-        const bool kill = L * R > S && kill_r >= 0 && kill_r < R;
-        const int kill_k = kill ? kill_r % RP : -1;
-        const bool kill_hi = kill_r >= RP;
+        // The order `states` falls on the voxel's last lane, at slot S % R
+        // (none when the lanes hold exactly S orders).
+        const int kill_slot = L * R > S ? S % R : -1;
+        const bool kills = q == L - 1;
         float2 P[RP], M[RP], Z[RP];
 #pragma unroll
         for (int k = 0; k < RP; ++k) P[k] = M[k] = Z[k] = dup(0.f);
@@ -176,14 +199,21 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                 };
                 if ((code & kEchoMask) == kEchoBits) {
                     relax();
-                    shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                    shift_pairs<RP>(P, M, q, L, kill_slot, kills);
                     rotate();
                     ++g;
-                    shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                    shift_pairs<RP>(P, M, q, L, kill_slot, kills);
+                    continue;
+                }
+                if ((code & kEchoMask) == kRecordBits) {
+                    relax();
+                    if (q == 0 && active)
+                        __stcs(orow + op.record, make_float2(0.f, (m0 * pe2) * P[0].x));
+                    ++g;
                     continue;
                 }
                 if (code & OP_RELAX) relax();
-                for (int s = 0; s < op_shift1(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                for (int s = 0; s < op_shift1(code); ++s) shift_pairs<RP>(P, M, q, L, kill_slot, kills);
                 const int rf = op_rf(code);
                 if (rf == RF_ROTATE) {
                     rotate();
@@ -197,14 +227,14 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                     pe1 = 1.f;
                 }
                 ++g;
-                for (int s = 0; s < op_shift2(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                for (int s = 0; s < op_shift2(code); ++s) shift_pairs<RP>(P, M, q, L, kill_slot, kills);
                 if (code & OP_SPOIL1) {
 #pragma unroll
                     for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
                 }
                 if ((code & OP_RECORD) && q == 0 && active)
                     __stcs(orow + op.record, make_float2(0.f, (m0 * pe2) * P[0].x));
-                for (int s = 0; s < op_shift3(code); ++s) shift_pairs<RP>(P, M, q, L, kill_k, kill_hi);
+                for (int s = 0; s < op_shift3(code); ++s) shift_pairs<RP>(P, M, q, L, kill_slot, kills);
                 if (code & OP_SPOIL2) {
 #pragma unroll
                     for (int k = 0; k < RP; ++k) P[k] = M[k] = dup(0.f);
