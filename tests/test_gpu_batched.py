@@ -125,3 +125,41 @@ def test_autotuner_picks_a_working_shape(cuda, tmp_path, monkeypatch):
     _check_against_oracle(batch)
     again, cached = batch.tune()
     assert again == shape and cached == {}
+
+
+def test_cpmg_echo_loop_and_op_loop_in_one_launch(cuda):
+    """CPMG trains run the kernel's echo loop; any other program (MRF trains
+    after an inversion, at a fixed or a varying TR) runs the general op loop.
+    Both kinds in one launch, each against the FP64 oracle, and a CPMG train
+    alone equal to its row in the mix."""
+    from torchsim_gb300.batching import BatchEntry, SequenceBatch
+    from torchsim_gb300.sequence import fse_events, mrf_events
+    from tests.helpers import mrf_schedule
+
+    rng = np.random.default_rng(7)
+
+    def tissue(v):
+        return (rng.uniform(300, 3000, v).astype(np.float32),
+                rng.uniform(10, 300, v).astype(np.float32),
+                rng.uniform(0.7, 1.3, v).astype(np.float32))
+
+    entries = [
+        BatchEntry(fse_events(rng.uniform(100, 180, 24).astype(np.float32), 8.0,
+                              phases_deg=90.0), 48, *tissue(200)),
+        BatchEntry(mrf_events(mrf_schedule()[:120], 10.0), 20, *tissue(150)),
+        BatchEntry(mrf_events(rng.uniform(5, 70, 90).astype(np.float32),
+                              rng.uniform(8, 15, 90).astype(np.float32), TI_ms=20.0), 33,
+                   *tissue(64)),
+        BatchEntry(fse_events(rng.uniform(100, 180, 9).astype(np.float32), 12.0,
+                              phases_deg=90.0), 18, *tissue(77)),
+    ]
+    for shape in ((16, 2, 8), (4, 4, 4)):
+        batch = SequenceBatch(entries, cuda)
+        batch.out.fill_(float("nan"))
+        batch.launch(shape)
+        torch.cuda.synchronize()
+        _check_against_oracle(batch)
+        alone = SequenceBatch([entries[0]], cuda)
+        alone.launch(shape)
+        torch.cuda.synchronize()
+        assert torch.equal(alone.signal(0), batch.signal(0))

@@ -73,6 +73,25 @@ __device__ __forceinline__ void shift_pairs(float2 (&p)[RP], float2 (&m)[RP], in
     truncate_slot<RP>(p, slot, kills);
 }
 
+// The pulse on the relaxed state (w2 p, w2 m, w1 z + (1 - w1) at order 0,
+// with the factors w1, w2 the relaxation still owes), without the recovery
+// term, which only the voxel's first lane adds.
+template <int RP>
+__device__ __forceinline__ void rotate_pairs(float2 (&P)[RP], float2 (&M)[RP], float2 (&Z)[RP],
+                                             float si, float co, float w1, float w2) {
+    const float a = 0.5f * (1.f + co) * w2, b = 0.5f * (1.f - co) * w2;
+    const float c = si * w1, h = 0.5f * si * w2, d = co * w1;
+    const float2 A = dup(a), B = dup(b), C = dup(c), nC = dup(-c), H = dup(h), nH = dup(-h),
+                 Dz = dup(d);
+#pragma unroll
+    for (int k = 0; k < RP; ++k) {
+        const float2 p = P[k], m = M[k], z = Z[k];
+        P[k] = fma2(A, p, fma2(B, m, mul2(nC, z)));
+        M[k] = fma2(B, p, fma2(A, m, mul2(C, z)));
+        Z[k] = fma2(H, p, fma2(nH, m, mul2(Dz, z)));
+    }
+}
+
 // A refocusing op of a CPMG echo: relax, shift, rotate, shift, nothing else.
 // It takes a straight-line path in which the shifts' moves fold into the
 // relaxation's and the rotation's own results.
@@ -148,6 +167,65 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
             for (int i = threadIdx.x; i < count; i += blockDim.x)
                 s_ops[i] = ops[sq.op_offset + base + i];
             __syncthreads();
+            // A CPMG train held whole in one chunk -- the excitation alone,
+            // then per echo the refocusing op and the recording op, one
+            // interval throughout -- runs the echo loop: no op decoding, the
+            // relaxation factors fixed (e at the first echo, e^2 after), the
+            // same arithmetic as the op loop below.
+            if (base == 0 && count == sq.op_count) {
+                const bool odd = (count & 1) && count >= 3;
+                bool fits = odd;
+                for (int i = threadIdx.x; odd && i < count; i += blockDim.x) {
+                    const Op o = s_ops[i];
+                    if (i == 0)
+                        fits &= o.code == (uint32_t(RF_ROTATE) << OP_RF_SHIFT);
+                    else
+                        fits &= (o.code & kEchoMask) == ((i & 1) ? kEchoBits : kRecordBits) &&
+                                o.dt == s_ops[1].dt;
+                }
+                if (__syncthreads_and(fits)) {
+                    const int echoes = count >> 1;
+                    {
+                        float si, co;
+                        sincosf(s_ops[0].flip * b1, &si, &co);
+                        rotate_pairs<RP>(P, M, Z, si, co, 1.f, 1.f);  // recovery 1 - 1 = 0
+                    }
+                    const float dt = s_ops[1].dt;
+                    const float f1 = expf(-r1 * dt), f2 = expf(-r2 * dt);
+                    const float f11 = f1 * f1, f22 = f2 * f2;
+                    const float m0f2 = m0 * f2;
+                    float w1 = f1, w2 = f2;
+                    float my_si = 0.f, my_co = 1.f;
+                    int g = L;  // echoes since the voxel's lanes last evaluated sin/cos
+                    for (int e = 0; e < echoes; ++e) {
+                        if (g == L) {
+                            g = 0;
+                            const int j = e + q;
+                            float sj = 0.f, cj = 1.f;
+                            if (j < echoes) sincosf(s_ops[2 * j + 1].flip * b1, &sj, &cj);
+                            my_si = sj;
+                            my_co = cj;
+                        }
+                        const float si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
+                        const float co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
+                        ++g;
+                        shift_pairs<RP>(P, M, q, L, kill_slot, kills);
+                        rotate_pairs<RP>(P, M, Z, si, co, w1, w2);
+                        if (q == 0) {
+                            const float r = 1.f - w1;
+                            P[0].x = fmaf(-si, r, P[0].x);
+                            M[0].x = fmaf(si, r, M[0].x);
+                            Z[0].x = fmaf(co, r, Z[0].x);
+                        }
+                        shift_pairs<RP>(P, M, q, L, kill_slot, kills);
+                        if (q == 0 && active)
+                            __stcs(orow + s_ops[2 * e + 2].record, make_float2(0.f, m0f2 * P[0].x));
+                        w1 = f11;
+                        w2 = f22;
+                    }
+                    continue;
+                }
+            }
             float my_si = 0.f, my_co = 1.f;
             int g = L;  // ops since the voxel's lanes last evaluated sin/cos
             for (int i = 0; i < count; ++i) {
@@ -178,17 +256,7 @@ __global__ void __launch_bounds__(256) epg_batched_kernel(
                 auto rotate = [&]() {
                     const float si = __shfl_sync(0xffffffffu, my_si, first_lane + g);
                     const float co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
-                    const float a = 0.5f * (1.f + co) * pe2, b = 0.5f * (1.f - co) * pe2;
-                    const float c = si * pe1, h = 0.5f * si * pe2, d = co * pe1;
-                    const float2 A = dup(a), B = dup(b), C = dup(c), nC = dup(-c), H = dup(h),
-                                 nH = dup(-h), Dz = dup(d);
-#pragma unroll
-                    for (int k = 0; k < RP; ++k) {
-                        const float2 p = P[k], m = M[k], z = Z[k];
-                        P[k] = fma2(A, p, fma2(B, m, mul2(nC, z)));
-                        M[k] = fma2(B, p, fma2(A, m, mul2(C, z)));
-                        Z[k] = fma2(H, p, fma2(nH, m, mul2(Dz, z)));
-                    }
+                    rotate_pairs<RP>(P, M, Z, si, co, pe1, pe2);
                     if (q == 0) {
                         const float r = 1.f - pe1;
                         P[0].x = fmaf(-si, r, P[0].x);
