@@ -700,8 +700,47 @@ def case_gn(ts, rec) -> dict:
             "unconverged": np.int64(est.unconverged)}
 
 
+def case_gn_slice(ts, rec) -> dict:
+    """The reference's NonlinearLeastSquares on a 4,096-voxel slice (the
+    mapping workload's request size), B1 known. The measured signals are not
+    stored: they are the reference's noise-free signal, which the oracle's
+    FP32 port reproduces bit for bit from the stored tissue, plus complex
+    Gaussian noise drawn from `noise_seed` and scaled by the stored `sigma`;
+    every 64th row of them is kept to check the regeneration."""
+    import torch
+    from torchsim import NonlinearLeastSquares
+    from torchsim.simulators import MRFSimulator
+
+    rng = np.random.default_rng(9)
+    v = 4096
+    flip = np.concatenate([np.linspace(5, 60, 60), np.linspace(60, 2, 60)]).astype(np.float32)
+    t1, t2, b1 = draw_tissue(rng, v)
+    m0 = rng.uniform(0.5, 1.5, v).astype(np.float32)
+    sim = MRFSimulator(flip=torch.from_numpy(flip), TR=10.0, states=10)
+    with torch.no_grad():
+        sig = sim.simulate(T1=torch.from_numpy(t1), T2=torch.from_numpy(t2),
+                           B1=torch.from_numpy(b1), M0=torch.from_numpy(m0))
+    sigma = float(sig.abs().mean()) / 50.0
+    noise_seed = 90
+    nrng = np.random.default_rng(noise_seed)
+    noise = (nrng.standard_normal(sig.shape) + 1j * nrng.standard_normal(sig.shape)) * sigma
+    y = (sig.numpy() + noise).astype(np.complex64)
+    bounds = {"T1": (50.0, 5000.0), "T2": (2.0, 1000.0), "M0": (0.0, 5.0)}
+    est = NonlinearLeastSquares(sim, bounds=bounds)
+    est.fit(T1=(100.0, 3000.0), T2=(10.0, 300.0), M0=(0.5, 1.5), known={"B1": (0.8, 1.2)}, seed=0)
+    maps = est.map(torch.from_numpy(y), known={"B1": torch.from_numpy(b1)})
+    return {"flip_deg": flip, "tr_ms": np.float32(10.0), "states": np.int64(10), "t1": t1,
+            "t2": t2, "b1": b1, "m0": m0, "sigma": np.float64(sigma),
+            "noise_seed": np.int64(noise_seed), "measured_every_64th": y[::64],
+            "start": est._start.numpy(),
+            "bounds": np.array([bounds[k] for k in ("T1", "T2", "M0")], np.float64),
+            "map_t1": maps["T1"].numpy(), "map_t2": maps["T2"].numpy(),
+            "map_m0": maps["M0"].numpy(), "iterations": np.int64(est.iterations),
+            "unconverged": np.int64(est.unconverged)}
+
+
 CASES = ("mrf880", "mrf_prep", "fse_cpmg", "mrf_adjoint", "gn_mrf", "fse_phase0", "mrf_offaxis",
-         "complex_jvp",
+         "complex_jvp", "gn_slice",
          "mrf_second", "complex_adjoint", "double_backward", "grouping", "design_loop", "bounds")
 
 
@@ -728,7 +767,7 @@ def main() -> None:
                      ("mrf_second", case_second), ("complex_adjoint", case_complex_adjoint),
                      ("double_backward", case_double_backward), ("grouping", case_grouping),
                      ("design_loop", case_design_loop), ("bounds", case_bounds),
-                     ("complex_jvp", case_complex_jvp)):
+                     ("complex_jvp", case_complex_jvp), ("gn_slice", case_gn_slice)):
         if name not in wanted:
             continue
         data = fn(ts, rec)

@@ -64,3 +64,22 @@ def max_rel(actual, expected) -> float:
     if scale == 0.0:
         return float(np.abs(actual).max()) if actual.size else 0.0
     return float(np.abs(actual - expected).max() / scale)
+
+
+def gn_slice_measured(d) -> np.ndarray:
+    """The noisy signals of the `gn_slice` fixture, (voxels, pulses)
+    complex64: the reference's noise-free MRF signal (1j times the recorded
+    sample 1j m0 F+[0], i.e. -m0 F+[0] on the real axis, which the oracle's
+    FP32 port reproduces bit for bit) plus the
+    fixture's seeded complex Gaussian noise, added in float64 and rounded to
+    complex64 as the fixture's generator did."""
+    from torchsim_gb300.sequence import mrf_events
+
+    events = mrf_events(d["flip_deg"], float(d["tr_ms"]))
+    imag = O.forward(packed_from_events(events, d["t1"], d["t2"], int(d["states"]),
+                                        m0=d["m0"], b1=d["b1"]), "f32", threads=8)
+    sig = (-imag.astype(np.float32)).astype(np.complex64)
+    rng = np.random.default_rng(int(d["noise_seed"]))
+    sigma = float(d["sigma"])
+    noise = (rng.standard_normal(sig.shape) + 1j * rng.standard_normal(sig.shape)) * sigma
+    return (sig + noise).astype(np.complex64)

@@ -304,3 +304,16 @@ def test_oracle_complex_adjoint_is_the_gradient_of_the_forward(golden):
         fd = (loss(1.0) - loss(-1.0)) / (2 * h)
         got = float((g[name].reshape(v.shape) * v).sum())
         assert abs(got - fd) <= 2e-3 * max(abs(fd), 1e-9), (name, got, fd)
+
+
+def test_gn_slice_signals_regenerate_bitwise(golden):
+    """The 4,096-voxel mapping fixture keeps the tissue, the noise seed and
+    sigma instead of its 4 MB of signals: the oracle's FP32 port gives the
+    reference's noise-free signal bit for bit, so the regenerated noisy
+    signals equal the stored sample of rows exactly."""
+    from tests.helpers import gn_slice_measured
+
+    d = golden("gn_slice")
+    y = gn_slice_measured(d)
+    assert y.shape == (4096, 120)
+    assert np.array_equal(y[::64], d["measured_every_64th"])
