@@ -454,7 +454,8 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
                                        "rotation 15",
                          "peak_source": "the FP32 FMA probe of this run"}
     if not args.skip_gn:
-        line["gn_server"] = gn_section(torch, device, requests=args.gn_requests)
+        line["gn_server"] = gn_section(torch, device, requests=args.gn_requests,
+                                       cpu_sample=0 if args.skip_cpu else 4096)
     if not args.skip_match:
         line["dictionary_match"] = match_section(torch, device, voxels=args.match_voxels)
     if not args.skip_cpu:
@@ -970,7 +971,8 @@ def match_section(torch, device, voxels: int = 65536, repeats: int = 3) -> dict:
 # ---- Gauss-Newton mapping server ---------------------------------------------
 
 
-def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:  # noqa: C901
+def gn_section(torch, device, requests: int = 40, rate: float = 20.0,  # noqa: C901
+               cpu_sample: int = 4096) -> dict:
     """Poisson arrivals (20 req/s, seeded); each request one slice of
     round(exp(U(ln 4096, ln 262144))) voxels of the 880-pulse MRF signal at
     ground-truth T1/T2/B1 (drawn as the 1,024-voxel workload) and M0 U(0.5,1.5)
@@ -1078,9 +1080,36 @@ def gn_section(torch, device, requests: int = 40, rate: float = 20.0) -> dict:  
         [MapRequest(s, b, arrival=0.0, id=i) for i, (s, b, a, _) in enumerate(made[:sat])],
         PlainGaussNewton(TrustRegion(), max_iterations=10)))
     sat_plain = time.perf_counter() - t0
+    # The CPU baseline of the mapping workload: the reference's loop (LM,
+    # TrustRegion, one forward and one tangent pass per EPG-dependent unknown
+    # per step) restated over the oracle's FP32 port of its kernels, on all
+    # host cores, on the first request's first `cpu_sample` voxels.
+    cpu = None
+    if cpu_sample > 0:
+        from oracle import gn_port
+
+        n = min(cpu_sample, made[0][0].shape[0])
+        y = made[0][0][:n].cpu().numpy()
+        b1_host = made[0][1][:n].cpu().numpy()
+        events = mrf_events(mrf_schedule(), 10.0)
+        low = np.array([bounds[k][0] for k in ("T1", "T2", "M0")])
+        high = np.array([bounds[k][1] for k in ("T1", "T2", "M0")])
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        got = gn_port.fit(events, y, np.asarray(start, np.float64), low, high, 10, b1=b1_host,
+                          max_iterations=10, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"maps_per_s": n / cpu_s, "seconds": cpu_s, "cores": threads, "kind": "port",
+               "cpu": cpu_model(),
+               "sample": f"the first request's first {n} voxels, <=10 LM steps "
+                         f"({got.passes} EPG passes over the voxels still moving)",
+               "form": "the reference's Levenberg-Marquardt/TrustRegion loop over the oracle's "
+                       "FP32 port of its kernels: per step one forward and one tangent pass "
+                       "per EPG-dependent unknown (T1, T2), FP64 3x3 solves"}
     return {
         "workload": f"{requests} requests, Poisson {rate}/s, {total_voxels} voxels, 880-pulse "
                     "MRF, nstates 10, SNR 50, <=10 LM steps, 120 GB budget",
+        "cpu_baseline": cpu,
         "server": {"maps_per_s": total_voxels / span, "makespan_s": span, **lat,
                    "iterations": server_stats.iterations,
                    "launches_per_iteration": 3,

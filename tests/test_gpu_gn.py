@@ -321,3 +321,32 @@ def test_nlls_on_a_4096_voxel_slice_matches_the_reference(cuda, golden):
         assert q99 <= 1e-3, (name, report)
         assert share == 0.0, (name, report)
     assert est.unconverged <= 2 * int(d["unconverged"]) + 20
+
+
+def test_fused_gn_matches_the_cpu_restatement_step_for_step(cuda, golden):
+    """The fused route (FP64 step and judge kernels over normal equations the
+    sweep reduces) against the CPU restatement of the same loop
+    (oracle/gn_port.py, pinned to the reference's estimator on the CPU), 1,024
+    voxels of the 4,096-voxel fixture, 10 steps, the same start: the same
+    number of steps per voxel almost everywhere and the same maps."""
+    from oracle import gn_port
+    from tests.helpers import gn_slice_measured
+    from torchsim_gb300.recon import GaussNewton, TrustRegion
+    from torchsim_gb300.sequence import mrf_events, program_for
+
+    d = golden("gn_slice")
+    n = 1024
+    y = gn_slice_measured(d)[:n]
+    events = mrf_events(d["flip_deg"], float(d["tr_ms"]))
+    bounds = {k: tuple(d["bounds"][i]) for i, k in enumerate(("T1", "T2", "M0"))}
+    cpu = gn_port.fit(events, y, d["start"], d["bounds"][:, 0], d["bounds"][:, 1],
+                      int(d["states"]), b1=d["b1"][:n], max_iterations=10, threads=8)
+    sol = GaussNewton(TrustRegion(), max_iterations=10).minimize_program(
+        program_for(events, cuda), torch.from_numpy(y).to(cuda), torch.from_numpy(d["start"]),
+        bounds, int(d["states"]), b1=torch.from_numpy(d["b1"][:n]).to(cuda))
+    x = sol.x.cpu().numpy().astype(np.float64)
+    for k in range(3):
+        err = np.abs(x[:, k] - cpu.x[:, k]) / np.abs(cpu.x[:, k])
+        assert np.median(err) <= 1e-5, k
+        assert np.quantile(err, 0.99) <= 1e-3, k
+    assert float((sol.steps.cpu().numpy() == cpu.steps).mean()) >= 0.95
