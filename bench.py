@@ -1190,6 +1190,11 @@ def cpu_baseline(sample: int) -> dict:
             "cores": threads, "kind": kind, "cpu": cpu_model(),
             "sample": f"first {sample} of the {ATOMS} grid atoms, forward + 3 tangent passes "
                       f"(the reference's per-column call pattern), {seconds:.2f} s"}
+    # One thread as well, on an eighth of the sample.
+    one = max(8, sample // 8)
+    seconds1, _ = cpu_run(one, 1)
+    line["single_thread"] = {"value": float(one) * PULSES * STATES / seconds1,
+                             "sample_atoms": one, "seconds": seconds1}
     if kind == "port":
         line["why_port"] = PORT_NOTE
     return line
