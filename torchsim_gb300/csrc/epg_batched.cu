@@ -110,8 +110,14 @@ constexpr uint32_t kRecordBits = OP_RELAX | OP_RECORD;
 // lane q of a voxel takes one of every L ops and the voxel's lanes exchange
 // the values by shuffle (all lanes of a warp run the same sequence, so the
 // shuffles are convergent).
-template <int R>
-__global__ void __launch_bounds__(256) epg_batched_kernel(
+// NARROW instantiations serve 2-warp blocks only, under a register budget
+// that lets kNarrowBlocks of them share an SM.
+#ifndef TSG_BATCH_NARROW_BLOCKS
+#define TSG_BATCH_NARROW_BLOCKS 10
+#endif
+constexpr int kNarrowBlocks = TSG_BATCH_NARROW_BLOCKS;
+template <int R, bool NARROW = false>
+__global__ void __launch_bounds__(NARROW ? 64 : 256, NARROW ? kNarrowBlocks : 1) epg_batched_kernel(
     const Op* __restrict__ ops, const tsg_batch_sequence* __restrict__ seqs,
     const tsg_batch_unit* __restrict__ units, int64_t unit_count, int* __restrict__ counter,
     const float* __restrict__ t1v, const float* __restrict__ t2v, const float* __restrict__ m0v,
@@ -351,9 +357,15 @@ extern "C" int tsg_epg_batched_forward(const void* ops, const tsg_batch_sequence
                                                           tissue->b1, y);
             break;
         case 16:
-            epg_batched_kernel<16><<<grid, block, 0, s>>>(o, sequences, units, unit_count, counter,
-                                                           tissue->t1_ms, tissue->t2_ms, tissue->m0,
-                                                           tissue->b1, y);
+            if (warps_per_block == 2)
+                epg_batched_kernel<16, true><<<grid, block, 0, s>>>(
+                    o, sequences, units, unit_count, counter, tissue->t1_ms, tissue->t2_ms,
+                    tissue->m0, tissue->b1, y);
+            else
+                epg_batched_kernel<16><<<grid, block, 0, s>>>(o, sequences, units, unit_count,
+                                                               counter, tissue->t1_ms,
+                                                               tissue->t2_ms, tissue->m0,
+                                                               tissue->b1, y);
             break;
         default:
             return fail(TSG_ERR_UNSUPPORTED, "orders_per_lane must be 2, 4, 8 or 16");
