@@ -92,6 +92,30 @@ __device__ __forceinline__ void rotate_pairs(float2 (&P)[RP], float2 (&M)[RP], f
     }
 }
 
+// The same pulse in sum/difference form, for the echo loop: with S = p + m
+// and D = p - m, P' = k S + T and M' = k S - T where T = e D - c z, and
+// Z' = h D + d z (k = w2/2, e = k cos, c = w1 sin, h = k sin, d = w1 cos).
+// The coefficient pairs come from the shuffled (sin, sin) and (cos, cos)
+// pairs by four paired products; K, W1 and -W1 are fixed per phase.
+template <int RP>
+__device__ __forceinline__ void rotate_sumdiff(float2 (&P)[RP], float2 (&M)[RP], float2 (&Z)[RP],
+                                               float2 si2, float2 co2, float2 K, float2 W1,
+                                               float2 nW1) {
+    const float2 neg1 = dup(-1.f);
+    const float2 E = mul2(co2, K), nC = mul2(si2, nW1), H = mul2(si2, K), Dz = mul2(co2, W1);
+#pragma unroll
+    for (int k = 0; k < RP; ++k) {
+        const float2 p = P[k], m = M[k], z = Z[k];
+        const float2 S = __fadd2_rn(p, m);
+        const float2 D = fma2(m, neg1, p);
+        const float2 T = fma2(E, D, mul2(nC, z));
+        const float2 KS = mul2(K, S);
+        P[k] = __fadd2_rn(KS, T);
+        M[k] = fma2(T, neg1, KS);
+        Z[k] = fma2(H, D, mul2(Dz, z));
+    }
+}
+
 // A refocusing op of a CPMG echo: relax, shift, rotate, shift, nothing else.
 // It takes a straight-line path in which the shifts' moves fold into the
 // relaxation's and the rotation's own results.
@@ -174,10 +198,11 @@ __global__ void __launch_bounds__(NARROW ? 64 : 256, NARROW ? kNarrowBlocks : 1)
                 s_ops[i] = ops[sq.op_offset + base + i];
             __syncthreads();
             // A CPMG train held whole in one chunk -- the excitation alone,
-            // then per echo the refocusing op and the recording op, one
-            // interval throughout -- runs the echo loop: no op decoding, the
-            // relaxation factors fixed (e at the first echo, e^2 after), the
-            // same arithmetic as the op loop below.
+            // then per echo the refocusing op and the recording op (echo e
+            // recorded as sample e), one interval throughout -- runs the echo
+            // loop: no op decoding, the relaxation factors fixed (e at the
+            // first echo, e^2 after), the pulse in sum/difference form, the
+            // record pointer advanced by one sample per echo.
             if (base == 0 && count == sq.op_count) {
                 const bool odd = (count & 1) && count >= 3;
                 bool fits = odd;
@@ -187,7 +212,7 @@ __global__ void __launch_bounds__(NARROW ? 64 : 256, NARROW ? kNarrowBlocks : 1)
                         fits &= o.code == (uint32_t(RF_ROTATE) << OP_RF_SHIFT);
                     else
                         fits &= (o.code & kEchoMask) == ((i & 1) ? kEchoBits : kRecordBits) &&
-                                o.dt == s_ops[1].dt;
+                                o.dt == s_ops[1].dt && ((i & 1) || o.record == (i >> 1) - 1);
                 }
                 if (__syncthreads_and(fits)) {
                     const int echoes = count >> 1;
@@ -200,9 +225,11 @@ __global__ void __launch_bounds__(NARROW ? 64 : 256, NARROW ? kNarrowBlocks : 1)
                     const float f1 = expf(-r1 * dt), f2 = expf(-r2 * dt);
                     const float f11 = f1 * f1, f22 = f2 * f2;
                     const float m0f2 = m0 * f2;
-                    float w1 = f1, w2 = f2;
+                    float w1 = f1;
+                    float2 K = dup(0.5f * f2), W1 = dup(f1), nW1 = dup(-f1);
                     float my_si = 0.f, my_co = 1.f;
                     int g = L;  // echoes since the voxel's lanes last evaluated sin/cos
+                    float2* rec = orow;
                     for (int e = 0; e < echoes; ++e) {
                         if (g == L) {
                             g = 0;
@@ -216,7 +243,7 @@ __global__ void __launch_bounds__(NARROW ? 64 : 256, NARROW ? kNarrowBlocks : 1)
                         const float co = __shfl_sync(0xffffffffu, my_co, first_lane + g);
                         ++g;
                         shift_pairs<RP>(P, M, q, L, kill_slot, kills);
-                        rotate_pairs<RP>(P, M, Z, si, co, w1, w2);
+                        rotate_sumdiff<RP>(P, M, Z, dup(si), dup(co), K, W1, nW1);
                         if (q == 0) {
                             const float r = 1.f - w1;
                             P[0].x = fmaf(-si, r, P[0].x);
@@ -224,10 +251,12 @@ __global__ void __launch_bounds__(NARROW ? 64 : 256, NARROW ? kNarrowBlocks : 1)
                             Z[0].x = fmaf(co, r, Z[0].x);
                         }
                         shift_pairs<RP>(P, M, q, L, kill_slot, kills);
-                        if (q == 0 && active)
-                            __stcs(orow + s_ops[2 * e + 2].record, make_float2(0.f, m0f2 * P[0].x));
+                        if (q == 0 && active) __stcs(rec, make_float2(0.f, m0f2 * P[0].x));
+                        ++rec;
                         w1 = f11;
-                        w2 = f22;
+                        K = dup(0.5f * f22);
+                        W1 = dup(f11);
+                        nW1 = dup(-f11);
                     }
                     continue;
                 }
