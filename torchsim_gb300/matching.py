@@ -270,7 +270,7 @@ class DictionaryMatcher:
             b = torch.cat((s.imag, -s.real), dim=1)
         else:
             a, b = s.real, s.imag
-        rows = torch.stack((a, b), dim=1).reshape(2 * s.shape[0], -1)
+        rows = torch.stack((a, b), dim=1).reshape(2 * s.shape[0], a.shape[1])
         rows = _pad8(rows * self._screen_scale).to(torch.float16)
         return torch.cat((rows, rows), dim=1).contiguous()
 
@@ -326,7 +326,7 @@ class DictionaryMatcher:
         shape = (*sample_shape, self.top_k)
         params = None
         if self.parameter_values is not None:
-            params = self.parameter_values[indices].reshape(*shape, -1)
+            params = self.parameter_values[indices].reshape(*shape, self.parameter_values.shape[-1])
         return MatchResult(parameters=params, indices=indices.reshape(shape),
                            scores=scores.reshape(shape), scales=scales.reshape(shape),
                            densities=densities.reshape(shape))

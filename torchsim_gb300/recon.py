@@ -564,7 +564,7 @@ class ModelOperator(torch.nn.Module):
         flat, shape = self._flat(x)
         blocks = self._blocks(flat)[1]
         out = torch.einsum("vct,vt->vc", blocks.conj(),
-                           v.reshape(flat.shape[0], -1).to(blocks.dtype)).real
+                           v.reshape(flat.shape[0], v.shape[-1]).to(blocks.dtype)).real
         return out.reshape(*shape, out.shape[-1])
 
 
@@ -658,7 +658,7 @@ class GaussNewton:
         shape = initial.shape[:-1]
         start = initial.reshape(-1, initial.shape[-1]).to(device)
         V = start.shape[0]
-        data = measured.reshape(V, -1).to(device, torch.complex64).contiguous()
+        data = measured.reshape(V, measured.shape[-1]).to(device, torch.complex64).contiguous()
         order = [operator.unknown.index(name) for name in UNKNOWN]
         u0 = start.to(torch.float64)[:, order]
         if b1 is not None:
@@ -733,7 +733,7 @@ class GaussNewton:
         policy = self.damping
         shape = initial.shape[:-1]
         start = initial.reshape(-1, initial.shape[-1])
-        data = measured.reshape(start.shape[0], -1).to(start.device)
+        data = measured.reshape(start.shape[0], measured.shape[-1]).to(start.device)
         retiring = bool(getattr(policy, "per_voxel", False))
         answer = start.clone()
         live = torch.arange(start.shape[0], device=start.device)
@@ -984,7 +984,7 @@ class NonlinearLeastSquares(torch.nn.Module):
         if given is None:
             raise ValueError(f"this estimator needs {sorted(self._known)} measured")
         if isinstance(given, torch.Tensor):
-            return given.reshape(voxels, -1).to(device, torch.float32)
+            return given.reshape(voxels, len(self._known)).to(device, torch.float32)
         columns = []
         for name in self._known:
             if name not in given:
