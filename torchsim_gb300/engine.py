@@ -572,12 +572,22 @@ def adjoint(program: Program, tissue: TissueMaps, states: int, seed: torch.Tenso
     return grads
 
 
+def _unwrapped(x):
+    """A tensor without the wrappers a function transform (``torch.func.jvp``)
+    puts around the tensors it tracks: the values the kernels read."""
+    if x is None:
+        return None
+    while torch._C._functorch.is_functorch_wrapped_tensor(x):
+        x = torch._C._functorch.get_unwrapped(x)
+    return x
+
+
 def _detached_maps(t1, t2, m0, b1, inv) -> TissueMaps:
     """The autograd inputs as contiguous device maps (a broadcast input is a
     stride-0 view; the kernels index one value per voxel)."""
 
     def c(x):
-        return None if x is None else x.detach().contiguous()
+        return None if x is None else _unwrapped(x).detach().contiguous()
 
     return TissueMaps(c(t1), c(t2), c(m0), c(b1), c(inv))
 
@@ -895,30 +905,67 @@ def adjoint_complex(program: Program, tissue: TissueMaps, states: int, seed: tor
     return grads
 
 
+def _offaxis_of(keep) -> _native.Offaxis:
+    """The off-axis maps (transmit phase, off-resonance) kept by a Function."""
+    return _native.Offaxis(None if keep[0] is None else keep[0].data_ptr(),
+                           None if keep[1] is None else keep[1].data_ptr())
+
+
 class EpgComplexFunction(torch.autograd.Function):
     """The complex-path forward whose backward is the complex adjoint kernel:
     the role of the reference's ``_NativeEpg`` with a complex verdict
     (sequence/_accelerators.py:1402-1594). Inputs are the flat tissue maps
     (with the transmit phase and off-resonance) and the event-level flip,
     duration and phase buffers of the program (for gradient routing only:
-    their values are baked into ``program``); the output is the complex64
-    ``1j * m0 F+[0] e^{-i phase}``, ``(trains*voxels, outputs)``."""
+    their values are baked into ``program``); the outputs are the complex64
+    ``1j * m0 F+[0] e^{-i phase}``, ``(trains*voxels, outputs)``, and the
+    stored trajectory (not differentiable). Forward mode (``jvp``, as
+    ``torch.func.jvp`` and dual tensors call it; the reference's
+    ``_NativeEpg.jvp``, :1512-1535) runs one general tangent sweep along all
+    the inputs' tangents at once."""
 
     @staticmethod
-    def forward(ctx, program, states, launch, t1, t2, m0, b1, inv, b1_phase, b0, flip_events,
+    def forward(program, states, launch, t1, t2, m0, b1, inv, b1_phase, b0, flip_events,
                 duration_events, phase_events):
         tissue = _detached_maps(t1, t2, m0, b1, inv)
         keep = [None if x is None else x.detach().contiguous() for x in (b1_phase, b0)]
-        off = _native.Offaxis(None if keep[0] is None else keep[0].data_ptr(),
-                              None if keep[1] is None else keep[1].data_ptr())
-        out, traj = forward_complex_trajectory(program, tissue, states, off, launch=launch)
-        ctx.program, ctx.states, ctx.launch, ctx.tissue, ctx.keep = program, states, launch, \
-            tissue, keep
-        ctx.save_for_backward(traj)
-        return out
+        return forward_complex_trajectory(program, tissue, states, _offaxis_of(keep),
+                                          launch=launch)
 
     @staticmethod
-    def backward(ctx, grad_out):
+    def setup_context(ctx, inputs, output):
+        program, states, launch, t1, t2, m0, b1, inv, b1_phase, b0 = inputs[:10]
+        _, traj = output
+        ctx.mark_non_differentiable(traj)
+        ctx.program, ctx.states, ctx.launch = program, states, launch
+        # Values for the kernels, taken outside any function transform.
+        with torch._C._DisableFuncTorch():
+            ctx.tissue = _detached_maps(t1, t2, m0, b1, inv)
+            ctx.keep = [None if x is None else _unwrapped(x).detach().contiguous()
+                        for x in (b1_phase, b0)]
+        ctx.save_for_backward(traj)
+
+    @staticmethod
+    def jvp(ctx, _program, _states, _launch, dt1, dt2, dm0, db1, dinv, db1_phase, db0, dflip,
+            ddur, dphase):
+        def flat(x):
+            return None if x is None else _unwrapped(x).detach().reshape(-1)
+
+        with torch._C._DisableFuncTorch():
+            direction = {k: flat(v) for k, v in (("t1_ms", dt1), ("t2_ms", dt2), ("m0", dm0),
+                                                 ("b1", db1), ("inversion", dinv),
+                                                 ("duration_s", ddur), ("flip_rad", dflip))
+                         if v is not None}
+            offaxis_direction = {k: flat(v) for k, v in (("b1_phase_rad", db1_phase),
+                                                         ("b0_hz", db0), ("phase_rad", dphase))
+                                 if v is not None}
+            out = tangent_complex(ctx.program, ctx.tissue, ctx.states,
+                                  _offaxis_of(ctx.keep), direction=direction,
+                                  offaxis_direction=offaxis_direction, launch=ctx.launch)
+        return out, None
+
+    @staticmethod
+    def backward(ctx, grad_out, _grad_traj):
         (traj,) = ctx.saved_tensors
         tissue, program = ctx.tissue, ctx.program
         need = ctx.needs_input_grad
@@ -933,12 +980,9 @@ class EpgComplexFunction(torch.autograd.Function):
         for i, name in enumerate(("flip_rad", "duration_s", "phase_rad")):
             if need[10 + i]:
                 grads[name] = torch.zeros(ev_shape, dtype=torch.float32, device=dev)
-        keep = ctx.keep
-        off = _native.Offaxis(None if keep[0] is None else keep[0].data_ptr(),
-                              None if keep[1] is None else keep[1].data_ptr())
         # The output is 1j * s: the cotangent of s is -1j times the output's.
-        adjoint_complex(program, tissue, ctx.states, -1j * grad_out, traj, grads, off,
-                        launch=ctx.launch)
+        adjoint_complex(program, tissue, ctx.states, -1j * grad_out, traj, grads,
+                        _offaxis_of(ctx.keep), launch=ctx.launch)
         out = [None, None, None]
         out += [grads.get(n) for n in names]
         out += [grads.get(n) for n in ("flip_rad", "duration_s", "phase_rad")]
@@ -952,14 +996,18 @@ class EpgFunction(torch.autograd.Function):
     The role of the reference's ``_NativeEpg`` (sequence/_accelerators.py:
     1402-1594): inputs are the flat tissue maps and the event-level flip and
     duration buffers of the program (for gradient routing only: their values
-    are baked into ``program``); the output is the complex64 signal
-    ``(trains*voxels, outputs)``. The backward is itself differentiable
-    (:class:`EpgVjpFunction`): a second backward through it, as a
-    Hessian-vector product takes, runs the second-order sweep.
+    are baked into ``program``); the outputs are the complex64 signal
+    ``(trains*voxels, outputs)`` and, not differentiable, the stored
+    checkpoints and the segment length they were taken with. The backward is
+    itself differentiable (:class:`EpgVjpFunction`): a second backward
+    through it, as a Hessian-vector product takes, runs the second-order
+    sweep. Forward mode (``jvp``: ``torch.func.jvp`` and dual tensors; the
+    reference's ``_NativeEpg.jvp``, :1512-1535) runs one general tangent
+    sweep along all the inputs' tangents at once.
     """
 
     @staticmethod
-    def forward(ctx, program, states, launch, t1, t2, m0, b1, inv, flip_events, duration_events):
+    def forward(program, states, launch, t1, t2, m0, b1, inv, flip_events, duration_events):
         tissue = _detached_maps(t1, t2, m0, b1, inv)
         c, ck_bytes, _ = adjoint_plan(program, tissue.voxels, states, launch,
                                       segment_for(program, tissue.voxels, states, launch))
@@ -967,15 +1015,39 @@ class EpgFunction(torch.autograd.Function):
         out = torch.empty((program.trains * tissue.voxels, program.outputs), dtype=torch.complex64,
                           device=t1.device)
         forward_checkpointed(program, tissue, states, c, ckpt, out=out, launch=launch)
-        ctx.program, ctx.states, ctx.launch, ctx.c = program, states, launch, c
-        ctx.tissue = tissue
-        given = (t1, t2, m0, b1, inv, flip_events, duration_events)
-        ctx.present = tuple(x is not None for x in given)
-        ctx.save_for_backward(ckpt, *(x for x in given if x is not None))
-        return out
+        return out, ckpt, torch.tensor(c)
 
     @staticmethod
-    def backward(ctx, grad_out):
+    def setup_context(ctx, inputs, output):
+        program, states, launch = inputs[:3]
+        given = inputs[3:]
+        _, ckpt, c = output
+        ctx.mark_non_differentiable(ckpt, c)
+        ctx.program, ctx.states, ctx.launch, ctx.c = program, states, launch, int(c)
+        # Values for the kernels, taken outside any function transform.
+        with torch._C._DisableFuncTorch():
+            ctx.tissue = _detached_maps(*given[:5])
+        ctx.present = tuple(x is not None for x in given)
+        ctx.save_for_backward(ckpt, *(x for x in given if x is not None))
+
+    @staticmethod
+    def jvp(ctx, _program, _states, _launch, dt1, dt2, dm0, db1, dinv, dflip, ddur):
+        rows = ctx.program.trains * ctx.tissue.voxels
+        with torch._C._DisableFuncTorch():
+            tangents = [None if x is None else _unwrapped(x).detach()
+                        for x in (dt1, dt2, dm0, db1, dinv, dflip, ddur)]
+            if all(x is None for x in tangents) or rows == 0:
+                return (torch.zeros((rows, ctx.program.outputs), dtype=torch.complex64,
+                                    device=ctx.tissue.t1.device), None, None)
+            dt1, dt2, dm0, db1, dinv, dflip, ddur = tangents
+            imag = tangent(ctx.program, ctx.tissue, ctx.states, t1=dt1, t2=dt2, m0=dm0, b1=db1,
+                           inv=dinv, duration=ddur, flip=dflip, launch=ctx.launch)
+            # The signal is 1j times the recorded i m0 F+[0]: its tangent is
+            # minus the tangent's imaginary plane, on the real axis.
+            return torch.complex(-imag, torch.zeros_like(imag)), None, None
+
+    @staticmethod
+    def backward(ctx, grad_out, _grad_ckpt, _grad_c):
         saved = list(ctx.saved_tensors)
         ckpt = saved.pop(0)
         inputs = [saved.pop(0) if present else None for present in ctx.present]

@@ -23,10 +23,35 @@ from typing import Any
 
 import numpy as np
 import torch
+from torch.autograd import forward_ad
 
 from . import engine
 from .sequence import (POST_SHIFT, PRE_SHIFT, SHIFT_AFTER, PackedEvents, fse_events, mrf_events,
                        mrf_gradient_map, mrf_stream_on_device, played_flip_torch, program_for)
+
+
+def _tracked(value: Any) -> bool:
+    """A tensor that autograd follows: one that requires grad (with grad
+    mode on), or one carrying a forward-mode tangent (``torch.func.jvp``,
+    ``torch.autograd.forward_ad`` dual tensors)."""
+    if not isinstance(value, torch.Tensor):
+        return False
+    if value.requires_grad and torch.is_grad_enabled():
+        return True
+    if torch._C._functorch.is_functorch_wrapped_tensor(value):
+        return True
+    return forward_ad.unpack_dual(value).tangent is not None
+
+
+def _primal(value: Any) -> Any:
+    """A tensor's value without any function-transform wrapper around it
+    (``torch.func.jvp`` wraps its inputs), for the host-side steps that read
+    values: packing the event stream, the real-subspace verdict."""
+    if not isinstance(value, torch.Tensor):
+        return value
+    while torch._C._functorch.is_functorch_wrapped_tensor(value):
+        value = torch._C._functorch.get_unwrapped(value)
+    return value.detach()
 
 
 def _tensorish(value: Any) -> bool:
@@ -63,7 +88,7 @@ def _nonzero(value: Any) -> bool:
     if value is None:
         return False
     if isinstance(value, torch.Tensor):
-        return bool(value.ne(0).any())
+        return bool(_primal(value).ne(0).any())
     return bool(np.any(np.asarray(value) != 0))
 
 
@@ -238,9 +263,7 @@ class _EpgSimulator:
         Differentiable: when a property or a sequence argument requires grad,
         the result carries a backward that runs the checkpointed adjoint
         kernel (``engine.EpgFunction``)."""
-        if torch.is_grad_enabled() and any(
-                isinstance(v, torch.Tensor) and v.requires_grad
-                for v in {**self.protocol, **values}.values()):
+        if any(_tracked(v) for v in {**self.protocol, **values}.values()):
             return self._run_differentiable(values)
         signal, _ = self._run(values, None)
         return signal
@@ -248,7 +271,7 @@ class _EpgSimulator:
     def _event_gradients(self, protocol, events, flip_ev, dur_ev, repetitions, phase_ev=None):
         """Attach the protocol's differentiable arguments to the event buffers
         (flip, duration, phase; ``(trains, events)``)."""
-        if any(isinstance(v, torch.Tensor) and v.requires_grad for v in protocol.values()):
+        if any(_tracked(v) for v in protocol.values()):
             raise NotImplementedError(
                 f"{type(self).__name__}: gradients w.r.t. its sequence arguments are not built")
         return flip_ev, dur_ev, phase_ev
@@ -261,14 +284,17 @@ class _EpgSimulator:
         home = _home(values)
         dev = engine.require_cuda(torch.device(device) if device is not None else
                                   (home if home.type == "cuda" else None))
-        plain = {k: (v.detach() if isinstance(v, torch.Tensor) else v) for k, v in protocol.items()}
-        on_device = self._device_stream(plain, repetitions, dev)
-        events = (on_device[0].events if on_device is not None
-                  else self.events(repetitions=repetitions, **plain))
-        complex_path = _leaves_real_subspace(events, held)
-        if complex_path and on_device is not None:
-            on_device = None
-            events = self.events(repetitions=repetitions, **plain)
+        plain = {k: _primal(v) for k, v in protocol.items()}
+        # The event stream and the verdict are values, built outside any
+        # function transform (torch.func.jvp wraps every tensor made inside).
+        with torch._C._DisableFuncTorch():
+            on_device = self._device_stream(plain, repetitions, dev)
+            events = (on_device[0].events if on_device is not None
+                      else self.events(repetitions=repetitions, **plain))
+            complex_path = _leaves_real_subspace(events, held)
+            if complex_path and on_device is not None:
+                on_device = None
+                events = self.events(repetitions=repetitions, **plain)
         if complex_path and names:
             raise NotImplementedError(
                 "a differentiable Jacobian on the complex path (RF phases, B0, B1phase) is not "
@@ -302,15 +328,16 @@ class _EpgSimulator:
             return flat(value, optional=False)
 
         with torch.cuda.device(dev):
-            if on_device is not None and not complex_path:
-                program, flip_ev, dur_ev = on_device
-                phase_ev = torch.zeros_like(flip_ev)
-            else:
-                program = program_for(events, dev, phased=complex_path)
-                flip_ev = torch.from_numpy(events.flip).to(dev)
-                dur_ev = torch.from_numpy(events.duration).to(dev)
-                phase_ev = torch.from_numpy(np.array(
-                    np.broadcast_to(events.phase, events.duration.shape), np.float32)).to(dev)
+            with torch._C._DisableFuncTorch():
+                if on_device is not None and not complex_path:
+                    program, flip_ev, dur_ev = on_device
+                    phase_ev = torch.zeros_like(flip_ev)
+                else:
+                    program = program_for(events, dev, phased=complex_path)
+                    flip_ev = torch.from_numpy(events.flip).to(dev)
+                    dur_ev = torch.from_numpy(events.duration).to(dev)
+                    phase_ev = torch.from_numpy(np.array(
+                        np.broadcast_to(events.phase, events.duration.shape), np.float32)).to(dev)
             flip_ev, dur_ev, phase_ev = self._event_gradients(protocol, events, flip_ev, dur_ev,
                                                               repetitions, phase_ev)
             tissue = (flat(maps["T1"], True, False), flat(maps["T2"], True, False),
@@ -319,13 +346,14 @@ class _EpgSimulator:
             if complex_path:
                 signal = engine.EpgComplexFunction.apply(
                     program, states, None, *tissue, turn(maps.get("B1phase")),
-                    turn(maps.get("B0")), flip_ev, dur_ev, phase_ev)
+                    turn(maps.get("B0")), flip_ev, dur_ev, phase_ev)[0]
             elif names:
                 kernel = tuple(self._kernel_names(names))
                 signal, jac = engine.JacobianFunction.apply(program, states, kernel, None, *tissue,
                                                             flip_ev, dur_ev)
             else:
-                signal = engine.EpgFunction.apply(program, states, None, *tissue, flip_ev, dur_ev)
+                signal = engine.EpgFunction.apply(program, states, None, *tissue, flip_ev,
+                                                  dur_ev)[0]
             signal, jac = self._post(signal, jac, names, held, plain, dev)
         signal = signal.reshape(*batch, signal.shape[-1]) if batch else signal.reshape(-1)
         if jac is not None:
@@ -339,6 +367,10 @@ class _EpgSimulator:
         """Return ``(signal, jacobian)``; the Jacobian is ``(*voxels, k, samples)``
         (``(*voxels, samples)`` for a single name given as a string)."""
         names = (diff,) if isinstance(diff, str) else tuple(diff)
+        if any(_tracked(v) and not v.requires_grad
+               for v in {**self.protocol, **values}.values()):
+            raise NotImplementedError("forward-mode derivatives of a Jacobian are not built; "
+                                      "its reverse mode is")
         if torch.is_grad_enabled() and any(
                 isinstance(v, torch.Tensor) and v.requires_grad
                 for v in {**self.protocol, **values}.values()):
@@ -404,23 +436,24 @@ class MRFSimulator(_EpgSimulator):
         tr = protocol.get("TR")
         ti = protocol.get("TI", 0.0)
         n = int(torch.atleast_1d(torch.as_tensor(
-            flip.detach() if isinstance(flip, torch.Tensor) else np.asarray(flip))).numel())
+            _primal(flip) if isinstance(flip, torch.Tensor) else np.asarray(flip))).numel())
         dev = flip_ev.device
-        where = _gradient_map_on(n, repetitions, dev)
-        if isinstance(flip, torch.Tensor) and flip.requires_grad:
+        with torch._C._DisableFuncTorch():
+            where = _gradient_map_on(n, repetitions, dev)
+        if _tracked(flip):
             played = played_flip_torch(torch.atleast_1d(flip).to(dev))
             delta = (played - played.detach()).expand(repetitions, n).reshape(-1)
             flip_ev = flip_ev.index_add(1, where["flip"].reshape(-1), delta[None])
-        if isinstance(tr, torch.Tensor) and tr.requires_grad:
+        if _tracked(tr):
             spacing = torch.atleast_1d(tr).to(dev, torch.float32).expand(n) * 1e-3
             pairs = where["tr"]
             delta = (spacing - spacing.detach())[pairs[:, 1]]
             dur_ev = dur_ev.index_add(1, pairs[:, 0], delta[None])
-        if isinstance(ti, torch.Tensor) and ti.requires_grad:
+        if _tracked(ti):
             t = ti.to(dev, torch.float32).reshape(()) * 1e-3
             idx = where["ti"]
             dur_ev = dur_ev.index_add(1, idx, (t - t.detach()).expand(idx.numel())[None])
-        if isinstance(protocol.get("phases"), torch.Tensor) and protocol["phases"].requires_grad:
+        if _tracked(protocol.get("phases")):
             raise NotImplementedError("MRFSimulator: gradients w.r.t. phases are not built")
         return flip_ev, dur_ev, phase_ev
 
@@ -455,18 +488,19 @@ class FSESimulator(_EpgSimulator):
         (:func:`torchsim_gb300.sequence.fse_events`), the ADC sharing the
         pulse's phase."""
         other = [k for k in protocol if k not in ("flip", "phases")]
-        if any(isinstance(protocol[k], torch.Tensor) and protocol[k].requires_grad for k in other):
+        if any(_tracked(protocol[k]) for k in other):
             raise NotImplementedError("FSESimulator: gradients w.r.t. ESP, TR and the excitation "
                                       "are not built")
         dev = flip_ev.device
         flip = protocol.get("flip")
         n = (events.events - 1) // 3
-        pulses = torch.from_numpy(1 + 3 * np.arange(n)).to(dev)
-        if isinstance(flip, torch.Tensor) and flip.requires_grad:
+        with torch._C._DisableFuncTorch():
+            pulses = torch.from_numpy(1 + 3 * np.arange(n)).to(dev)
+        if _tracked(flip):
             played = played_flip_torch(torch.atleast_1d(flip).to(dev))
             flip_ev = flip_ev.index_add(1, pulses, (played - played.detach())[None])
         phases = protocol.get("phases")
-        if isinstance(phases, torch.Tensor) and phases.requires_grad and phase_ev is not None:
+        if _tracked(phases) and phase_ev is not None:
             turn = torch.deg2rad(torch.atleast_1d(phases).to(dev, torch.float32)).expand(n)
             delta = (turn - turn.detach())[None]
             phase_ev = phase_ev.index_add(1, pulses, delta).index_add(1, pulses + 1, delta)
