@@ -262,7 +262,9 @@ class _EpgSimulator:
 
         Differentiable: when a property or a sequence argument requires grad,
         the result carries a backward that runs the checkpointed adjoint
-        kernel (``engine.EpgFunction``)."""
+        kernel (``engine.EpgFunction``); when one carries a forward-mode
+        tangent (``torch.func.jvp``, dual tensors), its tangent comes from one
+        general tangent sweep."""
         if any(_tracked(v) for v in {**self.protocol, **values}.values()):
             return self._run_differentiable(values)
         signal, _ = self._run(values, None)
