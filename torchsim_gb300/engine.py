@@ -937,6 +937,8 @@ class EpgComplexFunction(torch.autograd.Function):
         program, states, launch, t1, t2, m0, b1, inv, b1_phase, b0 = inputs[:10]
         _, traj = output
         ctx.mark_non_differentiable(traj)
+        # No zero-filled stand-in for the trajectory's (absent) gradient.
+        ctx.set_materialize_grads(False)
         ctx.program, ctx.states, ctx.launch = program, states, launch
         # Values for the kernels, taken outside any function transform.
         with torch._C._DisableFuncTorch():
@@ -966,6 +968,8 @@ class EpgComplexFunction(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, grad_out, _grad_traj):
+        if grad_out is None:
+            return (None,) * 13
         (traj,) = ctx.saved_tensors
         tissue, program = ctx.tissue, ctx.program
         need = ctx.needs_input_grad
@@ -1023,6 +1027,8 @@ class EpgFunction(torch.autograd.Function):
         given = inputs[3:]
         _, ckpt, c = output
         ctx.mark_non_differentiable(ckpt, c)
+        # No zero-filled stand-in for the checkpoints' (absent) gradient.
+        ctx.set_materialize_grads(False)
         ctx.program, ctx.states, ctx.launch, ctx.c = program, states, launch, int(c)
         # Values for the kernels, taken outside any function transform.
         with torch._C._DisableFuncTorch():
@@ -1048,6 +1054,8 @@ class EpgFunction(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, grad_out, _grad_ckpt, _grad_c):
+        if grad_out is None:
+            return (None,) * 10
         saved = list(ctx.saved_tensors)
         ckpt = saved.pop(0)
         inputs = [saved.pop(0) if present else None for present in ctx.present]
