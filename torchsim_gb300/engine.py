@@ -797,10 +797,15 @@ class JacobianFunction(torch.autograd.Function):
         ctx.tissue, ctx.with_m0, ctx.order = tissue, with_m0, order
         ctx.save_for_backward(traj, ws)
         ctx.present = (m0 is not None, b1 is not None, inv is not None)
+        # An unused signal (a cost of the Jacobian alone) has no cotangent:
+        # the reverse sweep then seeds the derivative columns only.
+        ctx.set_materialize_grads(False)
         return sig, jac
 
     @staticmethod
     def backward(ctx, grad_sig, grad_jac):
+        if grad_sig is None and grad_jac is None:
+            return (None,) * 11
         traj, ws = ctx.saved_tensors
         tissue, program = ctx.tissue, ctx.program
         need = ctx.needs_input_grad
