@@ -211,3 +211,33 @@ def test_free_variables_match_the_reference(golden):
     # And the reference's inverse takes them back (inside the edge clamps).
     inside = np.abs(d["back"] - d["natural"]) <= 1e-6 * np.maximum(1.0, np.abs(d["natural"]))
     assert inside.mean() > 0.95
+
+
+def test_autodiff_routing_sees_every_kind_of_tracked_tensor():
+    """The simulators take the differentiable route for a tensor that
+    requires grad, one inside torch.func.jvp and a forward-AD dual tensor, and
+    read the values of each on the host outside the transform."""
+    import torch
+    import torch.autograd.forward_ad as fwAD
+
+    from torchsim_gb300.simulators import _primal, _tracked
+
+    x = torch.arange(4, dtype=torch.float32)
+    assert not _tracked(x) and not _tracked(1.0) and not _tracked(None)
+    assert _tracked(x.clone().requires_grad_())
+    with torch.no_grad():
+        assert not _tracked(x.clone().requires_grad_())
+    seen = {}
+
+    def inside(a):
+        seen["tracked"] = _tracked(a)
+        with torch._C._DisableFuncTorch():
+            seen["values"] = _primal(a).numpy().copy()
+        return a * 2
+
+    torch.func.jvp(inside, (x,), (torch.ones(4),))
+    assert seen["tracked"] and np.array_equal(seen["values"], x.numpy())
+    with fwAD.dual_level():
+        d = fwAD.make_dual(x, torch.ones(4))
+        assert _tracked(d)
+        assert np.array_equal(_primal(d).numpy(), x.numpy())
