@@ -467,6 +467,12 @@ def run_gpu(args, rank: int, world: int, dist) -> dict | None:
     if not args.skip_match:
         line["dictionary_match"] = match_section(torch, device, voxels=args.match_voxels)
     if not args.skip_e2e:
+        # Start from a clean allocator state: the sections above leave tens
+        # of GB of cached device blocks and host garbage behind.
+        import gc
+
+        gc.collect()
+        torch.cuda.empty_cache()
         line["e2e"] = measure_e2e()
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
