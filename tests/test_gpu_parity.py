@@ -406,3 +406,27 @@ def test_dropin_several_trains(built_library, cuda):
                                                  E, S, 30, 1, FEATURES))
     p = O.Packed(t1, t2, dur, base.kind, flip, base.action, base.output_index, S, b1=b1)
     assert max_rel(out_i, O.forward(p, "f64")) <= SIGNAL_TOL
+
+
+def test_dropin_simulate_in_chunks(built_library, cuda, golden):
+    """A single-train drop-in call large enough to run in chunks (65,536
+    atoms x 880 samples, rows three samples wider than the program's
+    outputs): every chunk's rows equal the fixture's reference forward, the
+    real plane and the extra columns are zero."""
+    from torchsim_gb300 import _native
+
+    d = golden("mrf880")
+    tissue, events = _packed_arrays(d)
+    reps = 8192
+    V, P, W = 8 * reps, 880, 883
+    tissue = [np.ascontiguousarray(np.tile(a, reps)) if a.size == 8 else a for a in tissue]
+    out_r = np.full((V, W), 7.0, np.float32)
+    out_i = np.full((V, W), 7.0, np.float32)
+    arrays = [*tissue, *events, out_r, out_i, *([None] * 13)]
+    ptrs = _pointer_array(arrays)
+    _native.check(built_library.tsg_epg_simulate(ptrs, len(arrays), V, 1, d["event_kind"].size, 10,
+                                                 W, 1, FEATURES))
+    assert not out_r.any()
+    assert not out_i[:, P:].any()
+    want = np.tile(d["raw_forward"].imag, (reps, 1))
+    assert max_rel(out_i[:, :P], want) <= SIGNAL_TOL

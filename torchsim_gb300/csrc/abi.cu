@@ -625,6 +625,97 @@ int check_subset(void* const* ptrs, int64_t count, int64_t expected, int tail_be
 
 std::mutex g_dropin_mutex;
 
+// Output bytes (both planes) per chunk of a chunked drop-in call.
+constexpr size_t kDropinChunkBytes = size_t(64) << 20;
+
+// The forward of a single-train drop-in call in chunks of atoms: chunk c is
+// swept on one stream into device slot c % 2 (both planes zeroed first: the
+// caller's rows may be wider than the program's outputs), and copied to the
+// caller's planes on a second stream while chunk c + 1 is swept. Both
+// streams are blocking, so they order after the uploads on the caller's
+// stream `s` and before what it does next.
+int simulate_chunked(tsg_program* prog, const tsg_tissue& tissue, const tsg_offaxis& off,
+                     bool complex_path, int64_t atoms, int64_t states, size_t row_bytes,
+                     float* out_real, float* out_imag, std::vector<void*>& owned,
+                     cudaStream_t s) {
+    const int64_t per_chunk =
+        std::max<int64_t>(1, int64_t(kDropinChunkBytes / (2 * row_bytes)));
+    const int64_t chunks = (atoms + per_chunk - 1) / per_chunk;
+    const size_t slot_bytes = size_t(per_chunk) * row_bytes;
+    void* planes[2][2] = {};
+    for (int slot = 0; slot < 2; ++slot)
+        for (int pl = 0; pl < 2; ++pl) {
+            int rc = dense_device(slot_bytes, owned, &planes[slot][pl], s);
+            if (rc) return rc;
+        }
+    cudaStream_t sc = nullptr, sk = nullptr;
+    cudaEvent_t done[2] = {}, freed[2] = {};
+    int rc = TSG_OK;
+    auto check = [&](cudaError_t e, const char* what) {
+        if (!rc && e != cudaSuccess) rc = cuda_fail(e, what);
+    };
+    check(cudaStreamCreate(&sc), "cudaStreamCreate");
+    check(cudaStreamCreate(&sk), "cudaStreamCreate");
+    for (int i = 0; i < 2; ++i) {
+        check(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming), "cudaEventCreate");
+        check(cudaEventCreateWithFlags(&freed[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    auto sweep = [&](int64_t c) {
+        const int slot = int(c & 1);
+        const int64_t a = c * per_chunk;
+        const int64_t n = std::min(per_chunk, atoms - a);
+        if (c >= 2) check(cudaStreamWaitEvent(sc, freed[slot], 0), "cudaStreamWaitEvent");
+        check(cudaMemsetAsync(planes[slot][0], 0, size_t(n) * row_bytes, sc), "cudaMemsetAsync");
+        check(cudaMemsetAsync(planes[slot][1], 0, size_t(n) * row_bytes, sc), "cudaMemsetAsync");
+        auto at = [&](const float* p) -> const float* { return p ? p + a : nullptr; };
+        tsg_tissue part{at(tissue.t1_ms), at(tissue.t2_ms), at(tissue.m0), at(tissue.b1),
+                        at(tissue.inversion)};
+        float* pr = static_cast<float*>(planes[slot][0]);
+        float* pi = static_cast<float*>(planes[slot][1]);
+        if (!rc) {
+            if (complex_path) {
+                tsg_offaxis poff{at(off.b1_phase_rad), at(off.b0_hz)};
+                rc = tsg_epg_forward_complex(prog, &part, &poff, n, states, TSG_LAYOUT_PLANES, pr,
+                                             pi, nullptr, sc);
+            } else {
+                rc = tsg_epg_forward(prog, &part, n, states, TSG_LAYOUT_PLANES, pr, pi, nullptr,
+                                     sc);
+            }
+        }
+        check(cudaEventRecord(done[slot], sc), "cudaEventRecord");
+    };
+    auto copy_back = [&](int64_t c) {
+        const int slot = int(c & 1);
+        const int64_t a = c * per_chunk;
+        const int64_t n = std::min(per_chunk, atoms - a);
+        const size_t off_bytes = size_t(a) * row_bytes, bytes = size_t(n) * row_bytes;
+        check(cudaStreamWaitEvent(sk, done[slot], 0), "cudaStreamWaitEvent");
+        check(cudaMemcpyAsync(reinterpret_cast<char*>(out_real) + off_bytes, planes[slot][0],
+                              bytes, cudaMemcpyDeviceToHost, sk),
+              "cudaMemcpyAsync(outputs)");
+        check(cudaMemcpyAsync(reinterpret_cast<char*>(out_imag) + off_bytes, planes[slot][1],
+                              bytes, cudaMemcpyDeviceToHost, sk),
+              "cudaMemcpyAsync(outputs)");
+        check(cudaEventRecord(freed[slot], sk), "cudaEventRecord");
+    };
+    if (!rc) sweep(0);
+    for (int64_t c = 0; c < chunks && !rc; ++c) {
+        // The next chunk's sweep goes out before this chunk's copies, which
+        // may hold the host until they finish (pageable destinations).
+        if (c + 1 < chunks) sweep(c + 1);
+        copy_back(c);
+    }
+    if (sk) check(cudaStreamSynchronize(sk), "cudaStreamSynchronize");
+    if (sc) check(cudaStreamSynchronize(sc), "cudaStreamSynchronize");
+    for (int i = 0; i < 2; ++i) {
+        if (done[i]) cudaEventDestroy(done[i]);
+        if (freed[i]) cudaEventDestroy(freed[i]);
+    }
+    if (sc) cudaStreamDestroy(sc);
+    if (sk) cudaStreamDestroy(sk);
+    return rc;
+}
+
 }  // namespace
 }  // namespace tsg
 
@@ -677,6 +768,24 @@ extern "C" int tsg_epg_simulate(void* const* pointers, int64_t pointer_count, in
         if (!rc) rc = upload(pointers[5], abytes, owned, &b0, s);
     }
     const size_t obytes = size_t(train_count) * size_t(atom_count) * size_t(output_count) * 4;
+    const size_t row_bytes = size_t(output_count) * 4;
+    if (!rc && train_count == 1 && row_bytes > 0 && obytes > 2 * kDropinChunkBytes) {
+        // Large single-train calls: the atoms go in chunks swept into two
+        // device slots, each chunk's planes copied back while the next one
+        // is swept (the device-to-host copies bound such a call).
+        tsg_tissue tissue{static_cast<float*>(t1), static_cast<float*>(t2),
+                          static_cast<float*>(m0), static_cast<float*>(b1),
+                          static_cast<float*>(inv)};
+        tsg_offaxis off{static_cast<float*>(b1p), static_cast<float*>(b0)};
+        prog->host.outputs = output_count;
+        rc = simulate_chunked(prog, tissue, off, complex_path, atom_count, state_count,
+                              row_bytes, out_real, out_imag, owned, s);
+        free_all(owned, s);
+        cudaError_t es = cudaStreamSynchronize(s);
+        if (!rc && es != cudaSuccess) rc = cuda_fail(es, "cudaStreamSynchronize");
+        tsg_program_destroy(prog);
+        return rc;
+    }
     if (!rc) rc = dense_device(obytes, owned, &dr, s);
     if (!rc) rc = dense_device(obytes, owned, &di, s);
     if (!rc && obytes) {
