@@ -540,21 +540,11 @@ extern "C" int tsg_epg_tangent(const tsg_program* program, const tsg_tissue* tis
 namespace tsg {
 namespace {
 
-constexpr int TISSUE_COUNT = 17, EVENT_COUNT = 9, PACKED_COUNT = 26, FLOAT_COUNT = 20,
-              TAIL_COUNT = 13;
+constexpr int TISSUE_COUNT = 17, EVENT_COUNT = 9, PACKED_COUNT = TISSUE_COUNT + EVENT_COUNT,
+              FLOAT_COUNT = 20, TAIL_COUNT = 13;
 // Feature bits of the reference's mask (src/torchsim/_epg_cpu.cpp:91-98).
 constexpr int F_OFF_AXIS = 1, F_MOVING = 2, F_DIFFUSING = 4, F_TRANSMIT = 8, F_DENSITY = 16,
               F_INVERTING = 32;
-
-struct DeviceBuffer {
-    void* ptr = nullptr;
-    size_t bytes = 0;
-    void release() {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-    }
-};
 
 // Copies n host floats to a fresh device allocation.
 int upload(const void* host, size_t bytes, std::vector<void*>& owned, void** out,
@@ -617,8 +607,8 @@ int check_subset(void* const* ptrs, int64_t count, int64_t expected, int tail_be
             for (int64_t i = 0; i < atoms; ++i)
                 if (v[i] != 0.f) return fail(TSG_ERR_UNSUPPORTED, "second pools are not built");
     }
-    const int32_t* shim = static_cast<const int32_t*>(ptrs[TISSUE_COUNT + 6]);
-    (void)shim;  // a real-subspace run is single-shim: every index is row 0
+    // The shim index buffer (event slot 6) is not read: a single-pool run is
+    // single-shim, every index is row 0.
     (void)trains;
     return TSG_OK;
 }
