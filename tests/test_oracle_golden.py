@@ -340,3 +340,18 @@ def test_gn_port_matches_the_reference_estimator(golden):
         assert np.median(err) <= 1e-5, key
         assert np.quantile(err, 0.99) <= 1e-3, key
         assert err.max() <= 1e-2, key
+
+
+def test_gn_port_matches_the_reference_on_the_small_fixture(golden):
+    """The same restatement on the 16-voxel `gn_mrf` fixture, whose measured
+    signals are stored: the reference estimator's maps from its start."""
+    from oracle import gn_port
+    from torchsim_gb300.sequence import mrf_events
+
+    d = golden("gn_mrf")
+    events = mrf_events(d["flip_deg"], float(d["tr_ms"]))
+    got = gn_port.fit(events, d["measured"], d["start"], d["bounds"][:, 0], d["bounds"][:, 1],
+                      int(d["states"]), b1=d["b1"], max_iterations=20, threads=4)
+    for k, key in enumerate(("map_t1", "map_t2", "map_m0")):
+        ref = d[key].astype(np.float64)
+        assert np.max(np.abs(got.x[:, k] - ref) / np.abs(ref)) <= 2e-3, key
