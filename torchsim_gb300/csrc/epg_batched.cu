@@ -10,6 +10,12 @@
 // serves every echo-train length: voxels take floor(32/L) slots of a warp and
 // the shift's cross-lane moves respect the voxel boundaries through the lane's
 // index within its voxel, exactly as in the fixed-shape sweep.
+//
+// Two loops share the kernel: a CPMG train runs the echo loop (no op
+// decoding, the pulse in sum/difference form), any other program the general
+// op loop; both keep the relaxation as pending factors that the pulse, the
+// inversion and the record apply. 2-warp blocks at 16 orders per lane run an
+// instantiation budgeted for 10 blocks per SM.
 #include "tsg_internal.h"
 
 namespace tsg {
